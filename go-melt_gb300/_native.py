@@ -1,0 +1,176 @@
+"""ctypes binding of libgomelt.so (declared in include/gomelt.h).
+
+The library is the only compute path: if it is missing or fails to load, every
+call raises ``GomeltError``; there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgomelt.so")
+
+GM_OK, GM_ERR_ARG, GM_ERR_LAUNCH, GM_ERR_CUDA, GM_ERR_UNSUPPORTED, GM_ERR_TOO_LARGE = range(6)
+GM_F32, GM_F64 = 0, 1
+_ERRNAMES = {1: "invalid argument", 2: "kernel launch failed", 3: "CUDA runtime error",
+             4: "unsupported configuration", 5: "request exceeds a fixed capacity"}
+
+
+class GomeltError(RuntimeError):
+    pass
+
+
+vp = C.c_void_p
+
+
+class gm_props(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "k_powder", "k_bulk_a0", "k_bulk_a1", "k_fluid",
+        "cp_solid_a0", "cp_solid_a1", "cp_mushy", "cp_fluid", "rho",
+        "T_amb", "T_solidus", "T_liquidus", "T_boiling",
+        "h_conv", "emissivity", "sigma_sb", "evc", "Lev", "CM_coeff", "CT_coeff", "CP_coeff",
+        "laser_radius", "laser_depth", "laser_eta")]
+
+
+class gm_map3(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("src_nx", C.c_int), ("src_ny", C.c_int),
+                ("elem", vp * 3), ("w", vp * 3)]
+
+
+class gm_level_args(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("h", C.c_double * 3), ("origin", C.c_double * 3), ("ne_planes", C.c_int),
+        ("dt", vp), ("T_in", vp), ("T_out", vp), ("ph_in", vp), ("ph_out", vp),
+        ("substrate", C.c_longlong), ("k_arr", vp), ("rc_arr", vp), ("F_full", vp), ("corr_full", vp),
+        ("rhs_box", vp), ("box", C.c_int * 6), ("laser", vp), ("surface", C.c_int), ("bc_mode", C.c_int),
+        ("face", C.c_double * 5), ("inactive_amb", C.c_int), ("bc_new", vp), ("bc_old", vp),
+        ("bc_alpha", C.c_double), ("bc_beta", C.c_double), ("bc_map", gm_map3), ("clamp", C.c_int),
+        ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int),
+    ]
+
+
+class gm_interp_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("nterms", C.c_int), ("map", gm_map3 * 3),
+                ("src", vp * 3), ("coef", C.c_double * 3), ("base", vp), ("out", vp), ("out_term", vp),
+                ("which_term", C.c_int)]
+
+
+class gm_restrict_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("map", gm_map3), ("cidx", C.POINTER(C.c_int) * 3),
+                ("cnx", C.c_int), ("cny", C.c_int), ("fine", vp), ("coarse", vp)]
+
+
+class gm_restrict_s1_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("map", gm_map3), ("cidx", C.POINTER(C.c_int) * 3),
+                ("cnx", C.c_int), ("cny", C.c_int), ("fine_ph", C.POINTER(C.c_uint8)),
+                ("coarse_ph", C.POINTER(C.c_uint8)), ("substrate", C.c_longlong)]
+
+
+class gm_l0_args(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("idx", C.POINTER(C.c_int) * 3), ("l0_nx", C.c_longlong),
+                ("l0_ny", C.c_longlong), ("l0_s1", C.POINTER(C.c_uint8)), ("ph", C.POINTER(C.c_uint8)),
+                ("prev_ph", C.POINTER(C.c_uint8)), ("prev_lo", C.c_int * 3), ("prev_n", C.c_int * 3)]
+
+
+class gm_couple_axis(C.Structure):
+    _fields_ = [("nfe", C.c_int), ("cw", vp), ("node0", C.POINTER(C.c_int)), ("cb_lo", C.c_int),
+                ("ncb", C.c_int), ("flo", C.POINTER(C.c_int)), ("fhi", C.POINTER(C.c_int)), ("rmax", C.c_int),
+                ("H", C.c_double)]
+
+
+class gm_couple_geom(C.Structure):
+    _fields_ = [("ax", gm_couple_axis * 3)]
+
+
+class gm_couple_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("geom", gm_couple_geom), ("fine_nodes", C.c_int * 3),
+                ("fine_h", C.c_double * 3), ("T", vp), ("ph", C.POINTER(C.c_uint8)), ("substrate", C.c_longlong),
+                ("k_arr", vp), ("rc_arr", vp), ("Tp", vp), ("dTa", vp), ("dTb", vp), ("dt", vp), ("out", vp),
+                ("out_lo", C.c_int * 3), ("out_n", C.c_int * 3), ("scale", C.c_double), ("partials", vp),
+                ("partials_cap", C.c_longlong)]
+
+
+class gm_coarse_source_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("geom", gm_couple_geom), ("npos", C.c_int), ("rows", vp),
+                ("xq", C.POINTER(C.c_double) * 3), ("fine_wq", C.c_double), ("out", vp), ("out_lo", C.c_int * 3),
+                ("out_n", C.c_int * 3), ("scratch", vp), ("scratch_cap", C.c_longlong)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libgomelt.so once; raise GomeltError if it is not there."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise GomeltError(f"{LIB_PATH} not found: build it with build_lib.build() (nvcc, sm_103a)")
+        try:
+            L = C.CDLL(LIB_PATH)
+        except OSError as e:
+            raise GomeltError(f"cannot load {LIB_PATH}: {e}") from e
+        L.gm_version.restype = C.c_char_p
+        for name, args in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.gm_couple_partials_size.argtypes = [C.POINTER(gm_couple_geom)]
+        L.gm_couple_partials_size.restype = C.c_longlong
+        _lib = L
+    return _lib
+
+
+SIGNATURES = {
+    "gm_level_step": [C.POINTER(gm_level_args), C.POINTER(gm_props), vp],
+    "gm_interp": [C.POINTER(gm_interp_args), vp],
+    "gm_interp_matrix": [C.c_int, C.POINTER(gm_map3), vp, vp, vp],
+    "gm_interp_w_matrix": [C.c_int, vp, vp, vp, vp, C.c_longlong, vp],
+    "gm_restrict": [C.POINTER(gm_restrict_args), vp],
+    "gm_restrict_s1": [C.POINTER(gm_restrict_s1_args), vp],
+    "gm_l0_gather": [C.POINTER(gm_l0_args), vp],
+    "gm_l0_scatter": [C.POINTER(gm_l0_args), vp],
+    "gm_couple": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
+    "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
+}
+
+
+def check(code: int, what: str):
+    if code != GM_OK:
+        raise GomeltError(f"{what}: {_ERRNAMES.get(code, code)}")
+
+
+def call(name: str, *args):
+    check(getattr(lib(), name)(*args), name)
+
+
+def props_struct(p: dict) -> gm_props:
+    """gm_props from a SetupProperties-style dict."""
+    s = gm_props()
+    s.k_powder = float(p["k_powder"])
+    s.k_bulk_a0 = float(p["k_bulk_coeff_a0"])
+    s.k_bulk_a1 = float(p["k_bulk_coeff_a1"])
+    s.k_fluid = float(p["k_fluid_coeff_a0"])
+    s.cp_solid_a0 = float(p["cp_solid_coeff_a0"])
+    s.cp_solid_a1 = float(p["cp_solid_coeff_a1"])
+    s.cp_mushy = float(p["cp_mushy"])
+    s.cp_fluid = float(p["cp_fluid"])
+    s.rho = float(p["rho"])
+    s.T_amb = float(p["T_amb"])
+    s.T_solidus = float(p["T_solidus"])
+    s.T_liquidus = float(p["T_liquidus"])
+    s.T_boiling = float(p["T_boiling"])
+    s.h_conv = float(p["h_conv"])
+    s.emissivity = float(p["vareps"])
+    s.sigma_sb = float(p["sigma_sb"])
+    s.evc = float(p["evc"])
+    s.Lev = float(p["Lev"])
+    s.CM_coeff = float(p["CM_coeff"])
+    s.CT_coeff = float(p["CT_coeff"])
+    s.CP_coeff = float(p["CP_coeff"])
+    s.laser_radius = float(p["laser_radius"])
+    s.laser_depth = float(p["laser_depth"])
+    s.laser_eta = float(p["laser_eta"])
+    return s

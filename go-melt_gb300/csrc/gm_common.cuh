@@ -1,0 +1,168 @@
+// Shared device helpers for the GO-MELT GB300 kernels.
+//
+// Data layout (all levels): structured node grids, node-major with x fastest,
+// node id = ix + iy*nx + iz*nx*ny; element (ex,ey,ez) has corner nodes
+// (ex+ax, ey+ay, ez+az), a* in {0,1}.  This is the layout of the reference's
+// convert2XYZ (go_melt/computeFunctions.py:645-689).
+//
+// Phase byte per node: bit0 = S1 (bulk/solidified), bit1 = S2 (liquid).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "gomelt.h"
+
+namespace gm {
+
+constexpr uint8_t PH_S1 = 1;
+constexpr uint8_t PH_S2 = 2;
+
+template <typename real>
+struct Props {
+  real k_powder, k_bulk_a0, k_bulk_a1, k_fluid;  // W/(mm K)  (already /1000)
+  real cp_solid_a0, cp_solid_a1, cp_mushy, cp_fluid, rho;
+  real T_amb, T_solidus, T_liquidus, T_boiling;
+  real h_conv, sig_eps, evc, Lev, CM, CT, CP;  // surface model (reference units)
+  real Ta4;                                      // T_amb^4
+};
+
+template <typename real>
+inline Props<real> make_props(const gm_props& p) {
+  Props<real> q;
+  q.k_powder = (real)(p.k_powder / 1000.0);
+  q.k_bulk_a0 = (real)(p.k_bulk_a0 / 1000.0);
+  q.k_bulk_a1 = (real)(p.k_bulk_a1 / 1000.0);
+  q.k_fluid = (real)(p.k_fluid / 1000.0);
+  q.cp_solid_a0 = (real)p.cp_solid_a0;
+  q.cp_solid_a1 = (real)p.cp_solid_a1;
+  q.cp_mushy = (real)p.cp_mushy;
+  q.cp_fluid = (real)p.cp_fluid;
+  q.rho = (real)p.rho;
+  q.T_amb = (real)p.T_amb;
+  q.T_solidus = (real)p.T_solidus;
+  q.T_liquidus = (real)p.T_liquidus;
+  q.T_boiling = (real)p.T_boiling;
+  q.h_conv = (real)p.h_conv;
+  q.sig_eps = (real)(p.sigma_sb * p.emissivity);
+  q.evc = (real)p.evc;
+  q.Lev = (real)p.Lev;
+  q.CM = (real)p.CM_coeff;
+  q.CT = (real)p.CT_coeff;
+  q.CP = (real)p.CP_coeff;
+  q.Ta4 = (real)(p.T_amb * p.T_amb * p.T_amb * p.T_amb);
+  return q;
+}
+
+// Phase update and material properties of one node
+// (computeStateProperties, go_melt/computeFunctions.py:2567-2614):
+//   S2 = T >= T_liquidus; S3 = T_solidus < T < T_liquidus;
+//   S1 = (S1_old > 0.499) | S2, forced to 1 on substrate nodes;
+//   k  = [(1-S1)(1-S2) k_p + S1(1-S2)(a1 T + a0) + S2 k_f] / 1000
+//   rc = rho [(1-S2)(1-S3)(c1 T + c0) + S3 c_m + S2 c_f]
+// The products of 0/1 flags select exactly one term, so a select chain gives
+// the same value.
+template <typename real>
+__device__ __forceinline__ uint8_t node_props(const Props<real>& p, real T, uint8_t ph_old, bool substrate,
+                                              real& k, real& rc) {
+  const bool s2 = T >= p.T_liquidus;
+  const bool s3 = (T > p.T_solidus) && (T < p.T_liquidus);
+  const bool s1 = (ph_old & PH_S1) || s2 || substrate;
+  if (s2) {
+    k = p.k_fluid;
+  } else if (s1) {
+    k = p.k_bulk_a1 * T + p.k_bulk_a0;
+  } else {
+    k = p.k_powder;
+  }
+  real cp;
+  if (s2) {
+    cp = p.cp_fluid;
+  } else if (s3) {
+    cp = p.cp_mushy;
+  } else {
+    cp = p.cp_solid_a1 * T + p.cp_solid_a0;
+  }
+  rc = p.rho * cp;
+  return (uint8_t)((s1 ? PH_S1 : 0) | (s2 ? PH_S2 : 0));
+}
+
+// Flux into the top surface at one Gauss point [W/mm^2]
+// (computeConvRadBC, go_melt/computeFunctions.py:2263-2290).
+template <typename real>
+__device__ __forceinline__ real surface_flux(const Props<real>& p, real Tq) {
+  Tq = fmin(Tq, p.T_boiling + (real)1000);
+  const real T2 = Tq * Tq;
+  real q = p.h_conv * (p.T_amb - Tq) + p.sig_eps * (p.Ta4 - T2 * T2);
+  if (p.evc != (real)0) {
+    const real invT = (real)1 / Tq;
+    const real E_pv = p.Lev + p.cp_fluid * (Tq - p.T_amb);
+    const real MolMot = sqrt(p.CM * invT);
+    const real S = p.evc * p.CP * exp(-p.CT * (invT - (real)1 / p.T_boiling)) * MolMot * E_pv;
+    q -= S;
+  }
+  return q * (real)1e-6;
+}
+
+// Per-axis interpolation map: target index t -> source element e[t] with the
+// two linear weights (w[2t], w[2t+1]) = ((x_{e+1}-x)/h, (x-x_e)/h).
+template <typename real>
+struct AxisMap {
+  const int* e;
+  const real* w;
+};
+
+template <typename real>
+struct Map3 {
+  AxisMap<real> ax[3];
+  int src_nx, src_ny;  // source node strides
+};
+
+// Trilinear weights of the reference's compute3DN (:1361-1393) from per-axis
+// weights, with the validity rule of interpolatePointsMatrix (:1100-1102):
+// if any of the 8 weights leaves [-0.01, 1.01] all are zero, else they are
+// clipped to [0, 1].  Returns the base node id; w8 in reference node order.
+template <typename real>
+__device__ __forceinline__ int map3_weights(const Map3<real>& m, int tx, int ty, int tz, real w8[8]) {
+  const int ex = m.ax[0].e[tx], ey = m.ax[1].e[ty], ez = m.ax[2].e[tz];
+  const real x0 = m.ax[0].w[2 * tx], x1 = m.ax[0].w[2 * tx + 1];
+  const real y0 = m.ax[1].w[2 * ty], y1 = m.ax[1].w[2 * ty + 1];
+  const real z0 = m.ax[2].w[2 * tz], z1 = m.ax[2].w[2 * tz + 1];
+  w8[0] = x0 * y0 * z0;
+  w8[1] = x1 * y0 * z0;
+  w8[2] = x1 * y1 * z0;
+  w8[3] = x0 * y1 * z0;
+  w8[4] = x0 * y0 * z1;
+  w8[5] = x1 * y0 * z1;
+  w8[6] = x1 * y1 * z1;
+  w8[7] = x0 * y1 * z1;
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) ok = ok && (w8[i] >= (real)-1e-2) && (w8[i] <= (real)(1 + 1e-2));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) w8[i] = ok ? fmin(fmax(w8[i], (real)0), (real)1) : (real)0;
+  return ex + ey * m.src_nx + ez * m.src_nx * m.src_ny;
+}
+
+template <typename real>
+__device__ __forceinline__ real map3_apply(const Map3<real>& m, int tx, int ty, int tz, const real* __restrict__ u) {
+  real w8[8];
+  const int b = map3_weights(m, tx, ty, tz, w8);
+  const int sx = 1, sy = m.src_nx, sz = m.src_nx * m.src_ny;
+  return w8[0] * u[b] + w8[1] * u[b + sx] + w8[2] * u[b + sx + sy] + w8[3] * u[b + sy] + w8[4] * u[b + sz] +
+         w8[5] * u[b + sx + sz] + w8[6] * u[b + sx + sy + sz] + w8[7] * u[b + sy + sz];
+}
+
+template <typename real>
+inline Map3<real> make_map3(const gm_map3& m) {
+  Map3<real> r;
+  for (int d = 0; d < 3; ++d) {
+    r.ax[d].e = m.elem[d];
+    r.ax[d].w = (const real*)m.w[d];
+  }
+  r.src_nx = m.src_nx;
+  r.src_ny = m.src_ny;
+  return r;
+}
+
+__host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace gm

@@ -1,0 +1,449 @@
+// Fine -> coarse coupling terms and the coarse laser source.
+//
+// Replaces the products of the reference's coarse-at-fine shape tables
+// (computeCoarseFineShapeFunctions, go_melt/computeFunctions.py:1213-1358)
+// with fine-level fields and their BCOO projection:
+//   flux term  V_A -= sum_e sum_q grad Nc_A(q) . (kbar_e grad T'_e(q)) w
+//              (computeL1TprimeTerms_Part1 :2733-2810,
+//               computeL2TprimeTerms_Part1 :2857-2914,
+//               computeCoarseTprimeTerm_jax :1477-1565)
+//   mass term  V_A -= sum_e sum_q Nc_A(q) rcbar_e (T'a - T'b)_e(q) w / dt
+//              (computeL1TprimeTerms_Part2 :3057-3132,
+//               computeL2TprimeTerms_Part2 :3169-3221,
+//               computeCoarseTprimeMassTerm_jax :1396-1474)
+//   source     F_A += mean_p sum_e sum_q Nc_A(q) Q_p(q) w
+//              (computeLevelSource :2667-2730, computeSources :928-988)
+// with the reference's conventions: Nc and grad Nc are evaluated with the
+// coarse element of each quadrature point, the result is assigned to the
+// coarse nodes of quadrature point 0 of the fine element, k and rho*c enter
+// as element means of nodal values.
+//
+// Everything is separable per axis: per fine element index and Gauss side the
+// host supplies the two 1-D coarse weights (phi0, phi1), the coarse element of
+// side 0, and per coarse element the range of fine elements assigned to it.
+// One warp reduces one fine sub-box (at most 4x4x4 elements) of one coarse
+// element to 8 partial sums; a gather kernel adds the partials of the up to 8
+// coarse elements around each coarse node in a fixed order (deterministic,
+// no atomics).  The source is a sum over laser positions of rank-1 tensors of
+// 1-D factors, evaluated directly on the coarse node box.
+#include <math.h>
+
+#include "gm_common.cuh"
+
+namespace gm {
+
+constexpr int SB = 4;              // fine elements per sub-box edge
+constexpr int SBN = (SB + 1) * (SB + 1) * (SB + 1);
+
+template <typename real>
+struct CoupleAxis {
+  int nfe;
+  const real* cw;    // [(e*2+s)*2 + A]
+  const int* node0;  // [e]
+  int cb_lo, ncb;
+  const int* flo;
+  const int* fhi;
+  int nch;
+  real invH;
+};
+
+template <typename real>
+struct CoupleK {
+  int fnx, fny;
+  CoupleAxis<real> ax[3];
+  real ih[3];
+  const real* T;
+  const uint8_t* ph;
+  long long substrate;
+  const real* k_arr;
+  const real* rc_arr;
+  const real* Tp;
+  const real* dTa;
+  const real* dTb;
+  const double* dt;
+  real wq;
+  real* partials;
+  long long nitems;
+  int nchunk;
+  Props<real> p;
+};
+
+template <typename real>
+__device__ __forceinline__ real warp_sum(real v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename real>
+__global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
+  __shared__ real sTp[4][SBN], sD[4][SBN], sK[4][SBN], sC[4][SBN];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;
+  const real psi[2][2] = {{PQ, MQ}, {MQ, PQ}};  // psi[a][q]
+  const bool flux = a.Tp != nullptr, mass = a.dTa != nullptr;
+  const real wdt = mass ? a.wq / (real)(*a.dt) : (real)0;
+  const long long nw = (long long)gridDim.x * 4;
+  for (long long item = blockIdx.x * 4LL + warp; item < a.nitems; item += nw) {
+    const int chunk = (int)(item % a.nchunk);
+    long long ce = item / a.nchunk;
+    const int cx = (int)(ce % a.ax[0].ncb);
+    ce /= a.ax[0].ncb;
+    const int cy = (int)(ce % a.ax[1].ncb);
+    const int cz = (int)(ce / a.ax[1].ncb);
+    const int kx = chunk % a.ax[0].nch, ky = (chunk / a.ax[0].nch) % a.ax[1].nch,
+              kz = chunk / (a.ax[0].nch * a.ax[1].nch);
+    const int e0x = a.ax[0].flo[cx] + kx * SB, e0y = a.ax[1].flo[cy] + ky * SB, e0z = a.ax[2].flo[cz] + kz * SB;
+    const int nbx = min(a.ax[0].fhi[cx], e0x + SB) - e0x;
+    const int nby = min(a.ax[1].fhi[cy], e0y + SB) - e0y;
+    const int nbz = min(a.ax[2].fhi[cz], e0z + SB) - e0z;
+    real acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0;
+    if (nbx > 0 && nby > 0 && nbz > 0) {
+      const int mx = nbx + 1, my = nby + 1, mz = nbz + 1;
+      for (int i = lane; i < mx * my * mz; i += 32) {
+        const int lx = i % mx, ly = (i / mx) % my, lz = i / (mx * my);
+        const long long id = (e0x + lx) + (long long)(e0y + ly) * a.fnx + (long long)(e0z + lz) * a.fnx * a.fny;
+        real k, c;
+        const real T = a.T[id];
+        node_props(a.p, T, a.ph ? a.ph[id] : (uint8_t)0, id < a.substrate, k, c);
+        if (a.k_arr) {
+          k = a.k_arr[id];
+          c = a.rc_arr[id];
+        }
+        sK[warp][i] = k;
+        sC[warp][i] = c;
+        if (flux) sTp[warp][i] = a.Tp[id];
+        if (mass) sD[warp][i] = a.dTa[id] - a.dTb[id];
+      }
+      __syncwarp();
+      for (int f = lane; f < nbx * nby * nbz; f += 32) {
+        const int fx = f % nbx, fy = (f / nbx) % nby, fz = f / (nbx * nby);
+        const int ex = e0x + fx, ey = e0y + fy, ez = e0z + fz;
+        real ph[3][2][2];  // ph[d][A][s]
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+          ph[0][0][s] = a.ax[0].cw[(ex * 2 + s) * 2 + 0];
+          ph[0][1][s] = a.ax[0].cw[(ex * 2 + s) * 2 + 1];
+          ph[1][0][s] = a.ax[1].cw[(ey * 2 + s) * 2 + 0];
+          ph[1][1][s] = a.ax[1].cw[(ey * 2 + s) * 2 + 1];
+          ph[2][0][s] = a.ax[2].cw[(ez * 2 + s) * 2 + 0];
+          ph[2][1][s] = a.ax[2].cw[(ez * 2 + s) * 2 + 1];
+        }
+        int cid[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) cid[c] = (fx + (c & 1)) + (fy + ((c >> 1) & 1)) * mx + (fz + (c >> 2)) * mx * my;
+        real ks = 0, cs = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          ks += sK[warp][cid[c]];
+          cs += sC[warp][cid[c]];
+        }
+        if (flux) {
+          const real kb = ks * (real)0.125;
+          real t[8];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) t[c] = sTp[warp][cid[c]];
+          // gradients at the Gauss points: G_x depends on (qy,qz) only, etc.
+          real Gx[2][2], Gy[2][2], Gz[2][2];
+#pragma unroll
+          for (int q1 = 0; q1 < 2; ++q1)
+#pragma unroll
+            for (int q2 = 0; q2 < 2; ++q2) {
+              real gx = 0, gy = 0, gz = 0;
+#pragma unroll
+              for (int b1 = 0; b1 < 2; ++b1)
+#pragma unroll
+                for (int b2 = 0; b2 < 2; ++b2) {
+                  const real w = psi[b1][q1] * psi[b2][q2];
+                  gx += w * (t[1 + 2 * b1 + 4 * b2] - t[2 * b1 + 4 * b2]);  // (ay,az)=(b1,b2)
+                  gy += w * (t[b1 + 2 + 4 * b2] - t[b1 + 4 * b2]);          // (ax,az)
+                  gz += w * (t[b1 + 2 * b2 + 4] - t[b1 + 2 * b2]);          // (ax,ay)
+                }
+              Gx[q1][q2] = kb * a.ih[0] * gx;
+              Gy[q1][q2] = kb * a.ih[1] * gy;
+              Gz[q1][q2] = kb * a.ih[2] * gz;
+            }
+          // contraction with the coarse gradients (factor 2: the term does not
+          // depend on the Gauss side along its own axis)
+#pragma unroll
+          for (int A1 = 0; A1 < 2; ++A1)
+#pragma unroll
+            for (int A2 = 0; A2 < 2; ++A2) {
+              real X = 0, Y = 0, Z = 0;
+#pragma unroll
+              for (int q1 = 0; q1 < 2; ++q1)
+#pragma unroll
+                for (int q2 = 0; q2 < 2; ++q2) {
+                  X += ph[1][A1][q1] * ph[2][A2][q2] * Gx[q1][q2];
+                  Y += ph[0][A1][q1] * ph[2][A2][q2] * Gy[q1][q2];
+                  Z += ph[0][A1][q1] * ph[1][A2][q2] * Gz[q1][q2];
+                }
+              const real fX = (real)-2 * a.wq * a.ax[0].invH * X;
+              const real fY = (real)-2 * a.wq * a.ax[1].invH * Y;
+              const real fZ = (real)-2 * a.wq * a.ax[2].invH * Z;
+              // X -> nodes (Ax, A1=Ay, A2=Az); Y -> (A1=Ax, Ay, A2=Az); Z -> (A1=Ax, A2=Ay, Az)
+              acc[1 + 2 * A1 + 4 * A2] += fX;
+              acc[0 + 2 * A1 + 4 * A2] -= fX;
+              acc[A1 + 2 + 4 * A2] += fY;
+              acc[A1 + 0 + 4 * A2] -= fY;
+              acc[A1 + 2 * A2 + 4] += fZ;
+              acc[A1 + 2 * A2 + 0] -= fZ;
+            }
+        }
+        if (mass) {
+          const real cb = cs * (real)0.125;
+          real d[8];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) d[c] = sD[warp][cid[c]];
+          // trilinear values at the 8 Gauss points, then the coarse N contraction
+          real m[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int qx = q & 1, qy = (q >> 1) & 1, qz = q >> 2;
+            real v = 0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) v += psi[c & 1][qx] * psi[(c >> 1) & 1][qy] * psi[c >> 2][qz] * d[c];
+            m[q] = cb * v;
+          }
+#pragma unroll
+          for (int A = 0; A < 8; ++A) {
+            const int Ax = A & 1, Ay = (A >> 1) & 1, Az = A >> 2;
+            real v = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v += ph[0][Ax][q & 1] * ph[1][Ay][(q >> 1) & 1] * ph[2][Az][q >> 2] * m[q];
+            acc[A] -= wdt * v;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = warp_sum(acc[i]);
+    if (lane == 0) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) a.partials[item * 8 + i] = acc[i];
+    }
+    __syncwarp();
+  }
+}
+
+// Sum the partials onto the coarse nodes of the box and add them into an
+// output array covering the node box [ob0, ob0+on) per axis.
+template <typename real>
+__global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, int lo0, int lo1, int lo2,
+                                     const real* partials, real* out, int ob0, int ob1, int ob2, int on0, int on1,
+                                     real scale) {
+  const long long tot = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int bx = (int)(t % (ncbx + 1)), by = (int)((t / (ncbx + 1)) % (ncby + 1)),
+              bz = (int)(t / ((long long)(ncbx + 1) * (ncby + 1)));
+    real s = 0;
+    for (int cz = bz - 1; cz <= bz; ++cz) {
+      if (cz < 0 || cz >= ncbz) continue;
+      for (int cy = by - 1; cy <= by; ++cy) {
+        if (cy < 0 || cy >= ncby) continue;
+        for (int cx = bx - 1; cx <= bx; ++cx) {
+          if (cx < 0 || cx >= ncbx) continue;
+          const int A = (bx - cx) + 2 * (by - cy) + 4 * (bz - cz);
+          const long long base = (((long long)cz * ncby + cy) * ncbx + cx) * nchunk;
+          for (int c = 0; c < nchunk; ++c) s += partials[(base + c) * 8 + A];
+        }
+      }
+    }
+    const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
+    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * s;
+  }
+}
+
+// Per-position 1-D source factors on the coarse node box:
+// S[p][t] = sum_{fine e, side s assigned to coarse node t} phi_A(e,s) exp(-3 (x_q - v_p)^2 / r^2)
+template <typename real>
+__global__ void coarse_source_tables(int np, const double* rows, int n0, int n1, int n2, const double* xq0,
+                                     const double* xq1, const double* xq2, const real* cw0, const real* cw1,
+                                     const real* cw2, const int* flo0, const int* flo1, const int* flo2,
+                                     const int* fhi0, const int* fhi1, const int* fhi2, double rsq, double dsq,
+                                     real* S) {
+  const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
+  const long long tot = (long long)np * per;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int p = (int)(t / per);
+    int r = (int)(t % per);
+    int d, ncb;
+    const double* xq;
+    const real* cw;
+    const int *flo, *fhi;
+    double s2;
+    if (r < n0 + 1) {
+      d = 0; ncb = n0; xq = xq0; cw = cw0; flo = flo0; fhi = fhi0; s2 = rsq;
+    } else if (r < n0 + 1 + n1 + 1) {
+      r -= n0 + 1; d = 1; ncb = n1; xq = xq1; cw = cw1; flo = flo1; fhi = fhi1; s2 = rsq;
+    } else {
+      r -= n0 + 1 + n1 + 1; d = 2; ncb = n2; xq = xq2; cw = cw2; flo = flo2; fhi = fhi2; s2 = dsq;
+    }
+    const double v = rows[p * 7 + d];
+    double acc = 0.0;
+    for (int c = r - 1; c <= r; ++c) {
+      if (c < 0 || c >= ncb) continue;
+      const int A = r - c;
+      for (int e = flo[c]; e < fhi[c]; ++e)
+        for (int s = 0; s < 2; ++s) {
+          const double dx = xq[e * 2 + s] - v;
+          acc += (double)cw[(e * 2 + s) * 2 + A] * exp(-3.0 * dx * dx / s2);
+        }
+    }
+    S[t] = (real)acc;
+  }
+}
+
+template <typename real>
+__global__ void coarse_source_assemble(int np, const double* rows, int n0, int n1, int n2, int lo0, int lo1, int lo2,
+                                       const real* S, double cpre, real* out, int ob0, int ob1, int ob2, int on0,
+                                       int on1) {
+  const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
+  const long long tot = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int bx = (int)(t % (n0 + 1)), by = (int)((t / (n0 + 1)) % (n1 + 1)),
+              bz = (int)(t / ((long long)(n0 + 1) * (n1 + 1)));
+    real s = 0;
+    for (int p = 0; p < np; ++p) {
+      const real c = (real)(cpre * rows[p * 7 + 6]);
+      const real* Sp = S + (long long)p * per;
+      s += c * Sp[bx] * Sp[n0 + 1 + by] * Sp[n0 + 1 + n1 + 1 + bz];
+    }
+    const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
+    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += s / (real)np;
+  }
+}
+
+inline int grid1(long long n, int block = 256) {
+  long long g = (n + block - 1) / block;
+  if (g > 152 * 32) g = 152 * 32;
+  return g < 1 ? 1 : (int)g;
+}
+
+template <typename real>
+static void fill_axes(const gm_couple_geom* g, CoupleAxis<real> ax[3], int* nchunk) {
+  *nchunk = 1;
+  for (int d = 0; d < 3; ++d) {
+    ax[d].nfe = g->ax[d].nfe;
+    ax[d].cw = (const real*)g->ax[d].cw;
+    ax[d].node0 = g->ax[d].node0;
+    ax[d].cb_lo = g->ax[d].cb_lo;
+    ax[d].ncb = g->ax[d].ncb;
+    ax[d].flo = g->ax[d].flo;
+    ax[d].fhi = g->ax[d].fhi;
+    ax[d].nch = cdiv(g->ax[d].rmax, SB);
+    if (ax[d].nch < 1) ax[d].nch = 1;
+    ax[d].invH = (real)(1.0 / g->ax[d].H);
+    *nchunk *= ax[d].nch;
+  }
+}
+
+static bool geom_ok(const gm_couple_geom* g) {
+  for (int d = 0; d < 3; ++d) {
+    const gm_couple_axis& a = g->ax[d];
+    if (a.nfe < 1 || a.ncb < 1 || !a.cw || !a.flo || !a.fhi || a.rmax < 1 || !(a.H > 0)) return false;
+  }
+  return true;
+}
+
+}  // namespace gm
+
+using namespace gm;
+
+extern "C" long long gm_couple_partials_size(const gm_couple_geom* g) {
+  if (!g || !geom_ok(g)) return -1;
+  long long items = 1;
+  for (int d = 0; d < 3; ++d) items *= (long long)g->ax[d].ncb * cdiv(g->ax[d].rmax, SB);
+  return items * 8;
+}
+
+template <typename real>
+static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t st) {
+  CoupleK<real> a;
+  fill_axes<real>(&g->geom, a.ax, &a.nchunk);
+  a.fnx = g->fine_nodes[0];
+  a.fny = g->fine_nodes[1];
+  for (int d = 0; d < 3; ++d) a.ih[d] = (real)(1.0 / g->fine_h[d]);
+  a.T = (const real*)g->T;
+  a.ph = g->ph;
+  a.substrate = g->substrate;
+  a.k_arr = (const real*)g->k_arr;
+  a.rc_arr = (const real*)g->rc_arr;
+  a.Tp = (const real*)g->Tp;
+  a.dTa = (const real*)g->dTa;
+  a.dTb = (const real*)g->dTb;
+  a.dt = g->dt;
+  a.wq = (real)(g->fine_h[0] * g->fine_h[1] * g->fine_h[2] / 8.0);
+  a.partials = (real*)g->partials;
+  a.nitems = (long long)a.ax[0].ncb * a.ax[1].ncb * a.ax[2].ncb * a.nchunk;
+  a.p = make_props<real>(*pr);
+  long long blocks = (a.nitems + 3) / 4;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  couple_kernel<real><<<(int)blocks, 128, 0, st>>>(a);
+  if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
+  const int ncbx = a.ax[0].ncb, ncby = a.ax[1].ncb, ncbz = a.ax[2].ncb;
+  const long long nodes = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
+  couple_gather_kernel<real><<<grid1(nodes), 256, 0, st>>>(
+      ncbx, ncby, ncbz, a.nchunk, g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, a.partials,
+      (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1], (real)g->scale);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+static bool box_inside(const gm_couple_geom* g, const int lo[3], const int n[3]) {
+  for (int d = 0; d < 3; ++d) {
+    if (g->ax[d].cb_lo < lo[d] || g->ax[d].cb_lo + g->ax[d].ncb + 1 > lo[d] + n[d]) return false;
+  }
+  return true;
+}
+
+extern "C" int gm_couple(const gm_couple_args* g, const gm_props* p, void* stream) {
+  if (!g || !p || !geom_ok(&g->geom) || !g->T || !g->out || !g->partials) return GM_ERR_ARG;
+  if (!g->Tp && !g->dTa) return GM_ERR_ARG;
+  if ((g->dTa == nullptr) != (g->dTb == nullptr) || (g->dTa && !g->dt)) return GM_ERR_ARG;
+  if ((g->k_arr == nullptr) != (g->rc_arr == nullptr)) return GM_ERR_ARG;
+  if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
+  const long long need = gm_couple_partials_size(&g->geom);
+  if (need < 0 || need > g->partials_cap) return GM_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->dtype == GM_F32) return do_couple<float>(g, p, st);
+  if (g->dtype == GM_F64) return do_couple<double>(g, p, st);
+  return GM_ERR_ARG;
+}
+
+template <typename real>
+static int do_source(const gm_coarse_source_args* g, const gm_props* pr, cudaStream_t st) {
+  const gm_couple_geom& G = g->geom;
+  const int n0 = G.ax[0].ncb, n1 = G.ax[1].ncb, n2 = G.ax[2].ncb;
+  const long long tabs = (long long)g->npos * ((n0 + 1) + (n1 + 1) + (n2 + 1));
+  const double r = pr->laser_radius, d = pr->laser_depth;
+  coarse_source_tables<real><<<grid1(tabs), 128, 0, st>>>(
+      g->npos, g->rows, n0, n1, n2, g->xq[0], g->xq[1], g->xq[2], (const real*)G.ax[0].cw,
+      (const real*)G.ax[1].cw, (const real*)G.ax[2].cw, G.ax[0].flo, G.ax[1].flo, G.ax[2].flo, G.ax[0].fhi,
+      G.ax[1].fhi, G.ax[2].fhi, r * r, d * d, (real*)g->scratch);
+  if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
+  const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
+  const double cpre = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * g->fine_wq;
+  const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
+  coarse_source_assemble<real><<<grid1(nodes), 256, 0, st>>>(
+      g->npos, g->rows, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo, (const real*)g->scratch, cpre,
+      (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1]);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_coarse_source(const gm_coarse_source_args* g, const gm_props* p, void* stream) {
+  if (!g || !p || !geom_ok(&g->geom) || !g->rows || g->npos < 1 || !g->out || !g->scratch) return GM_ERR_ARG;
+  if (!g->xq[0] || !g->xq[1] || !g->xq[2]) return GM_ERR_ARG;
+  if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
+  const gm_couple_geom& G = g->geom;
+  const long long need = (long long)g->npos * ((G.ax[0].ncb + 1) + (G.ax[1].ncb + 1) + (G.ax[2].ncb + 1));
+  if (need > g->scratch_cap) return GM_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->dtype == GM_F32) return do_source<float>(g, p, st);
+  if (g->dtype == GM_F64) return do_source<double>(g, p, st);
+  return GM_ERR_ARG;
+}

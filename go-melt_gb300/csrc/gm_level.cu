@@ -1,0 +1,399 @@
+// Fused explicit level step (one forward-Euler step of one GO-MELT level).
+//
+// Replaces, for one level, the reference's sequence computeStateProperties ->
+// computeSourcesL3 -> computeConvRadBC -> solveMatrixFreeFE -> substitute_Tbar
+// -> assignBCs/assignBCsFine -> max(T, T_amb) (go_melt/computeFunctions.py
+// :2567-2614, :2960-3012, :2207-2301, :582-642, :1848-1865, :1568-1620).
+//
+// Scheme (identical algebra to solveMatrixFreeFE):
+//   T_new(i) = T(i) + [ sum_e R_e(i) + F(i) + Corr(i) ] / M(i)
+//   R_e = -kbar_e * K_ref * T_e,  M(i) = sum_e wq * mean_e(rho c) / dt
+// which equals (sum_e (diag(Me) - Ke) T_e + F + Corr) / sum_e Me.
+// K_ref (the exact 2x2x2-Gauss hex8 stiffness of a brick) is diagonal in the
+// 8-point Hadamard basis of the element's corner values, so K_ref*T_e is a
+// forward butterfly, 7 scalings and a backward butterfly.
+//
+// Thread mapping: a CTA of 32 x BY threads owns a 32 x BY tile of element
+// columns and marches up a range of node planes.  Node planes are staged in a
+// 3-deep shared-memory ring (T, k, rho*c, new phase).  Element corner
+// contributions are combined onto nodes without atomics: x-neighbours by warp
+// shuffle, y-neighbours through shared memory, z-neighbours by a register
+// carry from one plane to the next.  Each CTA writes 31 x (BY-1) node columns.
+#include <math.h>
+
+#include "gm_common.cuh"
+
+namespace gm {
+
+template <typename real>
+struct LevelK {
+  int nx, ny, nz, ne_planes, zchunk;
+  double ox, oy, oz, hx, hy, hz;
+  const double* dt;
+  const real* T_in;
+  real* T_out;
+  const uint8_t* ph_in;
+  uint8_t* ph_out;
+  long long substrate;
+  const real* k_arr;
+  const real* rc_arr;
+  const real* F_full;
+  const real* corr_full;
+  const real* rhs_box;
+  int box[6];
+  const double* laser;
+  int surface, bc_mode, inactive_amb, clamp;
+  real face[5];
+  const real* bc_new;
+  const real* bc_old;
+  real bc_alpha, bc_beta;
+  Map3<real> bc_map;
+  real* accum;
+  real* max_accum;
+  real lam[8];  // Hadamard-mode eigenvalues of K_ref, divided by 8
+  real wvol;    // hx*hy*hz/8
+  real w2;      // hx*hy/4
+  double rsq, dsq;
+  double src_c;  // 6*sqrt(3)*eta * rc^2 * dc * wvol  (times P)
+  Props<real> p;
+};
+
+constexpr int ZMAX = 64;
+
+template <typename real>
+__device__ __forceinline__ void bfly_fwd(real v[8]) {
+#pragma unroll
+  for (int s = 1; s < 8; s <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((i & s) == 0) {
+        const real a = v[i], b = v[i + s];
+        v[i] = a + b;
+        v[i + s] = b - a;
+      }
+    }
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void bfly_inv(real v[8]) {
+#pragma unroll
+  for (int s = 1; s < 8; s <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((i & s) == 0) {
+        const real a = v[i], b = v[i + s];
+        v[i] = a - b;
+        v[i + s] = a + b;
+      }
+    }
+  }
+}
+
+// 1-D source factor of node i: sum over the (up to two) elements touching the
+// node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
+__device__ __forceinline__ double src_factor(int i, int n, double o, double h, double v, double rsq) {
+  const double xi[2] = {-0.57735026918962576451, 0.57735026918962576451};
+  double s = 0.0;
+  for (int e = i - 1; e <= i; ++e) {
+    if (e < 0 || e >= n - 1) continue;
+    for (int q = 0; q < 2; ++q) {
+      const double xq = o + e * h + 0.5 * (1.0 + xi[q]) * h;
+      const double d = xq - v;
+      const double g = exp(-3.0 * d * d / rsq);
+      const double phi = (i == e) ? 0.5 * (1.0 - xi[q]) : 0.5 * (1.0 + xi[q]);
+      s += phi * g;
+    }
+  }
+  return s;
+}
+
+template <typename real, int BY>
+__global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> a) {
+  constexpr int TX = 32, PX = TX + 1, PY = BY + 1;
+  __shared__ real sT[3][PY][PX];
+  __shared__ real sK[3][PY][PX];
+  __shared__ real sC[3][PY][PX];
+  __shared__ uint8_t sP[3][PY][PX];
+  __shared__ real sX[2][3][BY][TX];
+  __shared__ real sSx[PX], sSy[PY], sSz[ZMAX];
+
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const long long nxy = (long long)nx * ny;
+  const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
+  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  const real dt = (real)(*a.dt);
+  const Props<real>& P = a.p;
+
+  // ---- laser source factors (separable rank-1 nodal source) ----
+  real srcP = 0;
+  if (a.laser != nullptr) {
+    const double vx = a.laser[0], vy = a.laser[1], vz = a.laser[2];
+    srcP = (real)(a.src_c * a.laser[6]);
+    for (int i = tid; i < PX + PY + (Z1 - Z0); i += TX * BY) {
+      if (i < PX) {
+        const int g = X0 - 1 + i;
+        sSx[i] = (g >= 0 && g < nx) ? (real)src_factor(g, nx, a.ox, a.hx, vx, a.rsq) : (real)0;
+      } else if (i < PX + PY) {
+        const int g = Y0 - 1 + (i - PX);
+        sSy[i - PX] = (g >= 0 && g < ny) ? (real)src_factor(g, ny, a.oy, a.hy, vy, a.rsq) : (real)0;
+      } else {
+        const int g = Z0 + (i - PX - PY);
+        sSz[i - PX - PY] = (real)src_factor(g, nz, a.oz, a.hz, vz, a.dsq);
+      }
+    }
+  }
+
+  auto load_plane = [&](int pl) {
+    const int slot = (pl + 3) % 3;
+    for (int i = tid; i < PX * PY; i += TX * BY) {
+      const int px = i % PX, py = i / PX;
+      const int gx = X0 - 1 + px, gy = Y0 - 1 + py;
+      real T = 0, k = 0, c = 0;
+      uint8_t ph = 0;
+      if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+        const long long id = gx + gy * (long long)nx + pl * nxy;
+        T = a.T_in[id];
+        const uint8_t po = a.ph_in ? a.ph_in[id] : (uint8_t)0;
+        ph = node_props(P, T, po, id < a.substrate, k, c);
+        if (a.k_arr) {
+          k = a.k_arr[id];
+          c = a.rc_arr[id];
+        }
+      }
+      sT[slot][py][px] = T;
+      sK[slot][py][px] = k;
+      sC[slot][py][px] = c;
+      sP[slot][py][px] = ph;
+    }
+  };
+
+  load_plane(Z0 - 1);
+
+  const int ex = X0 - 1 + tx, ey = Y0 - 1 + ty;
+  const bool col_ok = ex >= 0 && ex < nx - 1 && ey >= 0 && ey < ny - 1;
+  const int ix = X0 + tx, iy = Y0 + ty;
+  const bool out_col = tx < TX - 1 && ty < BY - 1 && ix < nx && iy < ny;
+  const int top_el = a.ne_planes - 1;
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
+
+  real carryU = 0, carryM = 0;
+  for (int ke = Z0 - 1; ke < Z1; ++ke) {
+    load_plane(ke + 1);
+    __syncthreads();
+    const int sl = (ke + 3) % 3, su = (ke + 4) % 3;
+
+    // ---- element (ex, ey, ke) ----
+    real R[8];
+    real me = 0;
+    const bool el_ok = col_ok && ke >= 0 && ke < a.ne_planes;
+    if (el_ok) {
+      real ks = 0, cs = 0;
+#pragma unroll
+      for (int az = 0; az < 2; ++az) {
+        const int s = az ? su : sl;
+#pragma unroll
+        for (int ay = 0; ay < 2; ++ay)
+#pragma unroll
+          for (int ax = 0; ax < 2; ++ax) {
+            R[ax + 2 * ay + 4 * az] = sT[s][ty + ay][tx + ax];
+            ks += sK[s][ty + ay][tx + ax];
+            cs += sC[s][ty + ay][tx + ax];
+          }
+      }
+      const real kbar = ks * (real)0.125;
+      me = a.wvol * (cs * (real)0.125 / dt);
+      real Tt[4];
+      if (a.surface && ke == top_el) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) Tt[i] = R[4 + i];
+      }
+      bfly_fwd(R);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) R[m] *= a.lam[m];
+      bfly_inv(R);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) R[m] = -kbar * R[m];
+      if (a.surface && ke == top_el) {
+        // top face: 2x2 Gauss points on the face of corners R[4..7]
+#pragma unroll
+        for (int qy = 0; qy < 2; ++qy)
+#pragma unroll
+          for (int qx = 0; qx < 2; ++qx) {
+            const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
+            const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
+            const real Tq = px0 * py0 * Tt[0] + px1 * py0 * Tt[1] + px0 * py1 * Tt[2] + px1 * py1 * Tt[3];
+            const real q = surface_flux(P, Tq) * a.w2;
+            R[4] += px0 * py0 * q;
+            R[5] += px1 * py0 * q;
+            R[6] += px0 * py1 * q;
+            R[7] += px1 * py1 * q;
+          }
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 8; ++m) R[m] = 0;
+    }
+
+    // ---- corners -> nodes: x by shuffle, y through shared memory ----
+    real cx[4];  // index ay + 2*az
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int ay = j & 1, az = j >> 1;
+      cx[j] = R[1 + 2 * ay + 4 * az] + __shfl_down_sync(0xffffffffu, R[2 * ay + 4 * az], 1);
+    }
+    const real mx = me + __shfl_down_sync(0xffffffffu, me, 1);
+    const int xb = (ke + 1) & 1;
+    sX[xb][0][ty][tx] = cx[0];  // ay=0, lower
+    sX[xb][1][ty][tx] = cx[2];  // ay=0, upper
+    sX[xb][2][ty][tx] = mx;
+    __syncthreads();
+    real lowN = cx[1], upN = cx[3], mN = mx;
+    if (ty + 1 < BY) {
+      lowN += sX[xb][0][ty + 1][tx];
+      upN += sX[xb][1][ty + 1][tx];
+      mN += sX[xb][2][ty + 1][tx];
+    }
+
+    // ---- finalize node plane ke ----
+    if (ke >= Z0 && out_col) {
+      const long long id = ix + iy * (long long)nx + ke * nxy;
+      real Rt = carryU + lowN;
+      const real M = carryM + mN;
+      const real Told = sT[sl][ty + 1][tx + 1];
+      const uint8_t phn = sP[sl][ty + 1][tx + 1];
+      if (a.laser != nullptr) Rt += srcP * sSx[tx + 1] * sSy[ty + 1] * sSz[ke - Z0];
+      if (a.rhs_box != nullptr && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3] &&
+          ke >= a.box[4] && ke < a.box[5]) {
+        const int bnx = a.box[1] - a.box[0], bny = a.box[3] - a.box[2];
+        Rt += a.rhs_box[(ix - a.box[0]) + (long long)(iy - a.box[2]) * bnx + (long long)(ke - a.box[4]) * bnx * bny];
+      }
+      if (a.F_full) Rt += a.F_full[id];
+      if (a.corr_full) Rt += a.corr_full[id];
+      real Tn = Told + Rt / M;
+      if (a.inactive_amb && ke > a.ne_planes) Tn = P.T_amb;
+      if (a.bc_mode == 1) {
+        if (iy == 0) Tn = a.face[2];
+        if (iy == ny - 1) Tn = a.face[3];
+        if (ix == 0) Tn = a.face[0];
+        if (ix == nx - 1) Tn = a.face[1];
+        if (ke == 0) Tn = a.face[4];
+      } else if (a.bc_mode == 2) {
+        if (ix == 0 || ix == nx - 1 || iy == 0 || iy == ny - 1 || ke == 0) {
+          real w8[8];
+          const int b = map3_weights(a.bc_map, ix, iy, ke, w8);
+          const int sx = 1, sy = a.bc_map.src_nx, sz = a.bc_map.src_nx * a.bc_map.src_ny;
+          const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+          real v = 0;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const real bc = a.bc_alpha * a.bc_new[b + off[j]] + a.bc_beta * a.bc_old[b + off[j]];
+            v += w8[j] * bc;
+          }
+          Tn = v;
+        }
+      }
+      if (a.clamp) Tn = fmax(Tn, P.T_amb);
+      a.T_out[id] = Tn;
+      if (a.ph_out) a.ph_out[id] = phn;
+      if (a.accum) {
+        const bool prev2 = a.ph_in ? (a.ph_in[id] & PH_S2) != 0 : false;
+        const bool s2 = (phn & PH_S2) != 0;
+        const real acc = a.accum[id];
+        const real racc = (s2 && !prev2) ? acc : (real)0;
+        a.max_accum[id] = fmax(racc, a.max_accum[id]);
+        a.accum[id] = (acc + dt * (s2 ? (real)1 : (real)0)) - racc;
+      }
+    }
+    carryU = upN;
+    carryM = mN;
+  }
+}
+
+template <typename real>
+static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st) {
+  LevelK<real> a;
+  a.nx = g->nx;
+  a.ny = g->ny;
+  a.nz = g->nz;
+  a.ne_planes = g->ne_planes;
+  a.ox = g->origin[0];
+  a.oy = g->origin[1];
+  a.oz = g->origin[2];
+  a.hx = g->h[0];
+  a.hy = g->h[1];
+  a.hz = g->h[2];
+  a.dt = g->dt;
+  a.T_in = (const real*)g->T_in;
+  a.T_out = (real*)g->T_out;
+  a.ph_in = g->ph_in;
+  a.ph_out = g->ph_out;
+  a.substrate = g->substrate;
+  a.k_arr = (const real*)g->k_arr;
+  a.rc_arr = (const real*)g->rc_arr;
+  a.F_full = (const real*)g->F_full;
+  a.corr_full = (const real*)g->corr_full;
+  a.rhs_box = (const real*)g->rhs_box;
+  for (int i = 0; i < 6; ++i) a.box[i] = g->box[i];
+  a.laser = g->laser;
+  a.surface = g->surface;
+  a.bc_mode = g->bc_mode;
+  a.inactive_amb = g->inactive_amb;
+  a.clamp = g->clamp;
+  for (int i = 0; i < 5; ++i) a.face[i] = (real)g->face[i];
+  a.bc_new = (const real*)g->bc_new;
+  a.bc_old = (const real*)g->bc_old;
+  a.bc_alpha = (real)g->bc_alpha;
+  a.bc_beta = (real)g->bc_beta;
+  a.bc_map = make_map3<real>(g->bc_map);
+  a.accum = (real*)g->accum;
+  a.max_accum = (real*)g->max_accum;
+  a.p = make_props<real>(*pr);
+  const double hx = g->h[0], hy = g->h[1], hz = g->h[2];
+  for (int m = 0; m < 8; ++m) {
+    const int mx = m & 1, my = (m >> 1) & 1, mz = (m >> 2) & 1;
+    const double Mx = mx ? hx / 6 : hx / 2, My = my ? hy / 6 : hy / 2, Mz = mz ? hz / 6 : hz / 2;
+    const double Kx = mx ? 2 / hx : 0, Ky = my ? 2 / hy : 0, Kz = mz ? 2 / hz : 0;
+    a.lam[m] = (real)((Kx * My * Mz + Mx * Ky * Mz + Mx * My * Kz) / 8.0);
+  }
+  a.wvol = (real)(hx * hy * hz / 8.0);
+  a.w2 = (real)(hx * hy / 4.0);
+  const double r = pr->laser_radius, d = pr->laser_depth;
+  a.rsq = r * r;
+  a.dsq = d * d;
+  const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
+  a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
+
+  constexpr int BY = 8;
+  const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, BY - 1);
+  int zc = g->zchunk;
+  if (zc <= 0) {
+    const int want = 2 * 152;
+    int chunks = cdiv(want, gx * gy);
+    chunks = chunks < 1 ? 1 : (chunks > a.nz ? a.nz : chunks);
+    zc = cdiv(a.nz, chunks);
+  }
+  if (zc > ZMAX) zc = ZMAX;
+  if (zc < 1) zc = 1;
+  a.zchunk = zc;
+  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(32, BY);
+  level_step_kernel<real, BY><<<grid, block, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+}  // namespace gm
+
+extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream) {
+  if (!a || !p || !a->T_in || !a->T_out || !a->dt || a->T_in == a->T_out) return GM_ERR_ARG;
+  if (a->nx < 2 || a->ny < 2 || a->nz < 2 || a->ne_planes < 0 || a->ne_planes > a->nz - 1) return GM_ERR_ARG;
+  if ((a->k_arr == nullptr) != (a->rc_arr == nullptr)) return GM_ERR_ARG;
+  if (a->bc_mode == 2 && (!a->bc_new || !a->bc_old || !a->bc_map.elem[0] || !a->bc_map.w[0])) return GM_ERR_ARG;
+  if ((a->accum == nullptr) != (a->max_accum == nullptr)) return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a->dtype == GM_F32) return gm::launch_level<float>(a, p, st);
+  if (a->dtype == GM_F64) return gm::launch_level<double>(a, p, st);
+  return GM_ERR_ARG;
+}
+
+extern "C" const char* gm_version(void) { return "gomelt-gb300 0.1 (sm_103a)"; }

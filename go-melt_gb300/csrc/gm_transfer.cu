@@ -1,0 +1,284 @@
+// Inter-level transfer kernels: prolongation (gather), restriction + T',
+// Level-1 S1 restriction and the Level-0 phase store gather/scatter.
+//
+// All maps are separable: a target point (i,j,k) of a tensor grid of points is
+// located in the source grid by three per-axis tables (gm_map3), so no kernel
+// stores or reads an 8-weight-per-point matrix.
+#include "gm_common.cuh"
+
+namespace gm {
+
+template <typename real>
+struct InterpK {
+  int n[3];
+  int nterms;
+  Map3<real> map[3];
+  const real* src[3];
+  real coef[3];
+  const real* base;
+  real* out;
+  real* out_term;
+  int which_term;
+};
+
+// out[t] = base[t] + sum_k coef_k * I_k(src_k)[t]; optionally out_term = I_which.
+// interpolatePoints / interpolate_w_matrix (computeFunctions.py:1110-1210),
+// the T' of getNewTprime (:2097) and the field remap of moveEverything
+// (:2427-2459).
+template <typename real>
+__global__ void interp_kernel(const InterpK<real> a) {
+  const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % a.n[0]);
+    const int j = (int)((t / a.n[0]) % a.n[1]);
+    const int k = (int)(t / ((long long)a.n[0] * a.n[1]));
+    real acc = a.base ? a.base[t] : (real)0;
+    for (int q = 0; q < a.nterms; ++q) {
+      const real v = map3_apply(a.map[q], i, j, k, a.src[q]);
+      if (a.out_term && q == a.which_term) a.out_term[t] = v;
+      acc = acc + a.coef[q] * v;
+    }
+    a.out[t] = acc;
+  }
+}
+
+// Materialised weights (interpolatePointsMatrix, :1028-1107).
+template <typename real>
+__global__ void interp_matrix_kernel(const Map3<real> m, int n0, int n1, int n2, real* Nc, int* node) {
+  const long long tot = (long long)n0 * n1 * n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    real w8[8];
+    const int b = map3_weights(m, i, j, k, w8);
+    const int sx = 1, sy = m.src_nx, sz = m.src_nx * m.src_ny;
+    const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      Nc[t * 8 + q] = w8[q];
+      node[t * 8 + q] = b + off[q];
+    }
+  }
+}
+
+// interpolate_w_matrix (:1110-1128) with stored weights.
+template <typename real>
+__global__ void w_matrix_kernel(const real* Nc, const int* node, const real* T, real* out, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    real s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += Nc[t * 8 + q] * T[node[t * 8 + q]];
+    out[t] = s;
+  }
+}
+
+// Restriction (getNewTprime, :2085-2093): coarse[idx] = fine field evaluated at
+// the coordinates of the coarse nodes inside the fine window.
+template <typename real>
+__global__ void restrict_kernel(int n0, int n1, int n2, const Map3<real> m, const int* cx, const int* cy, const int* cz,
+                                int cnx, int cny, const real* fine, real* coarse) {
+  const long long tot = (long long)n0 * n1 * n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    const real v = map3_apply(m, i, j, k, fine);
+    coarse[cx[i] + (long long)cy[j] * cnx + (long long)cz[k] * cnx * cny] = v;
+  }
+}
+
+// Level-1 S1 from Level 2 (subcycleGOMELT :3272-3278, updateStateProperties
+// :2547-2556): interpolate the 0/1 S1 of Level 2 at the Level-1 overlap nodes;
+// the stored bit is the value's use in computeStateProperties (S1 > 0.499),
+// then the substrate override.
+template <typename real>
+__global__ void restrict_s1_kernel(int n0, int n1, int n2, const Map3<real> m, const int* cx, const int* cy,
+                                   const int* cz, int cnx, int cny, const uint8_t* fine_ph, int fnx, int fny,
+                                   uint8_t* coarse_ph, long long substrate) {
+  const long long tot = (long long)n0 * n1 * n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    real w8[8];
+    const int b = map3_weights(m, i, j, k, w8);
+    const int sx = 1, sy = fnx, sz = fnx * fny;
+    const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+    real v = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v += w8[q] * (real)(fine_ph[b + off[q]] & PH_S1);
+    const long long id = cx[i] + (long long)cy[j] * cnx + (long long)cz[k] * cnx * cny;
+    const bool s1 = (v > (real)0.499) || id < substrate;
+    coarse_ph[id] = (uint8_t)((coarse_ph[id] & ~PH_S1) | (s1 ? PH_S1 : 0));
+  }
+}
+
+// Level-0 gather (moveEverything :2500-2502): window phase from the Level-0
+// S1 store; S2 from the previous window's phase where the windows overlap
+// (Level 0 holds S2 only inside the last scattered window, :2390-2392).
+__global__ void l0_gather_kernel(int n0, int n1, int n2, const int* ix, const int* iy, const int* iz, long long lnx,
+                                 long long lny, const uint8_t* l0, uint8_t* ph, const uint8_t* prev_ph, int plo0,
+                                 int plo1, int plo2, int pn0, int pn1, int pn2) {
+  const long long tot = (long long)n0 * n1 * n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    const long long id = ix[i] + iy[j] * lnx + iz[k] * lnx * lny;
+    uint8_t p = l0[id] ? PH_S1 : 0;
+    if (prev_ph) {
+      const int a = ix[i] - plo0, b = iy[j] - plo1, c = iz[k] - plo2;
+      if (a >= 0 && a < pn0 && b >= 0 && b < pn1 && c >= 0 && c < pn2)
+        p |= prev_ph[a + (long long)b * pn0 + (long long)c * pn0 * pn1] & PH_S2;
+    }
+    ph[t] = p;
+  }
+}
+
+// Level-0 scatter (subcycleGOMELT :3628-3630): store the window's S1.
+__global__ void l0_scatter_kernel(int n0, int n1, int n2, const int* ix, const int* iy, const int* iz, long long lnx,
+                                  long long lny, uint8_t* l0, const uint8_t* ph) {
+  const long long tot = (long long)n0 * n1 * n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    l0[ix[i] + iy[j] * lnx + iz[k] * lnx * lny] = (ph[t] & PH_S1) ? 1 : 0;
+  }
+}
+
+inline int grid_for(long long n, int block = 256) {
+  long long g = (n + block - 1) / block;
+  if (g > 152 * 32) g = 152 * 32;
+  return g < 1 ? 1 : (int)g;
+}
+
+template <typename real>
+static int do_interp(const gm_interp_args* g, cudaStream_t st) {
+  InterpK<real> a;
+  for (int d = 0; d < 3; ++d) a.n[d] = g->n[d];
+  a.nterms = g->nterms;
+  for (int q = 0; q < 3; ++q) {
+    if (q < g->nterms) {
+      a.map[q] = make_map3<real>(g->map[q]);
+      a.src[q] = (const real*)g->src[q];
+      a.coef[q] = (real)g->coef[q];
+    } else {
+      a.src[q] = nullptr;
+      a.coef[q] = 0;
+    }
+  }
+  a.base = (const real*)g->base;
+  a.out = (real*)g->out;
+  a.out_term = (real*)g->out_term;
+  a.which_term = g->which_term;
+  const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
+  interp_kernel<real><<<grid_for(tot), 256, 0, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+}  // namespace gm
+
+using namespace gm;
+
+static bool map_ok(const gm_map3& m, const int n[3]) {
+  for (int d = 0; d < 3; ++d)
+    if (!m.elem[d] || !m.w[d] || m.n[d] != n[d]) return false;
+  return m.src_nx > 1 && m.src_ny > 1;
+}
+
+extern "C" int gm_interp(const gm_interp_args* g, void* stream) {
+  if (!g || !g->out || g->nterms < 1 || g->nterms > 3) return GM_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (g->n[d] < 1) return GM_ERR_ARG;
+  for (int q = 0; q < g->nterms; ++q)
+    if (!g->src[q] || !map_ok(g->map[q], g->n) || g->src[q] == g->out) return GM_ERR_ARG;
+  if (g->out_term && (g->which_term < 0 || g->which_term >= g->nterms)) return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->dtype == GM_F32) return do_interp<float>(g, st);
+  if (g->dtype == GM_F64) return do_interp<double>(g, st);
+  return GM_ERR_ARG;
+}
+
+extern "C" int gm_interp_matrix(int dtype, const gm_map3* m, void* Nc, int* node, void* stream) {
+  if (!m || !Nc || !node || !map_ok(*m, m->n)) return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long tot = (long long)m->n[0] * m->n[1] * m->n[2];
+  if (dtype == GM_F32)
+    interp_matrix_kernel<float><<<grid_for(tot), 256, 0, st>>>(make_map3<float>(*m), m->n[0], m->n[1], m->n[2],
+                                                                (float*)Nc, node);
+  else if (dtype == GM_F64)
+    interp_matrix_kernel<double><<<grid_for(tot), 256, 0, st>>>(make_map3<double>(*m), m->n[0], m->n[1], m->n[2],
+                                                                 (double*)Nc, node);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_interp_w_matrix(int dtype, const void* Nc, const int* node, const void* T, void* out, long long n,
+                                  void* stream) {
+  if (!Nc || !node || !T || !out || n < 0) return GM_ERR_ARG;
+  if (n == 0) return GM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GM_F32)
+    w_matrix_kernel<float><<<grid_for(n), 256, 0, st>>>((const float*)Nc, node, (const float*)T, (float*)out, n);
+  else if (dtype == GM_F64)
+    w_matrix_kernel<double><<<grid_for(n), 256, 0, st>>>((const double*)Nc, node, (const double*)T, (double*)out, n);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_restrict(const gm_restrict_args* g, void* stream) {
+  if (!g || !g->fine || !g->coarse || !map_ok(g->map, g->n) || !g->cidx[0] || !g->cidx[1] || !g->cidx[2])
+    return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (tot == 0) return GM_OK;
+  if (g->dtype == GM_F32)
+    restrict_kernel<float><<<grid_for(tot), 256, 0, st>>>(g->n[0], g->n[1], g->n[2], make_map3<float>(g->map),
+                                                           g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
+                                                           (const float*)g->fine, (float*)g->coarse);
+  else if (g->dtype == GM_F64)
+    restrict_kernel<double><<<grid_for(tot), 256, 0, st>>>(g->n[0], g->n[1], g->n[2], make_map3<double>(g->map),
+                                                            g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
+                                                            (const double*)g->fine, (double*)g->coarse);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_restrict_s1(const gm_restrict_s1_args* g, void* stream) {
+  if (!g || !g->fine_ph || !g->coarse_ph || !map_ok(g->map, g->n) || !g->cidx[0] || !g->cidx[1] || !g->cidx[2])
+    return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (tot == 0) return GM_OK;
+  if (g->dtype == GM_F32)
+    restrict_s1_kernel<float><<<grid_for(tot), 256, 0, st>>>(
+        g->n[0], g->n[1], g->n[2], make_map3<float>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
+        g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
+  else if (g->dtype == GM_F64)
+    restrict_s1_kernel<double><<<grid_for(tot), 256, 0, st>>>(
+        g->n[0], g->n[1], g->n[2], make_map3<double>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
+        g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_l0_gather(const gm_l0_args* g, void* stream) {
+  if (!g || !g->l0_s1 || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2] || g->ph == g->prev_ph) return GM_ERR_ARG;
+  const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (tot == 0) return GM_OK;
+  l0_gather_kernel<<<grid_for(tot), 256, 0, (cudaStream_t)stream>>>(
+      g->n[0], g->n[1], g->n[2], g->idx[0], g->idx[1], g->idx[2], g->l0_nx, g->l0_ny, g->l0_s1, g->ph, g->prev_ph,
+      g->prev_lo[0], g->prev_lo[1], g->prev_lo[2], g->prev_n[0], g->prev_n[1], g->prev_n[2]);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_l0_scatter(const gm_l0_args* g, void* stream) {
+  if (!g || !g->l0_s1 || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2]) return GM_ERR_ARG;
+  const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (tot == 0) return GM_OK;
+  l0_scatter_kernel<<<grid_for(tot), 256, 0, (cudaStream_t)stream>>>(g->n[0], g->n[1], g->n[2], g->idx[0], g->idx[1],
+                                                                      g->idx[2], g->l0_nx, g->l0_ny, g->l0_s1, g->ph);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}

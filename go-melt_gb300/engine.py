@@ -1,0 +1,492 @@
+"""Multilevel engine: device state of Levels 0-3 and the hot-path sequences.
+
+``Engine.move`` is moveEverything (go_melt/computeFunctions.py:2400-2510),
+``Engine.subcycle`` is subcycleGOMELT (:3224-3632), ``Engine.step`` is
+stepGOMELT (:2304-2397) and ``Engine.dwell`` is stepGOMELTDwellTime
+(:2617-2664), each issued as a sequence of libgomelt kernels on one CUDA
+stream.  Host work per call is limited to FP64 index arithmetic and small
+per-axis tables; fields stay on the device.
+
+Device layout (per level, node-major, x fastest): T (float32 or float64),
+T' (Levels 2, 3), phase byte (bit0 S1, bit1 S2).  Level 0 keeps one byte
+(S1) per node of the part footprint at Level-3 resolution; its S2, which the
+reference stores only inside the last written window (:2390-2392), is taken
+from Level 3's phase at gather time.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+import _native as N
+import kern
+from geometry import axis_map, quad_points_1d
+from levels import Geometry
+
+PH_S1, PH_S2 = 1, 2
+
+
+class CoupleGeom:
+    """Per-axis tables of a fine level inside a coarse level (gm_couple_geom)."""
+
+    def __init__(self, fine_coords, coarse_coords, dtype, device, pad_ncb=None):
+        self.axes = []
+        self.tensors = []
+        g = N.gm_couple_geom()
+        for d in range(3):
+            xq = quad_points_1d(fine_coords[d])
+            c = np.asarray(coarse_coords[d], dtype=np.float64)
+            H = c[1] - c[0]
+            nce = c.size - 1
+            I = np.clip(np.floor((xq - c[0]) / H).astype(np.int64), 0, nce - 1)
+            cw = np.stack([(c[I + 1] - xq) / H, (xq - c[I]) / H], axis=-1)  # (nfe, 2, 2)
+            node0 = I[:, 0]
+            lo = int(node0.min())
+            ncb = int(node0.max()) - lo + 1
+            cells = lo + np.arange(ncb)
+            flo = np.searchsorted(node0, cells, side="left")
+            fhi = np.searchsorted(node0, cells, side="right")
+            rmax = int((fhi - flo).max())
+            t_cw = torch.as_tensor(cw.reshape(-1), dtype=dtype, device=device)
+            t_n0 = torch.as_tensor(node0.astype(np.int32), device=device)
+            t_flo = torch.as_tensor(flo.astype(np.int32), device=device)
+            t_fhi = torch.as_tensor(fhi.astype(np.int32), device=device)
+            t_xq = torch.as_tensor(xq.reshape(-1), dtype=torch.float64, device=device)
+            self.tensors += [t_cw, t_n0, t_flo, t_fhi, t_xq]
+            a = g.ax[d]
+            a.nfe = xq.shape[0]
+            a.cw = t_cw.data_ptr()
+            a.node0 = C.cast(t_n0.data_ptr(), C.POINTER(C.c_int))
+            a.cb_lo = lo
+            a.ncb = ncb
+            a.flo = C.cast(t_flo.data_ptr(), C.POINTER(C.c_int))
+            a.fhi = C.cast(t_fhi.data_ptr(), C.POINTER(C.c_int))
+            a.rmax = rmax
+            a.H = float(H)
+            self.axes.append(dict(lo=lo, ncb=ncb, xq=t_xq))
+        self.struct = g
+        self.box_lo = [ax["lo"] for ax in self.axes]
+        self.box_n = [ax["ncb"] + 1 for ax in self.axes]
+        self.partials = int(N.lib().gm_couple_partials_size(C.byref(g)))
+
+
+class Engine:
+    def __init__(self, solver_input: dict, props: dict, N2: int, N3: int, dtype=torch.float32, device="cuda",
+                 stream=None):
+        self.geo = Geometry(solver_input, props)
+        self.P = props
+        self.ps = N.props_struct(props)
+        self.dtype = dtype
+        self.dev = torch.device(device)
+        self.N2, self.N3 = int(N2), int(N3)
+        self.stream = stream
+        g = self.geo
+        Tamb = float(props["T_amb"])
+        f = dict(dtype=dtype, device=self.dev)
+        self.T = {lv: torch.full((g.L[lv].nn,), Tamb, **f) for lv in (1, 2, 3)}
+        self.Tp = {lv: torch.zeros(g.L[lv].nn, **f) for lv in (2, 3)}
+        self.ph = {lv: torch.zeros(g.L[lv].nn, dtype=torch.uint8, device=self.dev) for lv in (1, 2, 3)}
+        self.L0 = torch.zeros(g.L0_nn, dtype=torch.uint8, device=self.dev)
+        self.acc3 = torch.zeros(g.L[3].nn, **f)
+        self.macc3 = torch.zeros(g.L[3].nn, **f)
+        self.s2_prev_lo = None  # Level-0 start of the window last written (S2 snapshot)
+        self.substrate = g.substrate()
+        self.tmp = None
+        self._work = None
+        self.tables = None
+
+    # ------------------------------------------------------------------
+    # helpers
+    # ------------------------------------------------------------------
+    def _buf(self, name, n, dtype=None):
+        if self._work is None:
+            self._work = {}
+        t = self._work.get(name)
+        dt = dtype or self.dtype
+        if t is None or t.numel() < n or t.dtype != dt:
+            t = torch.empty(n, dtype=dt, device=self.dev)
+            self._work[name] = t
+        return t[:n]
+
+    def _map(self, src_level_coords, src_nodes, tgt_coords):
+        return kern.DeviceMap3([axis_map(src_level_coords[d], tgt_coords[d]) for d in range(3)], src_nodes,
+                               self.dtype, self.dev)
+
+    def _interp(self, terms, n, out, base=None, out_term=None, which=0):
+        a = N.gm_interp_args()
+        a.dtype = kern.dtype_code(out)
+        for d in range(3):
+            a.n[d] = int(n[d])
+        a.nterms = len(terms)
+        for q, (m, src, coef) in enumerate(terms):
+            a.map[q] = m.struct
+            a.src[q] = kern.ptr(src)
+            a.coef[q] = float(coef)
+        a.base = kern.ptr(base)
+        a.out = kern.ptr(out)
+        a.out_term = kern.ptr(out_term)
+        a.which_term = int(which)
+        N.call("gm_interp", C.byref(a), kern.stream_ptr(self.stream))
+
+    def _idx_tensor(self, arrs, nodes, what):
+        """Upload per-axis node-index arrays after checking they address the grid."""
+        for d in range(3):
+            a = np.asarray(arrs[d])
+            if a.size == 0 or a.min() < 0 or a.max() >= nodes[d]:
+                raise N.GomeltError(f"{what}: axis {d} indices [{a.min() if a.size else '-'}, "
+                                    f"{a.max() if a.size else '-'}] outside [0, {nodes[d]})")
+        return [torch.as_tensor(np.asarray(a).astype(np.int32), device=self.dev) for a in arrs]
+
+    # ------------------------------------------------------------------
+    # per-window tables (rebuilt after every move)
+    # ------------------------------------------------------------------
+    def build_tables(self):
+        g = self.geo
+        L1, L2, L3 = g.L[1], g.L[2], g.L[3]
+        t = {}
+        t["bc12"] = self._map(L1.coords, L1.nodes, L2.coords)  # Level 1 -> Level 2 nodes (LInterp[0])
+        t["bc23"] = self._map(L2.coords, L2.nodes, L3.coords)  # Level 2 -> Level 3 nodes (LInterp[1])
+        t["r32"] = self._map(L3.coords, L3.nodes, L3.overlap_coords)  # Level 3 at Level-2 overlap nodes
+        t["r21"] = self._map(L2.coords, L2.nodes, L2.overlap_coords)  # Level 2 at Level-1 overlap nodes
+        t["r32_idx"] = self._idx_tensor(L3.overlap_nodes, L2.nodes, "Level-3 overlap in Level 2")
+        t["r21_idx"] = self._idx_tensor(L2.overlap_nodes, L1.nodes, "Level-2 overlap in Level 1")
+        t["c32"] = CoupleGeom(L3.coords, L2.coords, self.dtype, self.dev)
+        t["c31"] = CoupleGeom(L3.coords, L1.coords, self.dtype, self.dev)
+        t["c21"] = CoupleGeom(L2.coords, L1.coords, self.dtype, self.dev)
+        t["l0_3"] = self._idx_tensor(g.L0_overlap, g.L0_nodes, "Level-3 window in Level 0")
+        t["l0_2"] = self._idx_tensor(g.L0_overlap_L2, g.L0_nodes, "Level-2 window in Level 0")
+        c31, c21 = t["c31"], t["c21"]
+        for d in range(3):
+            if c31.box_lo[d] < c21.box_lo[d] or c31.box_lo[d] + c31.box_n[d] > c21.box_lo[d] + c21.box_n[d]:
+                raise N.GomeltError("Level-3 window reaches outside Level 2's footprint in Level 1")
+        self.tables = t
+        nmax = max(t["c32"].partials, t["c31"].partials, t["c21"].partials)
+        self._buf("partials", nmax)
+        return t
+
+    # ------------------------------------------------------------------
+    # moveEverything (:2400-2510)
+    # ------------------------------------------------------------------
+    def move(self, v, vstart):
+        g = self.geo
+        L1, L2, L3 = g.L[1], g.L[2], g.L[3]
+        old3 = [c.copy() for c in L3.coords]
+        old2 = [c.copy() for c in L2.coords]
+        old_l0 = [a.copy() for a in g.L0_overlap]
+        new3, new2, move_v = g.move(v, vstart)
+        n3, n2 = L3.nodes, L2.nodes
+        # Level 3: T = I_L1(T1) + I_L2(T'2) + I_L3old(T'3); T'3 = I_L3old(T'3)
+        T3n = self._buf("mvT3", L3.nn)
+        Tp3n = self._buf("mvTp3", L3.nn)
+        self._interp([(self._map(L1.coords, L1.nodes, new3), self.T[1], 1.0),
+                      (self._map(old2, L2.nodes, new3), self.Tp[2], 1.0),
+                      (self._map(old3, L3.nodes, new3), self.Tp[3], 1.0)], n3, T3n, out_term=Tp3n, which=2)
+        # Level 2: T'2 = I_L2old(T'2); T = I_L1(T1) + T'2
+        T2n = self._buf("mvT2", L2.nn)
+        Tp2n = self._buf("mvTp2", L2.nn)
+        self._interp([(self._map(L1.coords, L1.nodes, new2), self.T[1], 1.0),
+                      (self._map(old2, L2.nodes, new2), self.Tp[2], 1.0)], n2, T2n, out_term=Tp2n, which=1)
+        self.T[3].copy_(T3n)
+        self.Tp[3].copy_(Tp3n)
+        self.T[2].copy_(T2n)
+        self.Tp[2].copy_(Tp2n)
+        L3.coords = new3
+        L2.coords = new2
+        # Level-0 gather of the window phases (:2500-2502)
+        l0_3 = self._idx_tensor(g.L0_overlap, g.L0_nodes, "Level-3 window in Level 0")
+        l0_2 = self._idx_tensor(g.L0_overlap_L2, g.L0_nodes, "Level-2 window in Level 0")
+        ph3n = self._buf("mvph3", L3.nn, torch.uint8)
+        self._l0_gather(l0_3, n3, ph3n, self.ph[3] if self.s2_prev_lo is not None else None, self.s2_prev_lo, n3)
+        self.ph[3].copy_(ph3n)
+        self._l0_gather(l0_2, n2, self.ph[2], None, None, None)
+        self.build_tables()
+        return move_v
+
+    def _l0_gather(self, idx, n, ph_out, prev_ph, prev_lo, prev_n):
+        a = N.gm_l0_args()
+        for d in range(3):
+            a.n[d] = int(n[d])
+            a.idx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+        a.l0_nx, a.l0_ny = self.geo.L0_nodes[0], self.geo.L0_nodes[1]
+        a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
+        a.ph = C.cast(ph_out.data_ptr(), C.POINTER(C.c_uint8))
+        if prev_ph is not None:
+            a.prev_ph = C.cast(prev_ph.data_ptr(), C.POINTER(C.c_uint8))
+            for d in range(3):
+                a.prev_lo[d] = int(prev_lo[d])
+                a.prev_n[d] = int(prev_n[d])
+        N.call("gm_l0_gather", C.byref(a), kern.stream_ptr(self.stream))
+
+    def l0_scatter(self):
+        g = self.geo
+        idx = self.tables["l0_3"]
+        a = N.gm_l0_args()
+        for d in range(3):
+            a.n[d] = g.L[3].nodes[d]
+            a.idx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+        a.l0_nx, a.l0_ny = g.L0_nodes[0], g.L0_nodes[1]
+        a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
+        a.ph = C.cast(self.ph[3].data_ptr(), C.POINTER(C.c_uint8))
+        N.call("gm_l0_scatter", C.byref(a), kern.stream_ptr(self.stream))
+        self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
+
+    # ------------------------------------------------------------------
+    # building blocks
+    # ------------------------------------------------------------------
+    def _level(self, lev, T_in, T_out, dt, ph_in, ph_out, *, rhs=None, box=None, laser=None, bc_new=None,
+               bc_old=None, alpha=0.0, accum=False, clamp=True):
+        g = self.geo
+        L = g.L[lev]
+        kw = {}
+        if lev == 1:
+            ne_planes = self.tmp[0] // (L.elements[0] * L.elements[1])
+            c = g.conditions
+            kw.update(bc_mode=1, face=[c["x"][0], c["x"][1], c["y"][0], c["y"][1], c["z"][0]], inactive_amb=1)
+        else:
+            ne_planes = L.elements[2]
+            m = self.tables["bc12"] if lev == 2 else self.tables["bc23"]
+            kw.update(bc_mode=2, bc_new=bc_new, bc_old=bc_old, bc_alpha=alpha, bc_beta=1.0 - alpha, bc_map=m)
+        if accum:
+            kw.update(accum=self.acc3, max_accum=self.macc3)
+        kern.level_step(self.ps, T_in=T_in, T_out=T_out, nodes=L.nodes, h=L.spacing(), origin=L.origin(),
+                        ne_planes=ne_planes, dt=dt, ph_in=ph_in, ph_out=ph_out, substrate=self.substrate[lev],
+                        rhs_box=rhs, box=box, laser=laser, surface=1, clamp=1 if clamp else 0, stream=self.stream,
+                        **kw)
+
+    def _couple(self, cg, fine_lev, out, out_lo, out_n, *, T, ph, Tp=None, dTa=None, dTb=None, dt=None):
+        g = self.geo
+        L = g.L[fine_lev]
+        a = N.gm_couple_args()
+        a.dtype = kern.dtype_code(out)
+        a.geom = cg.struct
+        for d in range(3):
+            a.fine_nodes[d] = L.nodes[d]
+            a.fine_h[d] = L.spacing()[d]
+            a.out_lo[d] = int(out_lo[d])
+            a.out_n[d] = int(out_n[d])
+        a.T = kern.ptr(T)
+        a.ph = C.cast(ph.data_ptr(), C.POINTER(C.c_uint8))
+        a.substrate = self.substrate[fine_lev]
+        a.Tp = kern.ptr(Tp)
+        a.dTa, a.dTb = kern.ptr(dTa), kern.ptr(dTb)
+        a.dt = kern.ptr(dt)
+        a.out = kern.ptr(out)
+        a.scale = 1.0
+        part = self._work["partials"]
+        a.partials = part.data_ptr()
+        a.partials_cap = part.numel()
+        N.call("gm_couple", C.byref(a), C.byref(self.ps), kern.stream_ptr(self.stream))
+
+    def _coarse_source(self, cg, rows, npos, out, out_lo, out_n):
+        L3 = self.geo.L[3]
+        a = N.gm_coarse_source_args()
+        a.dtype = kern.dtype_code(out)
+        a.geom = cg.struct
+        a.npos = int(npos)
+        a.rows = kern.ptr(rows)
+        for d in range(3):
+            a.xq[d] = C.cast(cg.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
+            a.out_lo[d] = int(out_lo[d])
+            a.out_n[d] = int(out_n[d])
+        h = L3.spacing()
+        a.fine_wq = h[0] * h[1] * h[2] / 8.0
+        a.out = kern.ptr(out)
+        per = sum(cg.box_n)
+        scr = self._buf("srcscratch", npos * per)
+        a.scratch = scr.data_ptr()
+        a.scratch_cap = scr.numel()
+        N.call("gm_coarse_source", C.byref(a), C.byref(self.ps), kern.stream_ptr(self.stream))
+
+    def _restrict(self, rmap, idx, coarse_nodes, fine_T, coarse_T):
+        a = N.gm_restrict_args()
+        a.dtype = kern.dtype_code(fine_T)
+        for d in range(3):
+            a.n[d] = rmap.n[d]
+            a.cidx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+        a.map = rmap.struct
+        a.cnx, a.cny = coarse_nodes[0], coarse_nodes[1]
+        a.fine = kern.ptr(fine_T)
+        a.coarse = kern.ptr(coarse_T)
+        N.call("gm_restrict", C.byref(a), kern.stream_ptr(self.stream))
+
+    def _new_tprime(self, fine_lev, fine_T, coarse_T, out_Tp):
+        """getNewTprime (:2060-2099): restrict into coarse_T, then T' = T_f - I(T_c)."""
+        g = self.geo
+        if fine_lev == 3:
+            rmap, idx, cmap, cn = self.tables["r32"], self.tables["r32_idx"], self.tables["bc23"], g.L[2].nodes
+        else:
+            rmap, idx, cmap, cn = self.tables["r21"], self.tables["r21_idx"], self.tables["bc12"], g.L[1].nodes
+        self._restrict(rmap, idx, cn, fine_T, coarse_T)
+        self._interp([(cmap, coarse_T, -1.0)], g.L[fine_lev].nodes, out_Tp, base=fine_T)
+
+    def _s1_restrict(self):
+        g = self.geo
+        a = N.gm_restrict_s1_args()
+        a.dtype = kern.dtype_code(self.T[1])
+        rmap, idx = self.tables["r21"], self.tables["r21_idx"]
+        for d in range(3):
+            a.n[d] = rmap.n[d]
+            a.cidx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+        a.map = rmap.struct
+        a.cnx, a.cny = g.L[1].nodes[0], g.L[1].nodes[1]
+        a.fine_ph = C.cast(self.ph[2].data_ptr(), C.POINTER(C.c_uint8))
+        a.coarse_ph = C.cast(self.ph[1].data_ptr(), C.POINTER(C.c_uint8))
+        a.substrate = self.substrate[1]
+        N.call("gm_restrict_s1", C.byref(a), kern.stream_ptr(self.stream))
+
+    # ------------------------------------------------------------------
+    # subcycleGOMELT (:3224-3632)
+    # ------------------------------------------------------------------
+    def subcycle(self, laser_rows, history=False):
+        g = self.geo
+        L1, L2, L3 = g.L[1], g.L[2], g.L[3]
+        N2, N3 = self.N2, self.N3
+        rows_h = np.ascontiguousarray(np.asarray(laser_rows, dtype=np.float64))
+        assert rows_h.shape == (N2 * N3, 7), rows_h.shape
+        if self.tmp is None:
+            raise N.GomeltError("active Level-1 region not set (call set_layer first)")
+        dts = np.concatenate([[rows_h[:, 5].sum()], rows_h[:, 5].reshape(N2, N3).sum(axis=1)])
+        rows = self._buf("rows", rows_h.size, torch.float64).view(N2 * N3, 7)
+        rows.copy_(torch.from_numpy(rows_h), non_blocking=False)
+        dtd = self._buf("dts", N2 + 1, torch.float64)
+        dtd.copy_(torch.from_numpy(dts))
+        tb = self.tables
+        c32, c31, c21 = tb["c32"], tb["c31"], tb["c21"]
+        T1s, T2s, T3s = self.T[1], self.T[2], self.T[3]
+        Tp2s, Tp3s = self.Tp[2], self.Tp[3]
+        ph1, ph2s, ph3s = self.ph[1], self.ph[2], self.ph[3]
+        nn1, nn2, nn3 = L1.nn, L2.nn, L3.nn
+
+        # Level-1 S1 from Level 2 at the overlap (:3272-3278)
+        self._s1_restrict()
+        # Level-1 right-hand side: source over all positions + subgrid fluxes of L3 and L2
+        rhs1 = self._buf("rhs1", int(np.prod(c21.box_n)))
+        rhs1.zero_()
+        self._coarse_source(c31, rows, N2 * N3, rhs1, c21.box_lo, c21.box_n)
+        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, Tp=Tp3s)
+        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, Tp=Tp2s)
+        box1 = [c21.box_lo[0], c21.box_lo[0] + c21.box_n[0], c21.box_lo[1], c21.box_lo[1] + c21.box_n[1],
+                c21.box_lo[2], c21.box_lo[2] + c21.box_n[2]]
+        T1p = self._buf("T1p", nn1)
+        self._level(1, T1s, T1p, dtd[0:1], ph1, None, rhs=rhs1, box=box1)
+
+        rhs2 = self._buf("rhs2", int(np.prod(c32.box_n)))
+        box2 = [c32.box_lo[0], c32.box_lo[0] + c32.box_n[0], c32.box_lo[1], c32.box_lo[1] + c32.box_n[1],
+                c32.box_lo[2], c32.box_lo[2] + c32.box_n[2]]
+        hist = self._buf("tp3hist", N2 * nn3).view(N2, nn3)
+        T3w = [self._buf("T3a", nn3), self._buf("T3b", nn3)]
+        ph3w = [self._buf("ph3a", nn3, torch.uint8), self._buf("ph3b", nn3, torch.uint8)]
+        T2w = [self._buf("T2a", nn2), self._buf("T2b", nn2), self._buf("T2c", nn2)]
+        ph2w = [self._buf("ph2a", nn2, torch.uint8), self._buf("ph2b", nn2, torch.uint8)]
+        out_hist = None
+        if history:
+            out_hist = (torch.empty(N2, nn2, dtype=self.dtype, device=self.dev),
+                        torch.empty(N2, nn3, dtype=self.dtype, device=self.dev),
+                        torch.empty(N2, nn3, dtype=self.dtype, device=self.dev))
+
+        def l2_pass(T1_new, part2):
+            T2c, ph2c = T2s, ph2s
+            T3c, ph3c, Tp3c = T3s, ph3s, Tp3s
+            k2 = 0
+            for l2 in range(N2):
+                rhs2.zero_()
+                if part2:
+                    self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3c, ph=ph3c, Tp=Tp3c, dTa=hist[l2],
+                                 dTb=Tp3c, dt=dtd[1 + l2:2 + l2])
+                else:
+                    self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3c, ph=ph3c, Tp=Tp3c)
+                self._coarse_source(c32, rows[l2 * N3:(l2 + 1) * N3], N3, rhs2, c32.box_lo, c32.box_n)
+                alpha2 = (l2 + 1) / float(N2)
+                T2n = T2w[k2 % 3] if T2w[k2 % 3].data_ptr() != T2c.data_ptr() else T2w[(k2 + 1) % 3]
+                ph2n = ph2w[l2 % 2]
+                self._level(2, T2c, T2n, dtd[1 + l2:2 + l2], ph2c, ph2n, rhs=rhs2, box=box2, bc_new=T1_new,
+                            bc_old=T1s, alpha=alpha2)
+                k2 += 1
+                for l3 in range(N3):
+                    i = l2 * N3 + l3
+                    Tn = T3w[i % 2]
+                    phn = ph3w[i % 2]
+                    self._level(3, T3c, Tn, rows[i, 5:6], ph3c, phn, laser=rows[i], bc_new=T2n, bc_old=T2c,
+                                alpha=(l3 + 1) / float(N3), accum=part2)
+                    T3c, ph3c = Tn, phn
+                Tp3n = hist[l2] if not part2 else self._buf("tp3w%d" % (l2 % 2), nn3)
+                self._new_tprime(3, T3c, T2n, Tp3n)
+                if part2 and history:
+                    out_hist[0][l2].copy_(T2n)
+                    out_hist[1][l2].copy_(T3c)
+                    out_hist[2][l2].copy_(Tp3n)
+                Tp3c = Tp3n
+                T2c, ph2c = T2n, ph2n
+            return T2c, ph2c, T3c, ph3c, Tp3c
+
+        # Part 1 (predictor)
+        T2f, _, _, _, Tp3f = l2_pass(T1p, False)
+        Tp2w = self._buf("Tp2w", nn2)
+        self._new_tprime(2, T2f, T1p, Tp2w)
+        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, dTa=Tp3f, dTb=Tp3s, dt=dtd[0:1])
+        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, dTa=Tp2w, dTb=Tp2s, dt=dtd[0:1])
+        T1c = self._buf("T1c", nn1)
+        self._level(1, T1s, T1c, dtd[0:1], ph1, None, rhs=rhs1, box=box1)
+        # Part 2 (corrector)
+        T2f, ph2f, T3f, ph3f, Tp3f = l2_pass(T1c, True)
+        T3s.copy_(T3f)
+        ph3s.copy_(ph3f)
+        Tp3s.copy_(Tp3f)
+        T2s.copy_(T2f)
+        ph2s.copy_(ph2f)
+        self._new_tprime(2, T2s, T1c, Tp2s)
+        T1s.copy_(T1c)
+        self.l0_scatter()
+        return out_hist
+
+    # ------------------------------------------------------------------
+    # state set-up
+    # ------------------------------------------------------------------
+    def set_layer(self, v):
+        """Active Level-1 region and substrate counts for the layer at v[2]."""
+        self.tmp = self.geo.tmp_ne_nn(v)
+        self.substrate = self.geo.substrate()
+
+    def load_levels(self, Levels):
+        """Adopt a reference-layout ``Levels`` list (host arrays): window
+        positions, overlap sets, fields, phases and the Level-0 store."""
+        g = self.geo
+        f = dict(dtype=self.dtype, device=self.dev)
+        for lev in (1, 2, 3):
+            Ld = Levels[lev]
+            g.L[lev].coords = [np.asarray(c, dtype=np.float64).copy() for c in Ld["node_coords"]]
+            self.T[lev] = torch.as_tensor(np.asarray(Ld["T0"], dtype=np.float64), **f).contiguous()
+            ph = (np.asarray(Ld["S1"], dtype=np.float64) > 0.499).astype(np.uint8)
+            if "S2" in Ld:
+                ph |= (np.asarray(Ld["S2"]).astype(bool).astype(np.uint8) << 1)
+            self.ph[lev] = torch.as_tensor(ph, device=self.dev).contiguous()
+            if lev > 1:
+                self.Tp[lev] = torch.as_tensor(np.asarray(Ld["Tprime0"], dtype=np.float64), **f).contiguous()
+                g.L[lev].overlap_nodes = [np.asarray(a).astype(np.int64) for a in Ld["overlapNodes"]]
+                g.L[lev].overlap_coords = [np.asarray(a, dtype=np.float64) for a in Ld["overlapCoords"]]
+        L0 = Levels[0]
+        g.L0_overlap = [np.asarray(a).astype(np.int64) for a in L0["overlapNodes"]]
+        g.L0_overlap_L2 = [np.asarray(a).astype(np.int64) for a in L0["overlapNodes_L2"]]
+        g.L0_coords = [np.asarray(c, dtype=np.float64).copy() for c in L0["node_coords"]]
+        self.L0 = torch.as_tensor((np.asarray(L0["S1"], dtype=np.float64) > 0.499).astype(np.uint8),
+                                  device=self.dev).contiguous()
+        s2 = np.asarray(L0["S2"]).astype(bool)
+        self.s2_prev_lo = [int(g.L0_overlap[d][0]) for d in range(3)] if s2.any() else None
+        self.acc3 = torch.zeros(g.L[3].nn, **f)
+        self.macc3 = torch.zeros(g.L[3].nn, **f)
+        self.build_tables()
+
+    def fields_numpy(self):
+        """Host copies of the state in the reference's field names."""
+        out = {}
+        for lev in (1, 2, 3):
+            ph = self.ph[lev].cpu().numpy()
+            out[lev] = {"T0": self.T[lev].double().cpu().numpy(), "S1": (ph & PH_S1).astype(np.float64),
+                        "S2": (ph & PH_S2) != 0}
+            if lev > 1:
+                out[lev]["Tprime0"] = self.Tp[lev].double().cpu().numpy()
+        out[0] = {"S1": self.L0.cpu().numpy().astype(np.float64)}
+        return out

@@ -1,0 +1,270 @@
+/*
+ * gomelt.h -- C ABI of the GB300 (sm_103a) implementation of GO-MELT's
+ * multilevel explicit thermal step.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*), enqueues work on that stream and returns a status code
+ * (GM_OK = 0).  No entry point allocates device memory.  Floating-point
+ * buffers are float (dtype GM_F32) or double (GM_F64), as the call says.
+ *
+ * Layout: every level is a structured node grid, node id = ix + iy*nx +
+ * iz*nx*ny (x fastest), as in the reference's convert2XYZ
+ * (go_melt/computeFunctions.py:645-689).  Phase bytes: bit0 = S1 (bulk),
+ * bit1 = S2 (liquid).  Units are the reference's (mm, s, W, K).
+ *
+ * Each declaration names the reference function of GO-MELT
+ * (JLnorthwestern/GO-MELT, go_melt/computeFunctions.py) that it replaces.
+ */
+#ifndef GOMELT_H
+#define GOMELT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum gm_status_code {
+  GM_OK = 0,
+  GM_ERR_ARG = 1,         /* invalid argument (null pointer, size, dtype) */
+  GM_ERR_LAUNCH = 2,      /* kernel launch failed */
+  GM_ERR_CUDA = 3,        /* other CUDA runtime error */
+  GM_ERR_UNSUPPORTED = 4, /* configuration outside what this build handles */
+  GM_ERR_TOO_LARGE = 5    /* request exceeds a fixed capacity */
+};
+
+enum gm_dtype { GM_F32 = 0, GM_F64 = 1 };
+
+/* Material, laser and surface constants after the reference's set-up
+ * (SetupProperties, computeFunctions.py:267-345).  Conductivities in W/(m K)
+ * as in the input file (divided by 1000 inside), h_conv already multiplied by
+ * 1e6 as the reference does (:318-319). */
+typedef struct gm_props {
+  double k_powder, k_bulk_a0, k_bulk_a1, k_fluid;
+  double cp_solid_a0, cp_solid_a1, cp_mushy, cp_fluid, rho;
+  double T_amb, T_solidus, T_liquidus, T_boiling;
+  double h_conv, emissivity, sigma_sb, evc, Lev, CM_coeff, CT_coeff, CP_coeff;
+  double laser_radius, laser_depth, laser_eta;
+} gm_props;
+
+/* Separable trilinear interpolation map from a source node grid to a tensor
+ * grid of target points (interpolatePointsMatrix, :1028-1107).  Per axis d
+ * and target index t: elem[d][t] = source element (clipped floor), w[d][2t]
+ * = (x_{e+1} - x)/h, w[d][2t+1] = (x - x_e)/h (dtype of the call). */
+typedef struct gm_map3 {
+  int n[3];
+  int src_nx, src_ny;
+  const int* elem[3];
+  const void* w[3];
+} gm_map3;
+
+/* One explicit level step, fused.  Replaces solveMatrixFreeFE (:582-642)
+ * together with what the reference computes around it for one level:
+ * computeStateProperties (:2567-2614), computeSourcesL3 (:2960-3012),
+ * computeConvRadBC (:2207-2301), substitute_Tbar (:1848-1865), assignBCs
+ * (:1568-1595) / assignBCsFine (:1598-1620) with the prolongated coarse field
+ * (interpolate_w_matrix, :1110-1128), the T >= T_amb clamp and the melt-time
+ * update (:3568-3578). */
+typedef struct gm_level_args {
+  int dtype;
+  int nx, ny, nz;              /* nodes per axis */
+  double h[3];                 /* node spacing */
+  double origin[3];            /* coordinates of node 0 (for the laser source) */
+  int ne_planes;               /* elements with ez < ne_planes are active */
+  const double* dt;            /* device pointer: time step [s] */
+  const void* T_in;            /* temperature at step start */
+  void* T_out;                 /* new temperature (must not alias T_in) */
+  const uint8_t* ph_in;        /* phase at step start (NULL: all zero) */
+  uint8_t* ph_out;             /* updated phase (NULL: not written) */
+  long long substrate;         /* nodes with id < substrate are always S1 */
+  const void* k_arr;           /* optional nodal k [W/(mm K)]; NULL: from T/phase */
+  const void* rc_arr;          /* optional nodal rho*cp; NULL: from T/phase */
+  const void* F_full;          /* optional full-size RHS vector */
+  const void* corr_full;       /* optional full-size correction vector */
+  const void* rhs_box;         /* optional extra RHS on a node box */
+  int box[6];                  /* box: x0,x1,y0,y1,z0,z1 (half-open) */
+  const double* laser;         /* device laser row (x,y,z,...,P at [6]); NULL: no source */
+  int surface;                 /* 1: conv/rad/evap flux on the top active plane */
+  int bc_mode;                 /* 0: none, 1: constant faces, 2: prolongated coarse field */
+  double face[5];              /* bc_mode 1: x0, x1, y0, y1, z0 face values */
+  int inactive_amb;            /* 1: nodes above the active region set to T_amb */
+  const void* bc_new;          /* bc_mode 2: coarse field alpha*bc_new + beta*bc_old */
+  const void* bc_old;
+  double bc_alpha, bc_beta;
+  gm_map3 bc_map;              /* coarse -> this level's nodes */
+  int clamp;                   /* 1: T = max(T, T_amb) */
+  void* accum;                 /* optional melt-time accumulators (Level 3) */
+  void* max_accum;
+  int zchunk;                  /* node planes per CTA (0: automatic) */
+} gm_level_args;
+
+int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream);
+
+/* Separable gather over a tensor grid of target points:
+ *   out = base + sum_k coef[k] * I_k(src[k]),  k < nterms <= 3
+ * and optionally out_term = I_which_term(src[which_term]).
+ * Replaces interpolatePoints (:1131-1210) and interpolate_w_matrix
+ * (:1110-1128); with base = fine T and coef = -1 it is the T' of
+ * getNewTprime (:2097); with three terms it is the field remap of
+ * moveEverything (:2427-2459). */
+typedef struct gm_interp_args {
+  int dtype;
+  int n[3];
+  int nterms;
+  gm_map3 map[3];
+  const void* src[3];
+  double coef[3];
+  const void* base; /* optional */
+  void* out;
+  void* out_term;   /* optional */
+  int which_term;
+} gm_interp_args;
+
+int gm_interp(const gm_interp_args* a, void* stream);
+
+/* Materialised interpolation matrix: Nc (npts x 8, dtype) and node (npts x 8)
+ * for the target tensor grid of m (interpolatePointsMatrix, :1028-1107). */
+int gm_interp_matrix(int dtype, const gm_map3* m, void* Nc, int* node, void* stream);
+
+/* out[t] = sum_q Nc[t,q] * T[node[t,q]] (interpolate_w_matrix, :1110-1128). */
+int gm_interp_w_matrix(int dtype, const void* Nc, const int* node, const void* T, void* out, long long n,
+                       void* stream);
+
+/* Restriction of getNewTprime (:2085-2093): coarse[cidx] = fine field
+ * interpolated at the coarse overlap nodes (map: fine grid -> overlap
+ * coordinates; cidx[d]: coarse node index of each overlap point per axis). */
+typedef struct gm_restrict_args {
+  int dtype;
+  int n[3];
+  gm_map3 map;
+  const int* cidx[3];
+  int cnx, cny;
+  const void* fine;
+  void* coarse;
+} gm_restrict_args;
+
+int gm_restrict(const gm_restrict_args* a, void* stream);
+
+/* Level-1 S1 from Level 2 (subcycleGOMELT :3272-3278, updateStateProperties
+ * :2547-2556): S1 bit of coarse_ph at the overlap nodes := interpolated
+ * Level-2 S1 > 0.499, or node id < substrate. */
+typedef struct gm_restrict_s1_args {
+  int dtype;
+  int n[3];
+  gm_map3 map;
+  const int* cidx[3];
+  int cnx, cny;
+  const uint8_t* fine_ph;
+  uint8_t* coarse_ph;
+  long long substrate;
+} gm_restrict_s1_args;
+
+int gm_restrict_s1(const gm_restrict_s1_args* a, void* stream);
+
+/* Level-0 phase store (one byte per Level-0 node: 1 = S1).
+ * gather: ph[t] = S1 from Level 0 at (idx[0][i], idx[1][j], idx[2][k]) plus
+ *   the S2 bit of prev_ph where the previous window (Level-0 start prev_lo,
+ *   size prev_n) covers the node (moveEverything :2500-2502; Level 0 keeps S2
+ *   only inside the last scattered window, :2390-2392, :3628-3630).
+ * scatter: Level-0 S1 at the window := S1 bit of ph (:2390-2391, :3628). */
+typedef struct gm_l0_args {
+  int n[3];
+  const int* idx[3];
+  long long l0_nx, l0_ny;
+  uint8_t* l0_s1;
+  uint8_t* ph;
+  const uint8_t* prev_ph; /* gather only; NULL: no S2 anywhere */
+  int prev_lo[3], prev_n[3];
+} gm_l0_args;
+
+int gm_l0_gather(const gm_l0_args* a, void* stream);
+int gm_l0_scatter(const gm_l0_args* a, void* stream);
+
+/* Per-axis geometry of a fine level inside a coarse level, for the terms that
+ * the reference evaluates through computeCoarseFineShapeFunctions
+ * (:1213-1358).  For fine element e and Gauss side s (0: xi=-1/sqrt3,
+ * 1: +1/sqrt3): cw[(e*2+s)*2 + A] = 1-D coarse weight of local coarse node A
+ * (A=0: (x1-x)/H, A=1: (x-x0)/H) in the coarse element of that Gauss point;
+ * node0[e] = coarse element of side 0 (whose nodes receive the result, as
+ * the reference's BCOO does).  Coarse elements [cb_lo, cb_lo+ncb) receive
+ * fine elements [flo[i], fhi[i]); rmax = max(fhi-flo); H = coarse spacing. */
+typedef struct gm_couple_axis {
+  int nfe;
+  const void* cw;
+  const int* node0;
+  int cb_lo, ncb;
+  const int* flo;
+  const int* fhi;
+  int rmax;
+  double H;
+} gm_couple_axis;
+
+typedef struct gm_couple_geom {
+  gm_couple_axis ax[3];
+} gm_couple_geom;
+
+/* Number of scratch elements (dtype) gm_couple needs for `partials`. */
+long long gm_couple_partials_size(const gm_couple_geom* g);
+
+/* Fine -> coarse subgrid terms, added into `out` (a dtype array over the
+ * coarse node box [out_lo, out_lo+out_n) per axis) times `scale`:
+ *   Tp != NULL : flux term  -sum grad Nc . (kbar grad Tp) w
+ *     (computeL1TprimeTerms_Part1 :2733-2810, computeL2TprimeTerms_Part1
+ *      :2857-2914, computeCoarseTprimeTerm_jax :1477-1565)
+ *   dTa != NULL: mass term  -sum Nc rcbar (dTa - dTb) w / dt
+ *     (computeL1TprimeTerms_Part2 :3057-3132, computeL2TprimeTerms_Part2
+ *      :3169-3221, computeCoarseTprimeMassTerm_jax :1396-1474)
+ * kbar, rcbar: element means of k and rho*c from the fine T and phase
+ * (computeStateProperties with `substrate`) or from k_arr/rc_arr.
+ * `partials` is caller-provided scratch of partials_cap elements. */
+typedef struct gm_couple_args {
+  int dtype;
+  gm_couple_geom geom;
+  int fine_nodes[3];
+  double fine_h[3];
+  const void* T;
+  const uint8_t* ph;
+  long long substrate;
+  const void* k_arr;
+  const void* rc_arr;
+  const void* Tp;
+  const void* dTa;
+  const void* dTb;
+  const double* dt;
+  void* out;
+  int out_lo[3], out_n[3];
+  double scale;
+  void* partials;
+  long long partials_cap;
+} gm_couple_args;
+
+int gm_couple(const gm_couple_args* a, const gm_props* p, void* stream);
+
+/* Coarse laser source averaged over npos laser rows (computeLevelSource
+ * :2667-2730; with npos = 1 the Fc/Fm of computeSources :928-988), added into
+ * `out` (coarse node box as in gm_couple).  rows: device array of npos rows of
+ * 7 doubles (x, y, z, ..., P at [6]); xq[d]: fine Gauss coordinates per axis
+ * (nfe*2 doubles); fine_wq: fine quadrature weight hx*hy*hz/8; scratch:
+ * npos*((ncb0+1)+(ncb1+1)+(ncb2+1)) dtype elements. */
+typedef struct gm_coarse_source_args {
+  int dtype;
+  gm_couple_geom geom;
+  int npos;
+  const double* rows;
+  const double* xq[3];
+  double fine_wq;
+  void* out;
+  int out_lo[3], out_n[3];
+  void* scratch;
+  long long scratch_cap;
+} gm_coarse_source_args;
+
+int gm_coarse_source(const gm_coarse_source_args* a, const gm_props* p, void* stream);
+
+/* Library identification: returns a static string; never fails. */
+const char* gm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GOMELT_H */
