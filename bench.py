@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Benchmark of GO-MELT's multilevel explicit thermal step on GB300.
+
+Metric: simulated scan length (mm) per wall-second.  One step = one subcycle
+call of the reference driver's hot loop: moveEverything + subcycleGOMELT over
+N2*N3 = 100 toolpath rows (0.1575 mm of scan at 1 m/s).  Workload: the
+part-scale configuration (Level 1 200x200x50 @ 100 um, Level 2 100x100x15 @
+20 um, Level 3 160x160x40 @ 5 um; first layer of a serpentine raster).
+
+value : steps timed with CUDA events on the engine's stream, toolpath rows
+        already on the device; L2 flushed between steps (untimed).
+e2e   : the same steps through the engine's public calls with the toolpath rows
+        in host memory (H2D inside the timed region) and the per-step device->
+        host read of the Level-3 peak temperature that the driver's
+        temperature check does.
+roofline: the Level-3 level-step kernel timed alone with CUDA events (its
+        algorithmic bytes: 10 B per node: T read + write, phase byte read +
+        write) against the measured HBM copy bandwidth.
+cpu_baseline / --impl reference: the NumPy FP64 oracle (a restatement of the
+        reference's JAX code; JAX is not installed on the GPU host) timed on
+        fine-level steps of the same workload.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "go-melt_gb300"))
+
+L2_FLUSH_BYTES = 512 << 20
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+PROFILE_FILE = os.path.join(ROOT, "profiles", "level_step_l3_config1.txt")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--cpu-steps", type=int, default=8, help="oracle fine steps in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload():
+    import createPath
+    import levels
+    import workloads
+
+    cfg = workloads.config1()
+    P = levels.setup_properties(cfg["properties"])
+    nm = levels.setup_nonmesh(cfg["nonmesh"])
+    r = cfg["raster"]
+    gcode = createPath.serpentine_gcode(r["x0"], r["y0"], r["length"], r["hatch"], r["ntracks"])
+    import numpy as np
+
+    rows = np.asarray(createPath.toolpath(nm, P, gcode), dtype=np.float64)
+    return cfg, P, nm, rows
+
+
+def scan_mm(rows):
+    """Laser-on travel: sum over rows with P > 0 of the in-plane displacement."""
+    import numpy as np
+
+    d = np.zeros(len(rows))
+    d[1:] = np.hypot(np.diff(rows[:, 0]), np.diff(rows[:, 1]))
+    return float((d * (rows[:, 6] > 0)).sum())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.idx = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 10:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax.append(float(c[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, c[6:10]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per Level-3 level-step launch from the committed ncu summary."""
+    try:
+        with open(PROFILE_FILE) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch_full:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle sample (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+def oracle_sample(cfg, rows, nsteps, warm=1):
+    """Fine-level (Level 3) steps of the NumPy oracle along the toolpath:
+    computeStateProperties + computeSourcesL3 + computeConvRadBC +
+    computeSolutions_L3 + clamp, per row.  Returns (mm/s, seconds, steps)."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gomelt_oracle as O
+
+    P = O.SetupProperties(cfg["properties"])
+    L = O.SetupLevels(cfg, P)
+    ne_nn = O.getStaticNodesAndElements(L)
+    C2F = O.interpolatePointsMatrix(L[2], L[3]["node_coords"])
+    T = np.asarray(L[3]["T0"], dtype=float)
+    S1 = np.asarray(L[3]["S1"], dtype=float)
+
+    def one(r):
+        nonlocal T, S1
+        S1n, _, k, rc = O.computeStateProperties(T, S1, P, 0)
+        F = O.computeSourcesL3(L[3], r, ne_nn, P, r[6])
+        F = O.computeConvRadBC(L[3], T, ne_nn[1], ne_nn[4], P, F)
+        T = np.maximum(P["T_amb"], O.computeSolutions_L3(L[2]["T0"], C2F, L, ne_nn, T, F, k, rc, r[5]))
+        S1 = S1n
+
+    for i in range(warm):
+        one(rows[i])
+    t0 = time.perf_counter()
+    for i in range(warm, warm + nsteps):
+        one(rows[i])
+    dt = time.perf_counter() - t0
+    mm = scan_mm(rows[warm - 1:warm + nsteps])
+    return mm / dt, dt, nsteps
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfg, P, nm, rows = workload()
+    v, secs, n = oracle_sample(cfg, rows, args.steps, warm=max(1, args.warmup))
+    cores = 1
+    line = {
+        "impl": "reference", "metric": "simulated scan mm per wall-s (plain multilevel explicit step)", "value": v,
+        "unit": "mm/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * secs / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (generated G-code raster)",
+        "config": {"workload": "part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, "
+                               "L3 160x160x40 @5um, first layer", "sample": "fine-level steps"},
+        "cpu_baseline": {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} Level-3 steps of the NumPy FP64 oracle (props, source, surface flux, "
+                                   f"solve, Dirichlet ring, clamp) along the toolpath; Level-1/2 work and "
+                                   f"coupling terms excluded, so this overstates the CPU rate"},
+        "e2e": {"value": v, "unit": "mm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import _native as N
+    import engine
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    N.lib()
+    cfg, P, nm, rows = workload()
+    N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
+    n23 = N2 * N3
+    dtype = torch.float32 if args.dtype == "f32" else torch.float64
+    stream = torch.cuda.Stream(device=dev)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    need = (args.warmup + 2 * args.steps + 1) * n23
+    if len(rows) < need:
+        raise SystemExit(f"toolpath too short: {len(rows)} rows < {need}")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    with torch.cuda.stream(stream):
+        eng = engine.Engine(cfg, P, N2, N3, dtype=dtype, device=dev, stream=stream)
+        eng.set_layer(rows[0])
+        eng.move(rows[0], vstart)
+
+        def chunk(k):
+            return rows[k * n23:(k + 1) * n23]
+
+        k = 0
+        for _ in range(args.warmup):
+            eng.move(chunk(k)[0], vstart)
+            eng.subcycle(chunk(k))
+            k += 1
+        stream.synchronize()
+
+        # ---- value: rows resident on the device --------------------------
+        dev_rows = [torch.as_tensor(chunk(k + i), device=dev) for i in range(args.steps)]
+        clocks = Clocks(local)
+        N.reset_launch_count()
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        ev = []
+        for i in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            eng.move(chunk(k + i)[0], vstart)
+            eng.subcycle(chunk(k + i), rows_device=dev_rows[i])
+            e.record(stream)
+            ev.append((s, e))
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        launches = N.launch_count() // args.steps
+        t_ms = sum(s.elapsed_time(e) for s, e in ev)
+        mm = sum(scan_mm(chunk(k + i)) for i in range(args.steps))
+        k += args.steps
+
+        # ---- e2e: host rows, H2D inside, D2H of the peak temperature -------
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e2e_ms = 0.0
+        mm_e2e = 0.0
+        for i in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            c = chunk(k + i)
+            eng.move(c[0], vstart)
+            eng.subcycle(c)
+            tmax = float(eng.T[3].max().item())  # the driver's per-chunk temperature check
+            e2e_ms += 1000.0 * (time.perf_counter() - t0)
+            mm_e2e += scan_mm(c)
+            if not np.isfinite(tmax) or tmax > 1e5:
+                raise SystemExit(f"non-finite or invalid temperature {tmax}")
+        k += args.steps
+
+        # ---- dominant kernel alone: Level-3 level step ---------------------
+        L3 = eng.geo.L[3]
+        Tout = torch.empty_like(eng.T[3])
+        phout = torch.empty_like(eng.ph[3])
+        last = torch.as_tensor(chunk(k - 1)[-1], device=dev)
+        reps = 50
+        for _ in range(5):
+            eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, bc_new=eng.T[2],
+                       bc_old=eng.T[2], alpha=1.0)
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, bc_new=eng.T[2],
+                       bc_old=eng.T[2], alpha=1.0)
+        e.record(stream)
+        torch.cuda.synchronize()
+        k_ms = s.elapsed_time(e) / reps
+
+    if ws > 1:
+        t = torch.tensor([t_ms, e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms, e2e_ms = float(t[0]), float(t[1])
+        m = torch.tensor([mm, mm_e2e], device=dev)
+        dist.all_reduce(m, op=dist.ReduceOp.SUM)
+        mm, mm_e2e = float(m[0]), float(m[1])
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = measured_peak()
+    alg_bytes = 10.0 * L3.nn
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+    line = {
+        "metric": "simulated scan mm per wall-s (plain multilevel explicit step)",
+        "value": mm / (t_ms * 1e-3), "unit": "mm/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if dtype == torch.float32 else "f64", "data": "synthetic (generated G-code raster)",
+        "config": {"workload": "part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, L3 160x160x40 @5um, "
+                               "first layer, N2=N3=10, dt3=1.575us",
+                   "step": "moveEverything + subcycleGOMELT (100 fine steps)", "l2": "flushed between steps",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": mm_e2e / (e2e_ms * 1e-3), "unit": "mm/s", "h2d_bytes_per_step": n23 * 7 * 8,
+                "d2h_bytes_per_step": 4 if dtype == torch.float32 else 8},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "level_step_kernel (Level 3)", "kernel_ms": k_ms,
+                     "alg_bytes": alg_bytes, "peak_kind": peak_kind},
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        v, secs, n = oracle_sample(cfg, rows, args.cpu_steps)
+        line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": 1, "kind": "port",
+                                "sample": f"{n} Level-3 steps of the NumPy FP64 oracle ({secs:.1f} s); Level-1/2 "
+                                          f"work and coupling terms excluded"}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

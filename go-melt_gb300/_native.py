@@ -52,6 +52,11 @@ class gm_level_args(C.Structure):
     ]
 
 
+class gm_state_props_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_longlong), ("T", vp), ("ph_in", C.POINTER(C.c_uint8)),
+                ("ph_out", C.POINTER(C.c_uint8)), ("k_out", vp), ("rc_out", vp), ("substrate", C.c_longlong)]
+
+
 class gm_interp_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("nterms", C.c_int), ("map", gm_map3 * 3),
                 ("src", vp * 3), ("coef", C.c_double * 3), ("base", vp), ("out", vp), ("out_term", vp),
@@ -125,6 +130,12 @@ def lib():
 
 SIGNATURES = {
     "gm_level_step": [C.POINTER(gm_level_args), C.POINTER(gm_props), vp],
+    "gm_state_properties": [C.POINTER(gm_state_props_args), C.POINTER(gm_props), vp],
+    "gm_fine_source": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), vp,
+                       C.POINTER(gm_props), vp, vp],
+    "gm_surface_flux": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int, vp, C.POINTER(gm_props),
+                        vp, vp],
+    "gm_clamp_min": [C.c_int, vp, C.c_longlong, C.c_double, vp],
     "gm_interp": [C.POINTER(gm_interp_args), vp],
     "gm_interp_matrix": [C.c_int, C.POINTER(gm_map3), vp, vp, vp],
     "gm_interp_w_matrix": [C.c_int, vp, vp, vp, vp, C.c_longlong, vp],
@@ -142,8 +153,22 @@ def check(code: int, what: str):
         raise GomeltError(f"{what}: {_ERRNAMES.get(code, code)}")
 
 
+# kernels launched by each entry point (for launch accounting)
+KERNELS_PER_CALL = {"gm_couple": 2, "gm_coarse_source": 2}
+_launches = [0]
+
+
+def reset_launch_count():
+    _launches[0] = 0
+
+
+def launch_count() -> int:
+    return _launches[0]
+
+
 def call(name: str, *args):
     check(getattr(lib(), name)(*args), name)
+    _launches[0] += KERNELS_PER_CALL.get(name, 1)
 
 
 def props_struct(p: dict) -> gm_props:

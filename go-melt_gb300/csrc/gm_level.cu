@@ -397,3 +397,132 @@ extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* st
 }
 
 extern "C" const char* gm_version(void) { return "gomelt-gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------------------
+// Stand-alone pieces of the level step (the reference's separate functions).
+// ---------------------------------------------------------------------------
+namespace gm {
+
+// computeStateProperties (:2567-2614): new phase byte, optional k and rho*c.
+template <typename real>
+__global__ void state_props_kernel(long long n, const real* T, const uint8_t* ph_in, uint8_t* ph_out, real* k_out,
+                                   real* rc_out, long long substrate, const Props<real> p) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    real k, c;
+    const uint8_t ph = node_props(p, T[i], ph_in ? ph_in[i] : (uint8_t)0, i < substrate, k, c);
+    if (ph_out) ph_out[i] = ph;
+    if (k_out) k_out[i] = k;
+    if (rc_out) rc_out[i] = c;
+  }
+}
+
+// computeSourcesL3 (:2960-3012): F[node] += c P Sx[ix] Sy[iy] Sz[iz].
+template <typename real>
+__global__ void fine_source_kernel(int nx, int ny, int nz, double ox, double oy, double oz, double hx, double hy,
+                                   double hz, const double* laser, double rsq, double dsq, double src_c, real* F) {
+  const long long n = (long long)nx * ny * nz;
+  const double vx = laser[0], vy = laser[1], vz = laser[2];
+  const double c = src_c * laser[6];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % nx), iy = (int)((i / nx) % ny), iz = (int)(i / ((long long)nx * ny));
+    F[i] += (real)(c * src_factor(ix, nx, ox, hx, vx, rsq) * src_factor(iy, ny, oy, hy, vy, rsq) *
+                   src_factor(iz, nz, oz, hz, vz, dsq));
+  }
+}
+
+// computeConvRadBC (:2207-2301): flux of the top faces of element plane
+// ne_planes-1 into the nodes of plane ne_planes; one thread per node gathers
+// its (up to four) faces.
+template <typename real>
+__global__ void surface_kernel(int nx, int ny, int kt, double hx, double hy, const real* T, real* F, const Props<real> p) {
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;
+  const long long nxy = (long long)nx * ny;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nxy; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % nx), iy = (int)(i / nx);
+    const real w2 = (real)(hx * hy / 4.0);
+    real acc = 0;
+    for (int fy = iy - 1; fy <= iy; ++fy) {
+      if (fy < 0 || fy >= ny - 1) continue;
+      for (int fx = ix - 1; fx <= ix; ++fx) {
+        if (fx < 0 || fx >= nx - 1) continue;
+        const long long b = fx + (long long)fy * nx + (long long)kt * nxy;
+        const real t00 = T[b], t10 = T[b + 1], t01 = T[b + nx], t11 = T[b + nx + 1];
+        const int ax = ix - fx, ay = iy - fy;
+        for (int qy = 0; qy < 2; ++qy)
+          for (int qx = 0; qx < 2; ++qx) {
+            const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ, py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
+            const real Tq = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
+            const real q = surface_flux(p, Tq) * w2;
+            acc += (ax ? px1 : px0) * (ay ? py1 : py0) * q;
+          }
+      }
+    }
+    F[i + (long long)kt * nxy] += acc;
+  }
+}
+
+inline int lgrid(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace gm
+
+extern "C" int gm_state_properties(const gm_state_props_args* a, const gm_props* p, void* stream) {
+  if (!a || !p || !a->T || a->n < 0 || a->ph_in == a->ph_out) return GM_ERR_ARG;
+  if ((a->k_out == nullptr) != (a->rc_out == nullptr)) return GM_ERR_ARG;
+  if (a->n == 0) return GM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a->dtype == GM_F32)
+    gm::state_props_kernel<float><<<gm::lgrid(a->n), 256, 0, st>>>(a->n, (const float*)a->T, a->ph_in, a->ph_out,
+                                                                    (float*)a->k_out, (float*)a->rc_out, a->substrate,
+                                                                    gm::make_props<float>(*p));
+  else if (a->dtype == GM_F64)
+    gm::state_props_kernel<double><<<gm::lgrid(a->n), 256, 0, st>>>(a->n, (const double*)a->T, a->ph_in, a->ph_out,
+                                                                     (double*)a->k_out, (double*)a->rc_out,
+                                                                     a->substrate, gm::make_props<double>(*p));
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_fine_source(int dtype, const int nodes[3], const double origin[3], const double h[3],
+                              const double* laser, const gm_props* p, void* F, void* stream) {
+  if (!nodes || !origin || !h || !laser || !p || !F || nodes[0] < 2 || nodes[1] < 2 || nodes[2] < 2)
+    return GM_ERR_ARG;
+  const double r = p->laser_radius, d = p->laser_depth;
+  const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
+  const double src_c = 6.0 * sqrt(3.0) * p->laser_eta * rc * rc * dc * (h[0] * h[1] * h[2] / 8.0);
+  const long long n = (long long)nodes[0] * nodes[1] * nodes[2];
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GM_F32)
+    gm::fine_source_kernel<float><<<gm::lgrid(n), 256, 0, st>>>(nodes[0], nodes[1], nodes[2], origin[0], origin[1],
+                                                                 origin[2], h[0], h[1], h[2], laser, r * r, d * d,
+                                                                 src_c, (float*)F);
+  else if (dtype == GM_F64)
+    gm::fine_source_kernel<double><<<gm::lgrid(n), 256, 0, st>>>(nodes[0], nodes[1], nodes[2], origin[0], origin[1],
+                                                                  origin[2], h[0], h[1], h[2], laser, r * r, d * d,
+                                                                  src_c, (double*)F);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_surface_flux(int dtype, const int nodes[3], const double h[3], int ne_planes, const void* T,
+                               const gm_props* p, void* F, void* stream) {
+  if (!nodes || !h || !T || !p || !F || nodes[0] < 2 || nodes[1] < 2 || ne_planes < 1 || ne_planes > nodes[2] - 1)
+    return GM_ERR_ARG;
+  const long long nxy = (long long)nodes[0] * nodes[1];
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GM_F32)
+    gm::surface_kernel<float><<<gm::lgrid(nxy), 256, 0, st>>>(nodes[0], nodes[1], ne_planes, h[0], h[1],
+                                                               (const float*)T, (float*)F, gm::make_props<float>(*p));
+  else if (dtype == GM_F64)
+    gm::surface_kernel<double><<<gm::lgrid(nxy), 256, 0, st>>>(nodes[0], nodes[1], ne_planes, h[0], h[1],
+                                                                (const double*)T, (double*)F,
+                                                                gm::make_props<double>(*p));
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}

@@ -282,3 +282,24 @@ extern "C" int gm_l0_scatter(const gm_l0_args* g, void* stream) {
                                                                       g->idx[2], g->l0_nx, g->l0_ny, g->l0_s1, g->ph);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
+
+// T = max(T, lo) (the reference's jnp.maximum(T_amb, T) after computeSolutions,
+// stepGOMELT :2360-2362, :2380-2382).
+template <typename real>
+__global__ void clamp_kernel(real* T, long long n, real lo) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    T[i] = fmax(T[i], lo);
+}
+
+extern "C" int gm_clamp_min(int dtype, void* T, long long n, double lo, void* stream) {
+  if (!T || n < 0) return GM_ERR_ARG;
+  if (n == 0) return GM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GM_F32)
+    clamp_kernel<float><<<grid_for(n), 256, 0, st>>>((float*)T, n, (float)lo);
+  else if (dtype == GM_F64)
+    clamp_kernel<double><<<grid_for(n), 256, 0, st>>>((double*)T, n, lo);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}

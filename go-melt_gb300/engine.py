@@ -340,7 +340,7 @@ class Engine:
     # ------------------------------------------------------------------
     # subcycleGOMELT (:3224-3632)
     # ------------------------------------------------------------------
-    def subcycle(self, laser_rows, history=False):
+    def subcycle(self, laser_rows, history=False, rows_device=None):
         g = self.geo
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         N2, N3 = self.N2, self.N3
@@ -349,8 +349,11 @@ class Engine:
         if self.tmp is None:
             raise N.GomeltError("active Level-1 region not set (call set_layer first)")
         dts = np.concatenate([[rows_h[:, 5].sum()], rows_h[:, 5].reshape(N2, N3).sum(axis=1)])
-        rows = self._buf("rows", rows_h.size, torch.float64).view(N2 * N3, 7)
-        rows.copy_(torch.from_numpy(rows_h), non_blocking=False)
+        if rows_device is not None:
+            rows = rows_device
+        else:
+            rows = self._buf("rows", rows_h.size, torch.float64).view(N2 * N3, 7)
+            rows.copy_(torch.from_numpy(rows_h), non_blocking=False)
         dtd = self._buf("dts", N2 + 1, torch.float64)
         dtd.copy_(torch.from_numpy(dts))
         tb = self.tables
@@ -441,6 +444,104 @@ class Engine:
         T1s.copy_(T1c)
         self.l0_scatter()
         return out_hist
+
+    # ------------------------------------------------------------------
+    # stepGOMELT (:2304-2397) and stepGOMELTDwellTime (:2617-2664)
+    # ------------------------------------------------------------------
+    def _state_props(self, lev, T, ph_in, ph_out):
+        a = N.gm_state_props_args()
+        a.dtype = kern.dtype_code(T)
+        a.n = T.numel()
+        a.T = kern.ptr(T)
+        a.ph_in = C.cast(ph_in.data_ptr(), C.POINTER(C.c_uint8))
+        a.ph_out = C.cast(ph_out.data_ptr(), C.POINTER(C.c_uint8))
+        a.substrate = self.substrate[lev]
+        N.call("gm_state_properties", C.byref(a), C.byref(self.ps), kern.stream_ptr(self.stream))
+
+    def _clamp(self, T):
+        N.call("gm_clamp_min", kern.dtype_code(T), kern.ptr(T), C.c_longlong(T.numel()),
+               C.c_double(float(self.P["T_amb"])), kern.stream_ptr(self.stream))
+
+    def step(self, v):
+        """One equal-dt step of all levels, predictor + corrector.  v: laser row
+        (x, y, z, ..., dt at [5], P at [6]).  Returns the newly-melted mask of
+        Level 3 (the reference's resetmask) as a device bool tensor."""
+        g = self.geo
+        L1, L2, L3 = g.L[1], g.L[2], g.L[3]
+        if self.tmp is None:
+            raise N.GomeltError("active Level-1 region not set (call set_layer first)")
+        row = self._buf("steprow", 7, torch.float64)
+        row.copy_(torch.as_tensor(np.asarray(v, dtype=np.float64)[:7]))
+        dtd = row[5:6]
+        tb = self.tables
+        c32, c31, c21 = tb["c32"], tb["c31"], tb["c21"]
+        T1s, T2s, T3s = self.T[1], self.T[2], self.T[3]
+        Tp2s, Tp3s = self.Tp[2], self.Tp[3]
+        ph1, ph2s, ph3s = self.ph[1], self.ph[2], self.ph[3]
+        nn1, nn2, nn3 = L1.nn, L2.nn, L3.nn
+        pre3 = self._buf("pre_ph3", nn3, torch.uint8)
+        pre3.copy_(ph3s)
+        # updateStateProperties (:2513-2564)
+        phn = self._buf("stph3", nn3, torch.uint8)
+        self._state_props(3, T3s, ph3s, phn)
+        ph3s.copy_(phn)
+        phn2 = self._buf("stph2", nn2, torch.uint8)
+        self._state_props(2, T2s, ph2s, phn2)
+        ph2s.copy_(phn2)
+        self._s1_restrict()
+        # sources (computeSources :928-988) and subgrid flux terms (:1477-1565)
+        rhs1 = self._buf("rhs1", int(np.prod(c21.box_n)))
+        rhs2 = self._buf("rhs2", int(np.prod(c32.box_n)))
+        rhs1.zero_()
+        rhs2.zero_()
+        self._coarse_source(c31, row, 1, rhs1, c21.box_lo, c21.box_n)
+        self._coarse_source(c32, row, 1, rhs2, c32.box_lo, c32.box_n)
+        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, Tp=Tp3s)
+        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, Tp=Tp2s)
+        self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3s, ph=ph3s, Tp=Tp3s)
+        box1 = [c21.box_lo[0], c21.box_lo[0] + c21.box_n[0], c21.box_lo[1], c21.box_lo[1] + c21.box_n[1],
+                c21.box_lo[2], c21.box_lo[2] + c21.box_n[2]]
+        box2 = [c32.box_lo[0], c32.box_lo[0] + c32.box_n[0], c32.box_lo[1], c32.box_lo[1] + c32.box_n[1],
+                c32.box_lo[2], c32.box_lo[2] + c32.box_n[2]]
+
+        def solutions(T1o, T2o, T3o):
+            # computeSolutions (:2135-2204): the coarse results feed the finer
+            # Dirichlet rings before the T >= T_amb clamp
+            self._level(1, T1s, T1o, dtd, ph1, None, rhs=rhs1, box=box1, clamp=False)
+            self._level(2, T2s, T2o, dtd, ph2s, None, rhs=rhs2, box=box2, bc_new=T1o, bc_old=T1o, alpha=1.0,
+                        clamp=False)
+            self._level(3, T3s, T3o, dtd, ph3s, None, laser=row, bc_new=T2o, bc_old=T2o, alpha=1.0, clamp=False)
+            for T in (T1o, T2o, T3o):
+                self._clamp(T)
+
+        T1p, T2p, T3p = self._buf("T1p", nn1), self._buf("T2a", nn2), self._buf("T3a", nn3)
+        solutions(T1p, T2p, T3p)
+        Tp3n, Tp2n = self._buf("tp3w0", nn3), self._buf("Tp2w", nn2)
+        self._new_tprime(3, T3p, T2p, Tp3n)
+        self._new_tprime(2, T2p, T1p, Tp2n)
+        # mass terms (:1396-1474)
+        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, dTa=Tp3n, dTb=Tp3s, dt=dtd)
+        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, dTa=Tp2n, dTb=Tp2s, dt=dtd)
+        self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3s, ph=ph3s, dTa=Tp3n, dTb=Tp3s, dt=dtd)
+        T1c, T2c, T3c = self._buf("T1c", nn1), self._buf("T2b", nn2), self._buf("T3b", nn3)
+        solutions(T1c, T2c, T3c)
+        self._new_tprime(3, T3c, T2c, Tp3s)
+        self._new_tprime(2, T2c, T1c, Tp2s)
+        T3s.copy_(T3c)
+        T2s.copy_(T2c)
+        T1s.copy_(T1c)
+        self.l0_scatter()
+        return ((ph3s & PH_S2) != 0) & ((pre3 & PH_S2) == 0)
+
+    def dwell(self, dt):
+        """Level 1 only, surface flux, no source, no clamp (stepGOMELTDwellTime)."""
+        if self.tmp is None:
+            raise N.GomeltError("active Level-1 region not set (call set_layer first)")
+        dtd = self._buf("dwelldt", 1, torch.float64)
+        dtd.fill_(float(dt))
+        T1w = self._buf("T1p", self.geo.L[1].nn)
+        self._level(1, self.T[1], T1w, dtd, self.ph[1], None, clamp=False)
+        self.T[1].copy_(T1w)
 
     # ------------------------------------------------------------------
     # state set-up

@@ -1,0 +1,74 @@
+"""Input files (the reference's JSON schema) of the benchmark workloads.
+
+All use a constant-property material (k = 22 W/mK, rho = 4400 kg/m^3,
+cp = 700 J/kgK in every phase), a 200 W Gaussian laser of radius 50 um and
+absorptivity 0.35 moving at 1 m/s, convection h = 10 W/m^2K and radiation with
+emissivity 0.3 on the top surface, 300 K Dirichlet faces and 300 K initial
+temperature.  The reference always adds evaporation (computeConvRadBC,
+go_melt/computeFunctions.py:2284-2287); these workloads name convection and
+radiation only, so evaporation_coefficient = 0.  laser_depth is not given by
+the workload descriptions: the reference default 0.05 mm is used.
+
+The fine time step is 0.9 x the explicit limit of the lumped hex8 operator on
+the finest level, h^2 / (2 alpha) with alpha = k / (rho cp): 1.575 us at 5 um.
+Level-2 and Level-1 steps are 10x and 100x longer (N2 = N3 = 10).
+"""
+
+from __future__ import annotations
+
+import copy
+
+MATERIAL = {
+    "thermal_conductivity_powder": 22.0, "thermal_conductivity_bulk_a0": 22.0,
+    "thermal_conductivity_bulk_a1": 0.0, "thermal_conductivity_fluid_a0": 22.0,
+    "heat_capacity_solid_a0": 700.0, "heat_capacity_solid_a1": 0.0, "heat_capacity_mushy": 700.0,
+    "heat_capacity_fluid": 700.0, "density": 4.4e-6,
+    "laser_radius": 0.05, "laser_depth": 0.05, "laser_power": 200.0, "laser_absorptivity": 0.35,
+    "T_amb": 300.0, "T_solidus": 1878.0, "T_liquidus": 1900.0, "T_boiling": 3038.0,
+    "h_conv": 1e-5, "emissivity": 0.3, "evaporation_coefficient": 0.0, "layer_height": 0.05,
+}
+
+ALPHA = 0.022 / (4.4e-6 * 700.0)  # mm^2/s
+
+
+def dt_fine(h):
+    return 0.9 * h * h / (2.0 * ALPHA)
+
+
+def _cond(T=300.0):
+    return {"x": [T, T], "y": [T, T], "z": [T, T]}
+
+
+def config0():
+    """Single 4 mm track on a 5x5x1 mm block (L1 50x50x10 @ 100 um, L2 1x1x0.2 mm
+    window 50x50x10 @ 20 um, L3 0.4x0.4x0.1 mm window 80x80x20 @ 5 um)."""
+    return {
+        "Level1": {"elements": [50, 50, 10], "bounds": {"x": [0.0, 5.0], "y": [0.0, 5.0], "z": [-1.0, 0.0]},
+                   "conditions": _cond()},
+        "Level2": {"elements": [50, 50, 10], "bounds": {"x": [0.0, 1.0], "y": [2.0, 3.0], "z": [-0.2, 0.0]}},
+        "Level3": {"elements": [80, 80, 20], "bounds": {"x": [0.3, 0.7], "y": [2.3, 2.7], "z": [-0.1, 0.0]}},
+        "properties": dict(copy.deepcopy(MATERIAL), laser_center=[0.5, 2.5, 0.0, 0, 0, 0, 0]),
+        "nonmesh": {"timestep_L3": dt_fine(0.005), "subcycle_num_L2": 10, "subcycle_num_L3": 10,
+                    "laser_velocity": 1000.0, "output_files": 0, "wait_time": 10, "dwell_time": 1e-4,
+                    "info_T": 0},
+        "gcode": "G0 X0.5 Y2.5 Z0.0\nG1 X4.5 Y2.5 Z0.0\n",
+    }
+
+
+def config1():
+    """Part-scale raster: L1 20x20x5 mm, 200x200x50 @ 100 um; L2 2x2x0.3 mm window,
+    100x100x15 @ 20 um; L3 0.8x0.8x0.2 mm window, 160x160x40 @ 5 um (element counts:
+    with these the windows sit on the coarser grids' nodes, which the reference's
+    overlap and restriction logic needs); serpentine tracks 100 um apart, centred
+    in the part, first layer."""
+    return {
+        "Level1": {"elements": [200, 200, 50], "bounds": {"x": [0.0, 20.0], "y": [0.0, 20.0], "z": [-5.0, 0.0]},
+                   "conditions": _cond()},
+        "Level2": {"elements": [100, 100, 15], "bounds": {"x": [9.0, 11.0], "y": [9.0, 11.0], "z": [-0.3, 0.0]}},
+        "Level3": {"elements": [160, 160, 40], "bounds": {"x": [9.6, 10.4], "y": [9.6, 10.4], "z": [-0.2, 0.0]}},
+        "properties": dict(copy.deepcopy(MATERIAL), laser_center=[10.0, 10.0, 0.0, 0, 0, 0, 0]),
+        "nonmesh": {"timestep_L3": dt_fine(0.005), "subcycle_num_L2": 10, "subcycle_num_L3": 10,
+                    "laser_velocity": 1000.0, "output_files": 0, "wait_time": 10, "dwell_time": 1e-4,
+                    "info_T": 0},
+        "raster": {"x0": 8.0, "y0": 8.0, "length": 4.0, "hatch": 0.1, "ntracks": 40},
+    }

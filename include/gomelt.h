@@ -100,6 +100,34 @@ typedef struct gm_level_args {
 
 int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream);
 
+/* Phase update and material properties per node (computeStateProperties,
+ * :2567-2614): ph_out = (S1 | S2) from T and ph_in (S1 forced below
+ * `substrate`); optional k [W/(mm K)] and rho*cp.  ph_out must not alias
+ * ph_in. */
+typedef struct gm_state_props_args {
+  int dtype;
+  long long n;
+  const void* T;
+  const uint8_t* ph_in;
+  uint8_t* ph_out;
+  void* k_out;
+  void* rc_out;
+  long long substrate;
+} gm_state_props_args;
+
+int gm_state_properties(const gm_state_props_args* a, const gm_props* p, void* stream);
+
+/* Fine-level Gaussian source assembled on the nodes, added into F
+ * (computeSourcesL3, :2960-3012).  laser: device row (x,y,z,...,P at [6]). */
+int gm_fine_source(int dtype, const int nodes[3], const double origin[3], const double h[3], const double* laser,
+                   const gm_props* p, void* F, void* stream);
+
+/* Convection + radiation + evaporation flux of the top faces of element plane
+ * ne_planes-1, added into F at node plane ne_planes (computeConvRadBC,
+ * :2207-2301). */
+int gm_surface_flux(int dtype, const int nodes[3], const double h[3], int ne_planes, const void* T, const gm_props* p,
+                    void* F, void* stream);
+
 /* Separable gather over a tensor grid of target points:
  *   out = base + sum_k coef[k] * I_k(src[k]),  k < nterms <= 3
  * and optionally out_term = I_which_term(src[which_term]).
@@ -176,6 +204,10 @@ typedef struct gm_l0_args {
   const uint8_t* prev_ph; /* gather only; NULL: no S2 anywhere */
   int prev_lo[3], prev_n[3];
 } gm_l0_args;
+
+/* T = max(T, lo) over n values (the T >= T_amb clamp of stepGOMELT,
+ * :2360-2362, :2380-2382). */
+int gm_clamp_min(int dtype, void* T, long long n, double lo, void* stream);
 
 int gm_l0_gather(const gm_l0_args* a, void* stream);
 int gm_l0_scatter(const gm_l0_args* a, void* stream);

@@ -105,3 +105,48 @@ def test_move_golden(case, n, dtype, tol):
     if pre + ".in.v" not in g:
         pytest.skip("no such call")
     _move(g, pre, dtype, tol)
+
+
+@pytest.mark.parametrize("dtype,tol", TOL)
+@pytest.mark.parametrize("n", [0, 1])
+def test_step_golden(case, n, dtype, tol):
+    g = golden(case)
+    pre = f"step{n}"
+    if pre + ".in.v" not in g:
+        pytest.skip("no such call")
+    Lin = stateio.unflatten(g, pre + ".in.Levels")
+    eng = make_engine(g, Lin, dtype)
+    eng.tmp = tup(g, pre + ".in.tmp_ne_nn")
+    eng.substrate = tup(g, pre + ".in.substrate")
+    v = np.array(g[pre + ".in.v"], dtype=float)
+    v[5] = float(g[pre + ".in.dt"])
+    v[6] = float(g[pre + ".in.laserP"])
+    reset = eng.step(v)
+    torch.cuda.synchronize()
+    Lr = stateio.unflatten(g, pre + ".out.Levels")
+    out = eng.fields_numpy()
+    Tscale = max(float(np.max(Lr[lev]["T0"])) for lev in (1, 2, 3))
+    for lev in (1, 2, 3):
+        assert relT(out[lev]["T0"], Lr[lev]["T0"]) < tol, lev
+        np.testing.assert_array_equal(out[lev]["S1"], np.asarray(Lr[lev]["S1"]) > 0.499)
+    for lev in (2, 3):
+        assert absdiff(out[lev]["Tprime0"], Lr[lev]["Tprime0"], Tscale) < tol, lev
+    np.testing.assert_array_equal(out[3]["S2"], np.asarray(Lr[3]["S2"]).astype(bool))
+    np.testing.assert_array_equal(out[0]["S1"], np.asarray(Lr[0]["S1"]) > 0.499)
+    np.testing.assert_array_equal(reset.cpu().numpy(), g[pre + ".out.resetmask"])
+
+
+@pytest.mark.parametrize("dtype,tol", TOL)
+def test_dwell_golden(case, dtype, tol):
+    g = golden(case)
+    pre = "dwell0"
+    if pre + ".in.dt" not in g:
+        pytest.skip("no dwell step")
+    Lin = stateio.unflatten(g, pre + ".in.Levels")
+    eng = make_engine(g, Lin, dtype)
+    eng.tmp = tup(g, pre + ".in.tmp_ne_nn")
+    eng.substrate = tup(g, pre + ".in.substrate")
+    eng.dwell(float(g[pre + ".in.dt"]))
+    torch.cuda.synchronize()
+    Lr = stateio.unflatten(g, pre + ".out.Levels")
+    assert relT(eng.T[1].double().cpu().numpy(), Lr[1]["T0"]) < tol
