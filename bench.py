@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--cpu-steps", type=int, default=8, help="oracle fine steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="run only the Level-3 level-step kernel --steps times (for profiling)")
     return ap.parse_args()
 
 
@@ -364,9 +366,38 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_kernel_only(args):
+    """The dominant kernel alone on the workload's Level-3 window after
+    --warmup subcycle calls (the case the ncu summaries under profiles/ use)."""
+    import numpy as np
+    import torch
+
+    import engine
+
+    cfg, P, nm, rows = workload()
+    N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
+    n23 = N2 * N3
+    eng = engine.Engine(cfg, P, N2, N3, dtype=torch.float32 if args.dtype == "f32" else torch.float64)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    eng.set_layer(rows[0])
+    for k in range(args.warmup):
+        eng.move(rows[k * n23], vstart)
+        eng.subcycle(rows[k * n23:(k + 1) * n23])
+    last = torch.as_tensor(rows[args.warmup * n23 - 1], device=eng.dev)
+    Tout = torch.empty_like(eng.T[3])
+    phout = torch.empty_like(eng.ph[3])
+    for _ in range(args.steps):
+        eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, bc_new=eng.T[2], bc_old=eng.T[2],
+                   alpha=1.0)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel_only": "level_step_kernel (Level 3)", "launches": args.steps, "nodes": eng.geo.L[3].nn}))
+
+
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.kernel_only:
+        run_kernel_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -104,6 +104,38 @@ class gm_coarse_source_args(C.Structure):
                 ("out_n", C.c_int * 3), ("scratch", vp), ("scratch_cap", C.c_longlong)]
 
 
+class gm_window(C.Structure):
+    _fields_ = [("nodes", C.c_int * 3), ("h", C.c_double * 3), ("origin", C.c_double * 3),
+                ("substrate", C.c_longlong), ("T", vp), ("Tp", vp), ("ph", C.POINTER(C.c_uint8))]
+
+
+_P_INT = C.POINTER(C.c_int)
+_P_DBL = C.POINTER(C.c_double)
+_P_U8 = C.POINTER(C.c_uint8)
+
+
+class gm_subcycle_plan(C.Structure):
+    _fields_ = [
+        ("dtype", C.c_int), ("N2", C.c_int), ("N3", C.c_int), ("L1", gm_window), ("L2", gm_window),
+        ("L3", gm_window), ("L1_ne_planes", C.c_int), ("face", C.c_double * 5), ("acc3", vp), ("macc3", vp),
+        ("bc12", gm_map3), ("bc23", gm_map3), ("r32", gm_map3), ("r21", gm_map3), ("r32_idx", _P_INT * 3),
+        ("r21_idx", _P_INT * 3), ("c32", gm_couple_geom), ("c31", gm_couple_geom), ("c21", gm_couple_geom),
+        ("xq32", _P_DBL * 3), ("xq31", _P_DBL * 3), ("rhs1_lo", C.c_int * 3), ("rhs1_n", C.c_int * 3),
+        ("rhs2_lo", C.c_int * 3), ("rhs2_n", C.c_int * 3), ("L0", _P_U8), ("L0_nx", C.c_longlong),
+        ("L0_ny", C.c_longlong), ("l0_idx3", _P_INT * 3), ("rows", vp), ("dts", vp), ("T1p", vp), ("T1c", vp),
+        ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
+        ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
+        ("src_scratch", vp), ("src_cap", C.c_longlong), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
+        ("zchunk", C.c_int)]
+
+
+def subcycle_kernel_count(N2: int, N3: int) -> int:
+    """Kernels gm_subcycle launches: set-up and Level 1 (8), two passes of
+    N2 Level-2 steps (coupling 2, source 2, Level-2 solve, N3 Level-3 solves,
+    restriction, T'), the T'2/mass/corrector block (7) and the tail (3)."""
+    return 18 + 2 * N2 * (7 + N3)
+
+
 _lib = None
 
 
@@ -145,6 +177,7 @@ SIGNATURES = {
     "gm_l0_scatter": [C.POINTER(gm_l0_args), vp],
     "gm_couple": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
+    "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
 }
 
 
@@ -166,9 +199,9 @@ def launch_count() -> int:
     return _launches[0]
 
 
-def call(name: str, *args):
+def call(name: str, *args, kernels=None):
     check(getattr(lib(), name)(*args), name)
-    _launches[0] += KERNELS_PER_CALL.get(name, 1)
+    _launches[0] += kernels if kernels is not None else KERNELS_PER_CALL.get(name, 1)
 
 
 def props_struct(p: dict) -> gm_props:

@@ -284,17 +284,18 @@ __global__ void coarse_source_tables(int np, const double* rows, int n0, int n1,
       r -= n0 + 1 + n1 + 1; d = 2; ncb = n2; xq = xq2; cw = cw2; flo = flo2; fhi = fhi2; s2 = dsq;
     }
     const double v = rows[p * 7 + d];
-    double acc = 0.0;
+    const double inv2 = 1.0 / s2;
+    real acc = 0;
     for (int c = r - 1; c <= r; ++c) {
       if (c < 0 || c >= ncb) continue;
       const int A = r - c;
       for (int e = flo[c]; e < fhi[c]; ++e)
         for (int s = 0; s < 2; ++s) {
-          const double dx = xq[e * 2 + s] - v;
-          acc += (double)cw[(e * 2 + s) * 2 + A] * exp(-3.0 * dx * dx / s2);
+          const double dx = xq[e * 2 + s] - v;  // offset in double, exponential in the kernel's precision
+          acc += cw[(e * 2 + s) * 2 + A] * exp((real)(-3.0 * dx * dx * inv2));
         }
     }
-    S[t] = (real)acc;
+    S[t] = acc;
   }
 }
 

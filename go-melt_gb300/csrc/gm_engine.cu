@@ -1,0 +1,329 @@
+// Native orchestration of the multilevel step: the whole subcycleGOMELT
+// (go_melt/computeFunctions.py:3224-3632) issued from C++ on one stream.
+//
+// Sequence (N2 Level-2 steps of N3 Level-3 steps each, predictor then
+// corrector, as the reference's two lax.scan passes):
+//   Level-1 S1 from Level 2 at the overlap (:3272-3278)
+//   Level-1 RHS = source over all rows + T' fluxes of L3 and L2 (:3285-3292)
+//   Level-1 predictor (:3294-3305)
+//   pass 1: per Level-2 step: Level-2 RHS (source of its rows + L3 T' flux),
+//           Level-2 solve with the blended Level-1 ring, N3 Level-3 solves with
+//           the blended Level-2 ring, restriction + T'3 (:3307-3430)
+//   T'2, Level-1 mass terms, Level-1 corrector (:3432-3456)
+//   pass 2: as pass 1 from the saved state, plus the Level-2 mass term and the
+//           Level-3 melt-time update (:3458-3622)
+//   final T'2 / Level-1 restriction, Level-0 S1 store (:3625-3630)
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include "gomelt.h"
+
+namespace {
+
+struct Ctx {
+  const gm_subcycle_plan* p;
+  const gm_props* pr;
+  void* st;
+  size_t esz;
+  int rc = GM_OK;
+};
+
+inline char* at(void* base, long long elems, size_t esz) { return (char*)base + elems * (long long)esz; }
+inline long long nn(const gm_window& w) { return (long long)w.nodes[0] * w.nodes[1] * w.nodes[2]; }
+
+#define GM_TRY(expr)             \
+  do {                           \
+    if (c.rc == GM_OK) {         \
+      int _r = (expr);           \
+      if (_r != GM_OK) c.rc = _r; \
+    }                            \
+  } while (0)
+
+void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tout, const double* dt,
+           const uint8_t* phin, uint8_t* phout, const void* rhs, const int lo[3], const int n[3],
+           const double* laser, int bc_mode, const gm_map3* map, const void* bnew, const void* bold, double alpha,
+           void* acc, void* macc) {
+  const gm_subcycle_plan& p = *c.p;
+  gm_level_args a;
+  memset(&a, 0, sizeof(a));
+  a.dtype = p.dtype;
+  a.nx = w.nodes[0];
+  a.ny = w.nodes[1];
+  a.nz = w.nodes[2];
+  for (int d = 0; d < 3; ++d) {
+    a.h[d] = w.h[d];
+    a.origin[d] = w.origin[d];
+  }
+  a.ne_planes = ne_planes;
+  a.dt = dt;
+  a.T_in = Tin;
+  a.T_out = Tout;
+  a.ph_in = phin;
+  a.ph_out = phout;
+  a.substrate = w.substrate;
+  if (rhs) {
+    a.rhs_box = rhs;
+    for (int d = 0; d < 3; ++d) {
+      a.box[2 * d] = lo[d];
+      a.box[2 * d + 1] = lo[d] + n[d];
+    }
+  }
+  a.laser = laser;
+  a.surface = 1;
+  a.bc_mode = bc_mode;
+  if (bc_mode == 1) {
+    for (int i = 0; i < 5; ++i) a.face[i] = p.face[i];
+    a.inactive_amb = 1;
+  } else if (bc_mode == 2) {
+    a.bc_new = bnew;
+    a.bc_old = bold;
+    a.bc_alpha = alpha;
+    a.bc_beta = 1.0 - alpha;
+    a.bc_map = *map;
+  }
+  a.clamp = 1;
+  a.accum = acc;
+  a.max_accum = macc;
+  a.zchunk = p.zchunk;
+  GM_TRY(gm_level_step(&a, c.pr, c.st));
+}
+
+void couple(Ctx& c, const gm_couple_geom& g, const gm_window& fine, void* out, const int lo[3], const int n[3],
+            const void* Tp, const void* dTa, const void* dTb, const double* dt) {
+  const gm_subcycle_plan& p = *c.p;
+  gm_couple_args a;
+  memset(&a, 0, sizeof(a));
+  a.dtype = p.dtype;
+  a.geom = g;
+  for (int d = 0; d < 3; ++d) {
+    a.fine_nodes[d] = fine.nodes[d];
+    a.fine_h[d] = fine.h[d];
+    a.out_lo[d] = lo[d];
+    a.out_n[d] = n[d];
+  }
+  a.T = fine.T;
+  a.ph = fine.ph;
+  a.substrate = fine.substrate;
+  a.Tp = Tp;
+  a.dTa = dTa;
+  a.dTb = dTb;
+  a.dt = dt;
+  a.out = out;
+  a.scale = 1.0;
+  a.partials = p.partials;
+  a.partials_cap = p.partials_cap;
+  GM_TRY(gm_couple(&a, c.pr, c.st));
+}
+
+// couple() reads the fine level's T/phase from the window; the passes use
+// carried fields instead, so this variant takes them explicitly.
+void couple_fields(Ctx& c, const gm_couple_geom& g, const gm_window& fine, const void* T, const uint8_t* ph,
+                   void* out, const int lo[3], const int n[3], const void* Tp, const void* dTa, const void* dTb,
+                   const double* dt) {
+  gm_window w = fine;
+  w.T = (void*)T;
+  w.ph = (uint8_t*)ph;
+  couple(c, g, w, out, lo, n, Tp, dTa, dTb, dt);
+}
+
+void source(Ctx& c, const gm_couple_geom& g, const double* const xq[3], const double* rows, int npos, void* out,
+            const int lo[3], const int n[3]) {
+  const gm_subcycle_plan& p = *c.p;
+  gm_coarse_source_args a;
+  memset(&a, 0, sizeof(a));
+  a.dtype = p.dtype;
+  a.geom = g;
+  a.npos = npos;
+  a.rows = rows;
+  for (int d = 0; d < 3; ++d) {
+    a.xq[d] = xq[d];
+    a.out_lo[d] = lo[d];
+    a.out_n[d] = n[d];
+  }
+  a.fine_wq = p.L3.h[0] * p.L3.h[1] * p.L3.h[2] / 8.0;
+  a.out = out;
+  a.scratch = p.src_scratch;
+  a.scratch_cap = p.src_cap;
+  GM_TRY(gm_coarse_source(&a, c.pr, c.st));
+}
+
+// getNewTprime (:2060-2099): restrict the fine field into coarse_T, then
+// T' = T_f - I(T_c).
+void new_tprime(Ctx& c, const gm_map3& rmap, const int* const idx[3], const gm_window& coarse, const gm_map3& cmap,
+                const gm_window& fine, const void* fineT, void* coarseT, void* outTp) {
+  const gm_subcycle_plan& p = *c.p;
+  gm_restrict_args r;
+  memset(&r, 0, sizeof(r));
+  r.dtype = p.dtype;
+  for (int d = 0; d < 3; ++d) {
+    r.n[d] = rmap.n[d];
+    r.cidx[d] = idx[d];
+  }
+  r.map = rmap;
+  r.cnx = coarse.nodes[0];
+  r.cny = coarse.nodes[1];
+  r.fine = fineT;
+  r.coarse = coarseT;
+  GM_TRY(gm_restrict(&r, c.st));
+  gm_interp_args a;
+  memset(&a, 0, sizeof(a));
+  a.dtype = p.dtype;
+  for (int d = 0; d < 3; ++d) a.n[d] = fine.nodes[d];
+  a.nterms = 1;
+  a.map[0] = cmap;
+  a.src[0] = coarseT;
+  a.coef[0] = -1.0;
+  a.base = fineT;
+  a.out = outTp;
+  GM_TRY(gm_interp(&a, c.st));
+}
+
+void memzero(Ctx& c, void* ptr, long long elems) {
+  if (c.rc != GM_OK) return;
+  if (cudaMemsetAsync(ptr, 0, elems * c.esz, (cudaStream_t)c.st) != cudaSuccess) c.rc = GM_ERR_CUDA;
+}
+
+void copy(Ctx& c, void* dst, const void* src, long long bytes) {
+  if (c.rc != GM_OK || dst == src) return;
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)c.st) != cudaSuccess)
+    c.rc = GM_ERR_CUDA;
+}
+
+struct PassOut {
+  void* T2;
+  uint8_t* ph2;
+  void* T3;
+  uint8_t* ph3;
+  void* Tp3;
+};
+
+// One pass over the N2 Level-2 steps (subcycleL2_Part1 / subcycleL2_Part2).
+PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
+  const gm_subcycle_plan& p = *c.p;
+  const int N2 = p.N2, N3 = p.N3;
+  const long long n3 = nn(p.L3);
+  void* T2c = p.L2.T;
+  uint8_t* ph2c = p.L2.ph;
+  void* T3c = p.L3.T;
+  uint8_t* ph3c = p.L3.ph;
+  void* Tp3c = p.L3.Tp;
+  const long long nrhs2 = (long long)p.rhs2_n[0] * p.rhs2_n[1] * p.rhs2_n[2];
+  for (int l2 = 0; l2 < N2; ++l2) {
+    void* hist_l2 = at(p.tp3hist, l2 * n3, c.esz);
+    const double* dt2 = p.dts + 1 + l2;
+    memzero(c, p.rhs2, nrhs2);
+    if (part2)
+      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, hist_l2, Tp3c, dt2);
+    else
+      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, nullptr, nullptr, nullptr);
+    source(c, p.c32, p.xq32, p.rows + (long long)l2 * N3 * 7, N3, p.rhs2, p.rhs2_lo, p.rhs2_n);
+    void* T2n = p.T2w[l2 % 2];
+    uint8_t* ph2n = p.ph2w[l2 % 2];
+    level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 2, &p.bc12,
+          T1new, p.L1.T, (l2 + 1) / (double)N2, nullptr, nullptr);
+    for (int l3 = 0; l3 < N3; ++l3) {
+      const int i = l2 * N3 + l3;
+      void* Tn = p.T3w[i % 2];
+      uint8_t* phn = p.ph3w[i % 2];
+      const double* row = p.rows + (long long)i * 7;
+      level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 2, &p.bc23, T2n,
+            T2c, (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr);
+      T3c = Tn;
+      ph3c = phn;
+    }
+    void* Tp3n = part2 ? p.tp3w[l2 % 2] : hist_l2;
+    new_tprime(c, p.r32, p.r32_idx, p.L2, p.bc23, p.L3, T3c, T2n, Tp3n);
+    if (part2 && p.L2all) {
+      copy(c, at(p.L2all, (long long)l2 * nn(p.L2), c.esz), T2n, nn(p.L2) * c.esz);
+      copy(c, at(p.L3all, l2 * n3, c.esz), T3c, n3 * c.esz);
+      copy(c, at(p.L3pall, l2 * n3, c.esz), Tp3n, n3 * c.esz);
+    }
+    Tp3c = Tp3n;
+    T2c = T2n;
+    ph2c = ph2n;
+  }
+  return PassOut{T2c, ph2c, T3c, ph3c, Tp3c};
+}
+
+bool plan_ok(const gm_subcycle_plan* p) {
+  if (!p || p->N2 < 1 || p->N3 < 1 || !p->rows || !p->dts) return false;
+  const gm_window* ws[3] = {&p->L1, &p->L2, &p->L3};
+  for (auto w : ws)
+    if (!w->T || !w->ph || w->nodes[0] < 2 || w->nodes[1] < 2 || w->nodes[2] < 2) return false;
+  if (!p->L2.Tp || !p->L3.Tp || !p->acc3 || !p->macc3) return false;
+  if (!p->T1p || !p->T1c || !p->T2w[0] || !p->T2w[1] || !p->T3w[0] || !p->T3w[1] || !p->tp3w[0] || !p->tp3w[1] ||
+      !p->Tp2w || !p->rhs1 || !p->rhs2 || !p->tp3hist || !p->ph2w[0] || !p->ph2w[1] || !p->ph3w[0] || !p->ph3w[1] ||
+      !p->partials || !p->src_scratch || !p->L0)
+    return false;
+  if ((p->L2all == nullptr) != (p->L3all == nullptr) || (p->L2all == nullptr) != (p->L3pall == nullptr)) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
+  if (!plan_ok(p) || !props || (p->dtype != GM_F32 && p->dtype != GM_F64)) return GM_ERR_ARG;
+  Ctx c;
+  c.p = p;
+  c.pr = props;
+  c.st = stream;
+  c.esz = p->dtype == GM_F32 ? 4 : 8;
+  const long long n1 = nn(p->L1), n2 = nn(p->L2), n3 = nn(p->L3);
+  const long long nrhs1 = (long long)p->rhs1_n[0] * p->rhs1_n[1] * p->rhs1_n[2];
+
+  // Level-1 S1 from Level 2 at the overlap, substrate forced
+  gm_restrict_s1_args s1;
+  memset(&s1, 0, sizeof(s1));
+  s1.dtype = p->dtype;
+  for (int d = 0; d < 3; ++d) {
+    s1.n[d] = p->r21.n[d];
+    s1.cidx[d] = p->r21_idx[d];
+  }
+  s1.map = p->r21;
+  s1.cnx = p->L1.nodes[0];
+  s1.cny = p->L1.nodes[1];
+  s1.fine_ph = p->L2.ph;
+  s1.coarse_ph = p->L1.ph;
+  s1.substrate = p->L1.substrate;
+  GM_TRY(gm_restrict_s1(&s1, c.st));
+
+  // Level-1 right-hand side and predictor
+  memzero(c, p->rhs1, nrhs1);
+  source(c, p->c31, p->xq31, p->rows, p->N2 * p->N3, p->rhs1, p->rhs1_lo, p->rhs1_n);
+  couple(c, p->c31, p->L3, p->rhs1, p->rhs1_lo, p->rhs1_n, p->L3.Tp, nullptr, nullptr, nullptr);
+  couple(c, p->c21, p->L2, p->rhs1, p->rhs1_lo, p->rhs1_n, p->L2.Tp, nullptr, nullptr, nullptr);
+  level(c, p->L1, p->L1_ne_planes, p->L1.T, p->T1p, p->dts, p->L1.ph, nullptr, p->rhs1, p->rhs1_lo, p->rhs1_n,
+        nullptr, 1, nullptr, nullptr, nullptr, 0.0, nullptr, nullptr);
+
+  // pass 1 (predictor)
+  PassOut o = l2_pass(c, p->T1p, false);
+  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, o.T2, p->T1p, p->Tp2w);
+  couple(c, p->c31, p->L3, p->rhs1, p->rhs1_lo, p->rhs1_n, nullptr, o.Tp3, p->L3.Tp, p->dts);
+  couple(c, p->c21, p->L2, p->rhs1, p->rhs1_lo, p->rhs1_n, nullptr, p->Tp2w, p->L2.Tp, p->dts);
+  level(c, p->L1, p->L1_ne_planes, p->L1.T, p->T1c, p->dts, p->L1.ph, nullptr, p->rhs1, p->rhs1_lo, p->rhs1_n,
+        nullptr, 1, nullptr, nullptr, nullptr, 0.0, nullptr, nullptr);
+
+  // pass 2 (corrector) and the new state
+  o = l2_pass(c, p->T1c, true);
+  copy(c, p->L3.T, o.T3, n3 * c.esz);
+  copy(c, p->L3.ph, o.ph3, n3);
+  copy(c, p->L3.Tp, o.Tp3, n3 * c.esz);
+  copy(c, p->L2.T, o.T2, n2 * c.esz);
+  copy(c, p->L2.ph, o.ph2, n2);
+  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, p->L2.T, p->T1c, p->L2.Tp);
+  copy(c, p->L1.T, p->T1c, n1 * c.esz);
+
+  // Level-0 S1 store at the Level-3 window
+  gm_l0_args l0;
+  memset(&l0, 0, sizeof(l0));
+  for (int d = 0; d < 3; ++d) {
+    l0.n[d] = p->L3.nodes[d];
+    l0.idx[d] = p->l0_idx3[d];
+  }
+  l0.l0_nx = p->L0_nx;
+  l0.l0_ny = p->L0_ny;
+  l0.l0_s1 = p->L0;
+  l0.ph = p->L3.ph;
+  GM_TRY(gm_l0_scatter(&l0, c.st));
+  return c.rc;
+}

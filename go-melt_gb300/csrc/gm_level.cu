@@ -53,7 +53,7 @@ struct LevelK {
   real lam[8];  // Hadamard-mode eigenvalues of K_ref, divided by 8
   real wvol;    // hx*hy*hz/8
   real w2;      // hx*hy/4
-  double rsq, dsq;
+  double inv_r2, inv_d2;
   double src_c;  // 6*sqrt(3)*eta * rc^2 * dc * wvol  (times P)
   Props<real> p;
 };
@@ -92,25 +92,38 @@ __device__ __forceinline__ void bfly_inv(real v[8]) {
 
 // 1-D source factor of node i: sum over the (up to two) elements touching the
 // node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
-__device__ __forceinline__ double src_factor(int i, int n, double o, double h, double v, double rsq) {
+// The offset xq - v is formed in double (coordinates are absolute); the
+// exponential is evaluated in the kernel's precision.
+template <typename real>
+__device__ __forceinline__ real src_factor(int i, int n, double o, double h, double v, double inv_r2) {
   const double xi[2] = {-0.57735026918962576451, 0.57735026918962576451};
-  double s = 0.0;
+  real s = 0;
   for (int e = i - 1; e <= i; ++e) {
     if (e < 0 || e >= n - 1) continue;
+#pragma unroll
     for (int q = 0; q < 2; ++q) {
       const double xq = o + e * h + 0.5 * (1.0 + xi[q]) * h;
       const double d = xq - v;
-      const double g = exp(-3.0 * d * d / rsq);
-      const double phi = (i == e) ? 0.5 * (1.0 - xi[q]) : 0.5 * (1.0 + xi[q]);
+      const real g = exp((real)(-3.0 * d * d * inv_r2));
+      const real phi = (real)((i == e) ? 0.5 * (1.0 - xi[q]) : 0.5 * (1.0 + xi[q]));
       s += phi * g;
     }
   }
   return s;
 }
 
+// Pipeline per CTA (one barrier per node plane):
+//   smem ring of 3 node planes (T, k, rho*c, new phase); at the start of
+//   iteration ke it holds planes ke and ke+1, registers hold plane ke+2
+//   (loaded during the previous iteration).  Iteration ke reads the upper
+//   corners (plane ke+1), writes plane ke+2 into the free slot, issues the
+//   loads of plane ke+3, computes element plane ke, exchanges corner sums
+//   (shuffle in x, shared memory in y), passes the barrier and finalizes node
+//   plane ke.  Lower-plane corner values are carried in registers.
 template <typename real, int BY>
-__global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> a) {
-  constexpr int TX = 32, PX = TX + 1, PY = BY + 1;
+__global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<real> a) {
+  constexpr int TX = 32, PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
+  constexpr int NSLOT = (NP + NT - 1) / NT;
   __shared__ real sT[3][PY][PX];
   __shared__ real sK[3][PY][PX];
   __shared__ real sC[3][PY][PX];
@@ -126,50 +139,75 @@ __global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> 
   const real dt = (real)(*a.dt);
   const Props<real>& P = a.p;
 
-  // ---- laser source factors (separable rank-1 nodal source) ----
+  // ---- plane staging ----
+  real pfT[NSLOT];
+  uint8_t pfP[NSLOT];
+  auto fetch = [&](int pl) {
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) {
+      const int i = tid + s * NT;
+      pfT[s] = 0;
+      pfP[s] = 0;
+      if (i < NP) {
+        const int gx = X0 - 1 + i % PX, gy = Y0 - 1 + i / PX;
+        if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+          const long long id = gx + gy * (long long)nx + pl * nxy;
+          pfT[s] = a.T_in[id];
+          if (a.ph_in) pfP[s] = a.ph_in[id];
+        }
+      }
+    }
+  };
+  auto store = [&](int pl) {
+    const int slot = (pl + 3) % 3;
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) {
+      const int i = tid + s * NT;
+      if (i < NP) {
+        const int px = i % PX, py = i / PX;
+        const int gx = X0 - 1 + px, gy = Y0 - 1 + py;
+        real k = 0, c = 0;
+        uint8_t ph = 0;
+        if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+          const long long id = gx + gy * (long long)nx + pl * nxy;
+          ph = node_props(P, pfT[s], pfP[s], id < a.substrate, k, c);
+          if (a.k_arr) {
+            k = a.k_arr[id];
+            c = a.rc_arr[id];
+          }
+        }
+        sT[slot][py][px] = pfT[s];
+        sK[slot][py][px] = k;
+        sC[slot][py][px] = c;
+        sP[slot][py][px] = ph;
+      }
+    }
+  };
+
+  // ---- prologue: planes Z0-1, Z0 in shared memory, plane Z0+1 in registers ----
+  fetch(Z0 - 1);
+  store(Z0 - 1);
+  fetch(Z0);
+  store(Z0);
+  fetch(Z0 + 1);
   real srcP = 0;
   if (a.laser != nullptr) {
     const double vx = a.laser[0], vy = a.laser[1], vz = a.laser[2];
     srcP = (real)(a.src_c * a.laser[6]);
-    for (int i = tid; i < PX + PY + (Z1 - Z0); i += TX * BY) {
+    for (int i = tid; i < PX + PY + (Z1 - Z0); i += NT) {
       if (i < PX) {
         const int g = X0 - 1 + i;
-        sSx[i] = (g >= 0 && g < nx) ? (real)src_factor(g, nx, a.ox, a.hx, vx, a.rsq) : (real)0;
+        sSx[i] = (g >= 0 && g < nx) ? src_factor<real>(g, nx, a.ox, a.hx, vx, a.inv_r2) : (real)0;
       } else if (i < PX + PY) {
         const int g = Y0 - 1 + (i - PX);
-        sSy[i - PX] = (g >= 0 && g < ny) ? (real)src_factor(g, ny, a.oy, a.hy, vy, a.rsq) : (real)0;
+        sSy[i - PX] = (g >= 0 && g < ny) ? src_factor<real>(g, ny, a.oy, a.hy, vy, a.inv_r2) : (real)0;
       } else {
         const int g = Z0 + (i - PX - PY);
-        sSz[i - PX - PY] = (real)src_factor(g, nz, a.oz, a.hz, vz, a.dsq);
+        sSz[i - PX - PY] = src_factor<real>(g, nz, a.oz, a.hz, vz, a.inv_d2);
       }
     }
   }
-
-  auto load_plane = [&](int pl) {
-    const int slot = (pl + 3) % 3;
-    for (int i = tid; i < PX * PY; i += TX * BY) {
-      const int px = i % PX, py = i / PX;
-      const int gx = X0 - 1 + px, gy = Y0 - 1 + py;
-      real T = 0, k = 0, c = 0;
-      uint8_t ph = 0;
-      if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
-        const long long id = gx + gy * (long long)nx + pl * nxy;
-        T = a.T_in[id];
-        const uint8_t po = a.ph_in ? a.ph_in[id] : (uint8_t)0;
-        ph = node_props(P, T, po, id < a.substrate, k, c);
-        if (a.k_arr) {
-          k = a.k_arr[id];
-          c = a.rc_arr[id];
-        }
-      }
-      sT[slot][py][px] = T;
-      sK[slot][py][px] = k;
-      sC[slot][py][px] = c;
-      sP[slot][py][px] = ph;
-    }
-  };
-
-  load_plane(Z0 - 1);
+  __syncthreads();
 
   const int ex = X0 - 1 + tx, ey = Y0 - 1 + ty;
   const bool col_ok = ex >= 0 && ex < nx - 1 && ey >= 0 && ey < ny - 1;
@@ -178,37 +216,48 @@ __global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> 
   const int top_el = a.ne_planes - 1;
   const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
 
+  // carried lower-plane corners (plane Z0-1)
+  real tl[4], ksl = 0, csl = 0;
+  uint8_t phl;
+  {
+    const int sl = (Z0 - 1 + 3) % 3;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int ax = c & 1, ay = c >> 1;
+      tl[c] = sT[sl][ty + ay][tx + ax];
+      ksl += sK[sl][ty + ay][tx + ax];
+      csl += sC[sl][ty + ay][tx + ax];
+    }
+    phl = sP[sl][ty + 1][tx + 1];
+  }
+
   real carryU = 0, carryM = 0;
   for (int ke = Z0 - 1; ke < Z1; ++ke) {
-    load_plane(ke + 1);
-    __syncthreads();
-    const int sl = (ke + 3) % 3, su = (ke + 4) % 3;
+    const int su = (ke + 1) % 3;
+    real tu[4], ksu = 0, csu = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int ax = c & 1, ay = c >> 1;
+      tu[c] = sT[su][ty + ay][tx + ax];
+      ksu += sK[su][ty + ay][tx + ax];
+      csu += sC[su][ty + ay][tx + ax];
+    }
+    const uint8_t phu = sP[su][ty + 1][tx + 1];
+    store(ke + 2);
+    fetch(ke + 3);
 
     // ---- element (ex, ey, ke) ----
     real R[8];
     real me = 0;
     const bool el_ok = col_ok && ke >= 0 && ke < a.ne_planes;
     if (el_ok) {
-      real ks = 0, cs = 0;
 #pragma unroll
-      for (int az = 0; az < 2; ++az) {
-        const int s = az ? su : sl;
-#pragma unroll
-        for (int ay = 0; ay < 2; ++ay)
-#pragma unroll
-          for (int ax = 0; ax < 2; ++ax) {
-            R[ax + 2 * ay + 4 * az] = sT[s][ty + ay][tx + ax];
-            ks += sK[s][ty + ay][tx + ax];
-            cs += sC[s][ty + ay][tx + ax];
-          }
+      for (int c = 0; c < 4; ++c) {
+        R[c] = tl[c];
+        R[4 + c] = tu[c];
       }
-      const real kbar = ks * (real)0.125;
-      me = a.wvol * (cs * (real)0.125 / dt);
-      real Tt[4];
-      if (a.surface && ke == top_el) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) Tt[i] = R[4 + i];
-      }
+      const real kbar = (ksl + ksu) * (real)0.125;
+      me = a.wvol * ((csl + csu) * (real)0.125 / dt);
       bfly_fwd(R);
 #pragma unroll
       for (int m = 0; m < 8; ++m) R[m] *= a.lam[m];
@@ -216,14 +265,14 @@ __global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> 
 #pragma unroll
       for (int m = 0; m < 8; ++m) R[m] = -kbar * R[m];
       if (a.surface && ke == top_el) {
-        // top face: 2x2 Gauss points on the face of corners R[4..7]
+        // top face: 2x2 Gauss points on the face of the upper corners
 #pragma unroll
         for (int qy = 0; qy < 2; ++qy)
 #pragma unroll
           for (int qx = 0; qx < 2; ++qx) {
             const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
             const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
-            const real Tq = px0 * py0 * Tt[0] + px1 * py0 * Tt[1] + px0 * py1 * Tt[2] + px1 * py1 * Tt[3];
+            const real Tq = px0 * py0 * tu[0] + px1 * py0 * tu[1] + px0 * py1 * tu[2] + px1 * py1 * tu[3];
             const real q = surface_flux(P, Tq) * a.w2;
             R[4] += px0 * py0 * q;
             R[5] += px1 * py0 * q;
@@ -261,8 +310,8 @@ __global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> 
       const long long id = ix + iy * (long long)nx + ke * nxy;
       real Rt = carryU + lowN;
       const real M = carryM + mN;
-      const real Told = sT[sl][ty + 1][tx + 1];
-      const uint8_t phn = sP[sl][ty + 1][tx + 1];
+      const real Told = tl[3];
+      const uint8_t phn = phl;
       if (a.laser != nullptr) Rt += srcP * sSx[tx + 1] * sSy[ty + 1] * sSz[ke - Z0];
       if (a.rhs_box != nullptr && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3] &&
           ke >= a.box[4] && ke < a.box[5]) {
@@ -308,6 +357,11 @@ __global__ void __launch_bounds__(32 * BY) level_step_kernel(const LevelK<real> 
     }
     carryU = upN;
     carryM = mN;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tl[c] = tu[c];
+    ksl = ksu;
+    csl = csu;
+    phl = phu;
   }
 }
 
@@ -360,8 +414,8 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   a.wvol = (real)(hx * hy * hz / 8.0);
   a.w2 = (real)(hx * hy / 4.0);
   const double r = pr->laser_radius, d = pr->laser_depth;
-  a.rsq = r * r;
-  a.dsq = d * d;
+  a.inv_r2 = 1.0 / (r * r);
+  a.inv_d2 = 1.0 / (d * d);
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
 
@@ -369,7 +423,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, BY - 1);
   int zc = g->zchunk;
   if (zc <= 0) {
-    const int want = 2 * 152;
+    const int want = 3 * 152;
     int chunks = cdiv(want, gx * gy);
     chunks = chunks < 1 ? 1 : (chunks > a.nz ? a.nz : chunks);
     zc = cdiv(a.nz, chunks);
@@ -425,8 +479,8 @@ __global__ void fine_source_kernel(int nx, int ny, int nz, double ox, double oy,
   const double c = src_c * laser[6];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int ix = (int)(i % nx), iy = (int)((i / nx) % ny), iz = (int)(i / ((long long)nx * ny));
-    F[i] += (real)(c * src_factor(ix, nx, ox, hx, vx, rsq) * src_factor(iy, ny, oy, hy, vy, rsq) *
-                   src_factor(iz, nz, oz, hz, vz, dsq));
+    F[i] += (real)(c * src_factor<double>(ix, nx, ox, hx, vx, 1.0 / rsq) *
+                   src_factor<double>(iy, ny, oy, hy, vy, 1.0 / rsq) * src_factor<double>(iz, nz, oz, hz, vz, 1.0 / dsq));
   }
 }
 

@@ -110,6 +110,12 @@ __global__ void restrict_s1_kernel(int n0, int n1, int n2, const Map3<real> m, c
     const bool s1 = (v > (real)0.499) || id < substrate;
     coarse_ph[id] = (uint8_t)((coarse_ph[id] & ~PH_S1) | (s1 ? PH_S1 : 0));
   }
+  // S1[:substrate] = 1 on the whole level.  Overlap nodes below `substrate`
+  // get the same byte from both loops (S1 set, S2 kept), so the order of the
+  // two writes does not matter.
+  for (long long id = blockIdx.x * (long long)blockDim.x + threadIdx.x; id < substrate;
+       id += (long long)gridDim.x * blockDim.x)
+    coarse_ph[id] |= PH_S1;
 }
 
 // Level-0 gather (moveEverything :2500-2502): window phase from the Level-0
@@ -250,13 +256,14 @@ extern "C" int gm_restrict_s1(const gm_restrict_s1_args* g, void* stream) {
     return GM_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
-  if (tot == 0) return GM_OK;
+  if (tot == 0 && g->substrate <= 0) return GM_OK;
+  const long long work = tot > g->substrate ? tot : g->substrate;
   if (g->dtype == GM_F32)
-    restrict_s1_kernel<float><<<grid_for(tot), 256, 0, st>>>(
+    restrict_s1_kernel<float><<<grid_for(work), 256, 0, st>>>(
         g->n[0], g->n[1], g->n[2], make_map3<float>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
         g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
   else if (g->dtype == GM_F64)
-    restrict_s1_kernel<double><<<grid_for(tot), 256, 0, st>>>(
+    restrict_s1_kernel<double><<<grid_for(work), 256, 0, st>>>(
         g->n[0], g->n[1], g->n[2], make_map3<double>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
         g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
   else

@@ -341,11 +341,16 @@ class Engine:
     # subcycleGOMELT (:3224-3632)
     # ------------------------------------------------------------------
     def subcycle(self, laser_rows, history=False, rows_device=None):
+        """One subcycleGOMELT call, issued natively (gm_subcycle).  laser_rows:
+        N2*N3 host rows (x, y, z, jump, dwell, dt, P); rows_device: the same
+        rows already on the device.  Returns (L2all, L3all, L3pall) device
+        tensors when ``history``, else None."""
         g = self.geo
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         N2, N3 = self.N2, self.N3
         rows_h = np.ascontiguousarray(np.asarray(laser_rows, dtype=np.float64))
-        assert rows_h.shape == (N2 * N3, 7), rows_h.shape
+        if rows_h.shape != (N2 * N3, 7):
+            raise N.GomeltError(f"expected {N2 * N3} laser rows of 7 values, got {rows_h.shape}")
         if self.tmp is None:
             raise N.GomeltError("active Level-1 region not set (call set_layer first)")
         dts = np.concatenate([[rows_h[:, 5].sum()], rows_h[:, 5].reshape(N2, N3).sum(axis=1)])
@@ -356,94 +361,81 @@ class Engine:
             rows.copy_(torch.from_numpy(rows_h), non_blocking=False)
         dtd = self._buf("dts", N2 + 1, torch.float64)
         dtd.copy_(torch.from_numpy(dts))
-        tb = self.tables
-        c32, c31, c21 = tb["c32"], tb["c31"], tb["c21"]
-        T1s, T2s, T3s = self.T[1], self.T[2], self.T[3]
-        Tp2s, Tp3s = self.Tp[2], self.Tp[3]
-        ph1, ph2s, ph3s = self.ph[1], self.ph[2], self.ph[3]
-        nn1, nn2, nn3 = L1.nn, L2.nn, L3.nn
-
-        # Level-1 S1 from Level 2 at the overlap (:3272-3278)
-        self._s1_restrict()
-        # Level-1 right-hand side: source over all positions + subgrid fluxes of L3 and L2
-        rhs1 = self._buf("rhs1", int(np.prod(c21.box_n)))
-        rhs1.zero_()
-        self._coarse_source(c31, rows, N2 * N3, rhs1, c21.box_lo, c21.box_n)
-        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, Tp=Tp3s)
-        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, Tp=Tp2s)
-        box1 = [c21.box_lo[0], c21.box_lo[0] + c21.box_n[0], c21.box_lo[1], c21.box_lo[1] + c21.box_n[1],
-                c21.box_lo[2], c21.box_lo[2] + c21.box_n[2]]
-        T1p = self._buf("T1p", nn1)
-        self._level(1, T1s, T1p, dtd[0:1], ph1, None, rhs=rhs1, box=box1)
-
-        rhs2 = self._buf("rhs2", int(np.prod(c32.box_n)))
-        box2 = [c32.box_lo[0], c32.box_lo[0] + c32.box_n[0], c32.box_lo[1], c32.box_lo[1] + c32.box_n[1],
-                c32.box_lo[2], c32.box_lo[2] + c32.box_n[2]]
-        hist = self._buf("tp3hist", N2 * nn3).view(N2, nn3)
-        T3w = [self._buf("T3a", nn3), self._buf("T3b", nn3)]
-        ph3w = [self._buf("ph3a", nn3, torch.uint8), self._buf("ph3b", nn3, torch.uint8)]
-        T2w = [self._buf("T2a", nn2), self._buf("T2b", nn2), self._buf("T2c", nn2)]
-        ph2w = [self._buf("ph2a", nn2, torch.uint8), self._buf("ph2b", nn2, torch.uint8)]
         out_hist = None
         if history:
-            out_hist = (torch.empty(N2, nn2, dtype=self.dtype, device=self.dev),
-                        torch.empty(N2, nn3, dtype=self.dtype, device=self.dev),
-                        torch.empty(N2, nn3, dtype=self.dtype, device=self.dev))
-
-        def l2_pass(T1_new, part2):
-            T2c, ph2c = T2s, ph2s
-            T3c, ph3c, Tp3c = T3s, ph3s, Tp3s
-            k2 = 0
-            for l2 in range(N2):
-                rhs2.zero_()
-                if part2:
-                    self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3c, ph=ph3c, Tp=Tp3c, dTa=hist[l2],
-                                 dTb=Tp3c, dt=dtd[1 + l2:2 + l2])
-                else:
-                    self._couple(c32, 3, rhs2, c32.box_lo, c32.box_n, T=T3c, ph=ph3c, Tp=Tp3c)
-                self._coarse_source(c32, rows[l2 * N3:(l2 + 1) * N3], N3, rhs2, c32.box_lo, c32.box_n)
-                alpha2 = (l2 + 1) / float(N2)
-                T2n = T2w[k2 % 3] if T2w[k2 % 3].data_ptr() != T2c.data_ptr() else T2w[(k2 + 1) % 3]
-                ph2n = ph2w[l2 % 2]
-                self._level(2, T2c, T2n, dtd[1 + l2:2 + l2], ph2c, ph2n, rhs=rhs2, box=box2, bc_new=T1_new,
-                            bc_old=T1s, alpha=alpha2)
-                k2 += 1
-                for l3 in range(N3):
-                    i = l2 * N3 + l3
-                    Tn = T3w[i % 2]
-                    phn = ph3w[i % 2]
-                    self._level(3, T3c, Tn, rows[i, 5:6], ph3c, phn, laser=rows[i], bc_new=T2n, bc_old=T2c,
-                                alpha=(l3 + 1) / float(N3), accum=part2)
-                    T3c, ph3c = Tn, phn
-                Tp3n = hist[l2] if not part2 else self._buf("tp3w%d" % (l2 % 2), nn3)
-                self._new_tprime(3, T3c, T2n, Tp3n)
-                if part2 and history:
-                    out_hist[0][l2].copy_(T2n)
-                    out_hist[1][l2].copy_(T3c)
-                    out_hist[2][l2].copy_(Tp3n)
-                Tp3c = Tp3n
-                T2c, ph2c = T2n, ph2n
-            return T2c, ph2c, T3c, ph3c, Tp3c
-
-        # Part 1 (predictor)
-        T2f, _, _, _, Tp3f = l2_pass(T1p, False)
-        Tp2w = self._buf("Tp2w", nn2)
-        self._new_tprime(2, T2f, T1p, Tp2w)
-        self._couple(c31, 3, rhs1, c21.box_lo, c21.box_n, T=T3s, ph=ph3s, dTa=Tp3f, dTb=Tp3s, dt=dtd[0:1])
-        self._couple(c21, 2, rhs1, c21.box_lo, c21.box_n, T=T2s, ph=ph2s, dTa=Tp2w, dTb=Tp2s, dt=dtd[0:1])
-        T1c = self._buf("T1c", nn1)
-        self._level(1, T1s, T1c, dtd[0:1], ph1, None, rhs=rhs1, box=box1)
-        # Part 2 (corrector)
-        T2f, ph2f, T3f, ph3f, Tp3f = l2_pass(T1c, True)
-        T3s.copy_(T3f)
-        ph3s.copy_(ph3f)
-        Tp3s.copy_(Tp3f)
-        T2s.copy_(T2f)
-        ph2s.copy_(ph2f)
-        self._new_tprime(2, T2s, T1c, Tp2s)
-        T1s.copy_(T1c)
-        self.l0_scatter()
+            out_hist = (torch.empty(N2, L2.nn, dtype=self.dtype, device=self.dev),
+                        torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev),
+                        torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev))
+        p = self._plan(rows, dtd, out_hist)
+        N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
+               kernels=N.subcycle_kernel_count(N2, N3))
+        self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         return out_hist
+
+    def _window(self, lev):
+        L = self.geo.L[lev]
+        w = N.gm_window()
+        for d in range(3):
+            w.nodes[d] = L.nodes[d]
+            w.h[d] = L.spacing()[d]
+            w.origin[d] = L.origin()[d]
+        w.substrate = self.substrate[lev]
+        w.T = self.T[lev].data_ptr()
+        w.Tp = self.Tp[lev].data_ptr() if lev > 1 else None
+        w.ph = C.cast(self.ph[lev].data_ptr(), C.POINTER(C.c_uint8))
+        return w
+
+    def _plan(self, rows, dtd, out_hist):
+        g = self.geo
+        L1, L2, L3 = g.L[1], g.L[2], g.L[3]
+        N2, N3 = self.N2, self.N3
+        tb = self.tables
+        c32, c31, c21 = tb["c32"], tb["c31"], tb["c21"]
+        nn1, nn2, nn3 = L1.nn, L2.nn, L3.nn
+        u8 = torch.uint8
+        pi = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_int))  # noqa: E731
+        pu = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_uint8))  # noqa: E731
+        p = N.gm_subcycle_plan()
+        p.dtype = kern.dtype_code(self.T[3])
+        p.N2, p.N3 = N2, N3
+        p.L1, p.L2, p.L3 = self._window(1), self._window(2), self._window(3)
+        p.L1_ne_planes = self.tmp[0] // (L1.elements[0] * L1.elements[1])
+        c = g.conditions
+        for i, v in enumerate((c["x"][0], c["x"][1], c["y"][0], c["y"][1], c["z"][0])):
+            p.face[i] = float(v)
+        p.acc3, p.macc3 = self.acc3.data_ptr(), self.macc3.data_ptr()
+        p.bc12, p.bc23, p.r32, p.r21 = tb["bc12"].struct, tb["bc23"].struct, tb["r32"].struct, tb["r21"].struct
+        for d in range(3):
+            p.r32_idx[d] = pi(tb["r32_idx"][d])
+            p.r21_idx[d] = pi(tb["r21_idx"][d])
+            p.xq32[d] = C.cast(c32.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
+            p.xq31[d] = C.cast(c31.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
+            p.rhs1_lo[d], p.rhs1_n[d] = c21.box_lo[d], c21.box_n[d]
+            p.rhs2_lo[d], p.rhs2_n[d] = c32.box_lo[d], c32.box_n[d]
+            p.l0_idx3[d] = pi(tb["l0_3"][d])
+        p.c32, p.c31, p.c21 = c32.struct, c31.struct, c21.struct
+        p.L0 = pu(self.L0)
+        p.L0_nx, p.L0_ny = g.L0_nodes[0], g.L0_nodes[1]
+        p.rows, p.dts = rows.data_ptr(), dtd.data_ptr()
+        p.T1p, p.T1c = self._buf("T1p", nn1).data_ptr(), self._buf("T1c", nn1).data_ptr()
+        p.T2w[0], p.T2w[1] = self._buf("T2a", nn2).data_ptr(), self._buf("T2b", nn2).data_ptr()
+        p.T3w[0], p.T3w[1] = self._buf("T3a", nn3).data_ptr(), self._buf("T3b", nn3).data_ptr()
+        p.tp3w[0], p.tp3w[1] = self._buf("tp3w0", nn3).data_ptr(), self._buf("tp3w1", nn3).data_ptr()
+        p.Tp2w = self._buf("Tp2w", nn2).data_ptr()
+        p.rhs1 = self._buf("rhs1", int(np.prod(c21.box_n))).data_ptr()
+        p.rhs2 = self._buf("rhs2", int(np.prod(c32.box_n))).data_ptr()
+        p.tp3hist = self._buf("tp3hist", N2 * nn3).data_ptr()
+        p.ph2w[0], p.ph2w[1] = pu(self._buf("ph2a", nn2, u8)), pu(self._buf("ph2b", nn2, u8))
+        p.ph3w[0], p.ph3w[1] = pu(self._buf("ph3a", nn3, u8)), pu(self._buf("ph3b", nn3, u8))
+        part = self._work["partials"]
+        p.partials, p.partials_cap = part.data_ptr(), part.numel()
+        ns = max(N2 * N3 * sum(c31.box_n), N3 * sum(c32.box_n))
+        scr = self._buf("srcscratch", ns)
+        p.src_scratch, p.src_cap = scr.data_ptr(), scr.numel()
+        if out_hist is not None:
+            p.L2all, p.L3all, p.L3pall = (t.data_ptr() for t in out_hist)
+        p.zchunk = int(getattr(self, "zchunk", 0))
+        return p
 
     # ------------------------------------------------------------------
     # stepGOMELT (:2304-2397) and stepGOMELTDwellTime (:2617-2664)

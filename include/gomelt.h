@@ -293,6 +293,68 @@ typedef struct gm_coarse_source_args {
 
 int gm_coarse_source(const gm_coarse_source_args* a, const gm_props* p, void* stream);
 
+/* One level as the subcycle sees it: grid, state buffers and substrate count
+ * (nodes with id < substrate are always S1, getSubstrateNodes :562-579). */
+typedef struct gm_window {
+  int nodes[3];
+  double h[3];      /* node spacing */
+  double origin[3]; /* node 0 coordinates */
+  long long substrate;
+  void* T;          /* temperature (state, dtype) */
+  void* Tp;         /* subgrid field T' (Levels 2, 3) */
+  uint8_t* ph;      /* phase bytes */
+} gm_window;
+
+/* Everything one subcycleGOMELT call (:3224-3632) needs: the three levels,
+ * the per-window maps and coupling geometry of the current window positions,
+ * the N2*N3 laser rows of the call, caller-provided work buffers (sizes in
+ * elements of dtype unless noted) and optional per-Level-2-step histories. */
+typedef struct gm_subcycle_plan {
+  int dtype;
+  int N2, N3;
+  gm_window L1, L2, L3;
+  int L1_ne_planes;          /* active Level-1 element planes (calcStaticTmpNodesAndElements) */
+  double face[5];            /* Level-1 Dirichlet values: x0, x1, y0, y1, z0 */
+  void* acc3;                /* melt time on the Level-3 window (accum_L3) */
+  void* macc3;               /* its running maximum (max_accum_L3) */
+  gm_map3 bc12, bc23;        /* Level 1 -> Level-2 nodes, Level 2 -> Level-3 nodes */
+  gm_map3 r32, r21;          /* Level 3 at the Level-2 overlap nodes, Level 2 at the Level-1 overlap nodes */
+  const int* r32_idx[3];     /* Level-2 node index of each Level-3 overlap point, per axis */
+  const int* r21_idx[3];     /* Level-1 node index of each Level-2 overlap point, per axis */
+  gm_couple_geom c32, c31, c21;
+  const double* xq32[3];     /* Level-3 Gauss-point coordinates per axis (nfe*2) */
+  const double* xq31[3];
+  int rhs1_lo[3], rhs1_n[3]; /* Level-1 node box of the coupling terms (c21) */
+  int rhs2_lo[3], rhs2_n[3]; /* Level-2 node box of the coupling terms (c32) */
+  uint8_t* L0;               /* Level-0 S1 store */
+  long long L0_nx, L0_ny;
+  const int* l0_idx3[3];     /* Level-0 node index of the Level-3 window, per axis */
+  const double* rows;        /* device: N2*N3 rows (x, y, z, jump, dwell, dt, P) */
+  const double* dts;         /* device: N2+1 values: sum of all dt, then per Level-2 step */
+  void* T1p;                 /* work: Level-1 predictor, corrector (nn1 each) */
+  void* T1c;
+  void* T2w[2];              /* work: nn2 each */
+  void* T3w[2];              /* work: nn3 each */
+  void* tp3w[2];             /* work: nn3 each */
+  void* Tp2w;                /* work: nn2 */
+  void* rhs1;                /* work: prod(rhs1_n) */
+  void* rhs2;                /* work: prod(rhs2_n) */
+  void* tp3hist;             /* work: N2*nn3 */
+  uint8_t* ph2w[2];          /* work: nn2 bytes each */
+  uint8_t* ph3w[2];          /* work: nn3 bytes each */
+  void* partials;            /* scratch of gm_couple */
+  long long partials_cap;
+  void* src_scratch;         /* scratch of gm_coarse_source */
+  long long src_cap;
+  void* L2all;               /* optional (N2*nn2): Level-2 T after each corrector Level-2 step */
+  void* L3all;               /* optional (N2*nn3): Level-3 T */
+  void* L3pall;              /* optional (N2*nn3): Level-3 T' */
+  int zchunk;                /* level-kernel tuning (0: automatic) */
+} gm_subcycle_plan;
+
+/* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
+int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream);
+
 /* Library identification: returns a static string; never fails. */
 const char* gm_version(void);
 
