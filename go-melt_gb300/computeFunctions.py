@@ -36,7 +36,7 @@ import _native as N
 import kern
 from _native import GomeltError  # noqa: F401
 from createPath import count_lines, parsingGcode  # noqa: F401
-from engine import PH_S1, PH_S2, CoupleGeom, Engine
+from engine import PH_S1, PH_S2, CoupleGeom, Engine, TableArena
 from geometry import axis_map
 from levels import setup_nonmesh, setup_properties
 
@@ -448,7 +448,11 @@ class Shape:
         g = engine.geo
         self.engine = engine
         self.coarse, self.fine = coarse_lev, fine_lev
-        self.geom = CoupleGeom(g.L[fine_lev].coords, g.L[coarse_lev].coords, engine.dtype, engine.dev)
+        fc, cc = g.L[fine_lev].coords, g.L[coarse_lev].coords
+        self.arena = TableArena(1 << 16 | 128 * sum(len(c) for c in fc), engine.dev)
+        self.arena.begin()
+        self.geom = CoupleGeom(fc, cc, engine.np_dtype, self.arena)
+        self.arena.upload(None)
 
 
 def computeCoarseFineShapeFunctions(Coarse, Fine):

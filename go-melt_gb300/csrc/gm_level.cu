@@ -112,6 +112,29 @@ __device__ __forceinline__ real src_factor(int i, int n, double o, double h, dou
   return s;
 }
 
+template <typename real>
+__device__ __forceinline__ real fast_div(real a, real b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fast_div<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+
+// Phase and properties with selects (same values as node_props).
+template <typename real>
+__device__ __forceinline__ uint8_t node_props_sel(const Props<real>& p, real T, uint8_t ph_old, bool substrate,
+                                                  real& k, real& rc) {
+  const bool s2 = T >= p.T_liquidus;
+  const bool s3 = (T > p.T_solidus) && (T < p.T_liquidus);
+  const bool s1 = (ph_old & PH_S1) || s2 || substrate;
+  const real kb = p.k_bulk_a1 * T + p.k_bulk_a0;
+  const real cs = p.cp_solid_a1 * T + p.cp_solid_a0;
+  k = s2 ? p.k_fluid : (s1 ? kb : p.k_powder);
+  rc = p.rho * (s2 ? p.cp_fluid : (s3 ? p.cp_mushy : cs));
+  return (uint8_t)((s1 ? PH_S1 : 0) | (s2 ? PH_S2 : 0));
+}
+
 // Pipeline per CTA (one barrier per node plane):
 //   smem ring of 3 node planes (T, k, rho*c, new phase); at the start of
 //   iteration ke it holds planes ke and ke+1, registers hold plane ke+2
@@ -119,76 +142,83 @@ __device__ __forceinline__ real src_factor(int i, int n, double o, double h, dou
 //   corners (plane ke+1), writes plane ke+2 into the free slot, issues the
 //   loads of plane ke+3, computes element plane ke, exchanges corner sums
 //   (shuffle in x, shared memory in y), passes the barrier and finalizes node
-//   plane ke.  Lower-plane corner values are carried in registers.
+//   plane ke.  Lower-plane corner values are carried in registers; all
+//   per-thread indexing is computed once, outside the plane loop.
 template <typename real, int BY>
 __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<real> a) {
   constexpr int TX = 32, PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
   constexpr int NSLOT = (NP + NT - 1) / NT;
-  __shared__ real sT[3][PY][PX];
-  __shared__ real sK[3][PY][PX];
-  __shared__ real sC[3][PY][PX];
-  __shared__ uint8_t sP[3][PY][PX];
+  __shared__ real sT[3][PY * PX];
+  __shared__ real sK[3][PY * PX];
+  __shared__ real sC[3][PY * PX];
+  __shared__ uint8_t sP[3][PY * PX];
   __shared__ real sX[2][3][BY][TX];
   __shared__ real sSx[PX], sSy[PY], sSz[ZMAX];
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
-  const long long nxy = (long long)nx * ny;
+  const int nxy = nx * ny;
   const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
   const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
   const real dt = (real)(*a.dt);
   const Props<real>& P = a.p;
 
-  // ---- plane staging ----
+  // ---- per-thread staging slots (constant over the plane loop) ----
+  int sbase[NSLOT];  // node id of the slot in plane 0, or -1 outside the grid / tile
   real pfT[NSLOT];
   uint8_t pfP[NSLOT];
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const int i = tid + s * NT;
+    sbase[s] = -1;
+    if (i < NP) {
+      const int gx = X0 - 1 + i % PX, gy = Y0 - 1 + i / PX;
+      if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) sbase[s] = gx + gy * nx;
+    }
+  }
   auto fetch = [&](int pl) {
+    const bool pin = pl >= 0 && pl < nz;
 #pragma unroll
     for (int s = 0; s < NSLOT; ++s) {
-      const int i = tid + s * NT;
       pfT[s] = 0;
       pfP[s] = 0;
-      if (i < NP) {
-        const int gx = X0 - 1 + i % PX, gy = Y0 - 1 + i / PX;
-        if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
-          const long long id = gx + gy * (long long)nx + pl * nxy;
-          pfT[s] = a.T_in[id];
-          if (a.ph_in) pfP[s] = a.ph_in[id];
-        }
+      if (pin && sbase[s] >= 0) {
+        const int id = sbase[s] + pl * nxy;
+        pfT[s] = a.T_in[id];
+        if (a.ph_in) pfP[s] = a.ph_in[id];
       }
     }
   };
-  auto store = [&](int pl) {
-    const int slot = (pl + 3) % 3;
+  auto store = [&](int pl, int slot) {
+    const bool pin = pl >= 0 && pl < nz;
 #pragma unroll
     for (int s = 0; s < NSLOT; ++s) {
       const int i = tid + s * NT;
       if (i < NP) {
-        const int px = i % PX, py = i / PX;
-        const int gx = X0 - 1 + px, gy = Y0 - 1 + py;
         real k = 0, c = 0;
         uint8_t ph = 0;
-        if (pl >= 0 && pl < nz && gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
-          const long long id = gx + gy * (long long)nx + pl * nxy;
-          ph = node_props(P, pfT[s], pfP[s], id < a.substrate, k, c);
+        if (pin && sbase[s] >= 0) {
+          const int id = sbase[s] + pl * nxy;
+          ph = node_props_sel(P, pfT[s], pfP[s], (long long)id < a.substrate, k, c);
           if (a.k_arr) {
             k = a.k_arr[id];
             c = a.rc_arr[id];
           }
         }
-        sT[slot][py][px] = pfT[s];
-        sK[slot][py][px] = k;
-        sC[slot][py][px] = c;
-        sP[slot][py][px] = ph;
+        sT[slot][i] = pfT[s];
+        sK[slot][i] = k;
+        sC[slot][i] = c;
+        sP[slot][i] = ph;
       }
     }
   };
 
   // ---- prologue: planes Z0-1, Z0 in shared memory, plane Z0+1 in registers ----
+  int s_lo = 0, s_up = 1, s_nx = 2;  // ring slots of planes ke, ke+1, ke+2
   fetch(Z0 - 1);
-  store(Z0 - 1);
+  store(Z0 - 1, s_lo);
   fetch(Z0);
-  store(Z0);
+  store(Z0, s_up);
   fetch(Z0 + 1);
   real srcP = 0;
   if (a.laser != nullptr) {
@@ -215,35 +245,38 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
   const bool out_col = tx < TX - 1 && ty < BY - 1 && ix < nx && iy < ny;
   const int top_el = a.ne_planes - 1;
   const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
+  const int c00 = ty * PX + tx;  // smem offset of this element's (0,0) corner
+  const int nid0 = ix + iy * nx;  // node id of this thread's output column in plane 0
+  const bool ring_xy = ix == 0 || ix == nx - 1 || iy == 0 || iy == ny - 1;
+  const bool box_xy = a.rhs_box != nullptr && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3];
+  const int box_off = box_xy ? (ix - a.box[0]) + (iy - a.box[2]) * (a.box[1] - a.box[0]) : 0;
+  const int box_pl = (a.box[1] - a.box[0]) * (a.box[3] - a.box[2]);
+  const real srcxy = (a.laser != nullptr && out_col) ? srcP * sSx[tx + 1] * sSy[ty + 1] : (real)0;
 
   // carried lower-plane corners (plane Z0-1)
   real tl[4], ksl = 0, csl = 0;
   uint8_t phl;
-  {
-    const int sl = (Z0 - 1 + 3) % 3;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int ax = c & 1, ay = c >> 1;
-      tl[c] = sT[sl][ty + ay][tx + ax];
-      ksl += sK[sl][ty + ay][tx + ax];
-      csl += sC[sl][ty + ay][tx + ax];
-    }
-    phl = sP[sl][ty + 1][tx + 1];
+  for (int c = 0; c < 4; ++c) {
+    const int o = c00 + (c >> 1) * PX + (c & 1);
+    tl[c] = sT[s_lo][o];
+    ksl += sK[s_lo][o];
+    csl += sC[s_lo][o];
   }
+  phl = sP[s_lo][c00 + PX + 1];
 
   real carryU = 0, carryM = 0;
   for (int ke = Z0 - 1; ke < Z1; ++ke) {
-    const int su = (ke + 1) % 3;
     real tu[4], ksu = 0, csu = 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const int ax = c & 1, ay = c >> 1;
-      tu[c] = sT[su][ty + ay][tx + ax];
-      ksu += sK[su][ty + ay][tx + ax];
-      csu += sC[su][ty + ay][tx + ax];
+      const int o = c00 + (c >> 1) * PX + (c & 1);
+      tu[c] = sT[s_up][o];
+      ksu += sK[s_up][o];
+      csu += sC[s_up][o];
     }
-    const uint8_t phu = sP[su][ty + 1][tx + 1];
-    store(ke + 2);
+    const uint8_t phu = sP[s_up][c00 + PX + 1];
+    store(ke + 2, s_nx);
     fetch(ke + 3);
 
     // ---- element (ex, ey, ke) ----
@@ -257,13 +290,11 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
         R[4 + c] = tu[c];
       }
       const real kbar = (ksl + ksu) * (real)0.125;
-      me = a.wvol * ((csl + csu) * (real)0.125 / dt);
+      me = a.wvol * ((csl + csu) * (real)0.125) / dt;
       bfly_fwd(R);
 #pragma unroll
-      for (int m = 0; m < 8; ++m) R[m] *= a.lam[m];
+      for (int m = 0; m < 8; ++m) R[m] *= a.lam[m] * kbar;
       bfly_inv(R);
-#pragma unroll
-      for (int m = 0; m < 8; ++m) R[m] = -kbar * R[m];
       if (a.surface && ke == top_el) {
         // top face: 2x2 Gauss points on the face of the upper corners
 #pragma unroll
@@ -274,10 +305,10 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
             const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
             const real Tq = px0 * py0 * tu[0] + px1 * py0 * tu[1] + px0 * py1 * tu[2] + px1 * py1 * tu[3];
             const real q = surface_flux(P, Tq) * a.w2;
-            R[4] += px0 * py0 * q;
-            R[5] += px1 * py0 * q;
-            R[6] += px0 * py1 * q;
-            R[7] += px1 * py1 * q;
+            R[4] -= px0 * py0 * q;
+            R[5] -= px1 * py0 * q;
+            R[6] -= px0 * py1 * q;
+            R[7] -= px1 * py1 * q;
           }
       }
     } else {
@@ -285,7 +316,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
       for (int m = 0; m < 8; ++m) R[m] = 0;
     }
 
-    // ---- corners -> nodes: x by shuffle, y through shared memory ----
+    // ---- corners -> nodes (R holds kbar*K*T minus sources): x by shuffle, y via smem ----
     real cx[4];  // index ay + 2*az
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -293,7 +324,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
       cx[j] = R[1 + 2 * ay + 4 * az] + __shfl_down_sync(0xffffffffu, R[2 * ay + 4 * az], 1);
     }
     const real mx = me + __shfl_down_sync(0xffffffffu, me, 1);
-    const int xb = (ke + 1) & 1;
+    const int xb = ke & 1;
     sX[xb][0][ty][tx] = cx[0];  // ay=0, lower
     sX[xb][1][ty][tx] = cx[2];  // ay=0, upper
     sX[xb][2][ty][tx] = mx;
@@ -307,20 +338,16 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
 
     // ---- finalize node plane ke ----
     if (ke >= Z0 && out_col) {
-      const long long id = ix + iy * (long long)nx + ke * nxy;
-      real Rt = carryU + lowN;
+      const int id = nid0 + ke * nxy;
+      real Rt = -(carryU + lowN);
       const real M = carryM + mN;
       const real Told = tl[3];
       const uint8_t phn = phl;
-      if (a.laser != nullptr) Rt += srcP * sSx[tx + 1] * sSy[ty + 1] * sSz[ke - Z0];
-      if (a.rhs_box != nullptr && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3] &&
-          ke >= a.box[4] && ke < a.box[5]) {
-        const int bnx = a.box[1] - a.box[0], bny = a.box[3] - a.box[2];
-        Rt += a.rhs_box[(ix - a.box[0]) + (long long)(iy - a.box[2]) * bnx + (long long)(ke - a.box[4]) * bnx * bny];
-      }
+      if (a.laser != nullptr) Rt += srcxy * sSz[ke - Z0];
+      if (box_xy && ke >= a.box[4] && ke < a.box[5]) Rt += a.rhs_box[box_off + (ke - a.box[4]) * box_pl];
       if (a.F_full) Rt += a.F_full[id];
       if (a.corr_full) Rt += a.corr_full[id];
-      real Tn = Told + Rt / M;
+      real Tn = Told + fast_div(Rt, M);
       if (a.inactive_amb && ke > a.ne_planes) Tn = P.T_amb;
       if (a.bc_mode == 1) {
         if (iy == 0) Tn = a.face[2];
@@ -328,20 +355,18 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
         if (ix == 0) Tn = a.face[0];
         if (ix == nx - 1) Tn = a.face[1];
         if (ke == 0) Tn = a.face[4];
-      } else if (a.bc_mode == 2) {
-        if (ix == 0 || ix == nx - 1 || iy == 0 || iy == ny - 1 || ke == 0) {
-          real w8[8];
-          const int b = map3_weights(a.bc_map, ix, iy, ke, w8);
-          const int sx = 1, sy = a.bc_map.src_nx, sz = a.bc_map.src_nx * a.bc_map.src_ny;
-          const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
-          real v = 0;
+      } else if (a.bc_mode == 2 && (ring_xy || ke == 0)) {
+        real w8[8];
+        const int b = map3_weights(a.bc_map, ix, iy, ke, w8);
+        const int sx = 1, sy = a.bc_map.src_nx, sz = a.bc_map.src_nx * a.bc_map.src_ny;
+        const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+        real v = 0;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const real bc = a.bc_alpha * a.bc_new[b + off[j]] + a.bc_beta * a.bc_old[b + off[j]];
-            v += w8[j] * bc;
-          }
-          Tn = v;
+        for (int j = 0; j < 8; ++j) {
+          const real bc = a.bc_alpha * a.bc_new[b + off[j]] + a.bc_beta * a.bc_old[b + off[j]];
+          v += w8[j] * bc;
         }
+        Tn = v;
       }
       if (a.clamp) Tn = fmax(Tn, P.T_amb);
       a.T_out[id] = Tn;
@@ -362,7 +387,38 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
     ksl = ksu;
     csl = csu;
     phl = phu;
+    const int t = s_lo;  // rotate the ring: ke+1 -> lower, ke+2 -> upper
+    s_lo = s_up;
+    s_up = s_nx;
+    s_nx = t;
   }
+}
+
+// Node planes per CTA when the caller does not choose: minimise
+// (waves of CTAs) x (planes per CTA + 1 halo plane) for the resident CTA
+// slots of this GPU.
+template <typename real, int BY>
+static int auto_zchunk(int tiles_xy, int nz) {
+  static int slots = 0;
+  if (slots == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, level_step_kernel<real, BY>, 32 * BY, 0);
+    slots = (sms > 0 ? sms : 152) * (per > 0 ? per : 1);
+  }
+  int best = nz < ZMAX ? nz : ZMAX;
+  long long best_cost = -1;
+  for (int zc = 2; zc <= ZMAX && zc <= nz; ++zc) {
+    const long long ctas = (long long)tiles_xy * cdiv(nz, zc);
+    const long long waves = (ctas + slots - 1) / slots;
+    const long long cost = waves * (zc + 1);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = zc;
+    }
+  }
+  return best;
 }
 
 template <typename real>
@@ -422,12 +478,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   constexpr int BY = 8;
   const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, BY - 1);
   int zc = g->zchunk;
-  if (zc <= 0) {
-    const int want = 3 * 152;
-    int chunks = cdiv(want, gx * gy);
-    chunks = chunks < 1 ? 1 : (chunks > a.nz ? a.nz : chunks);
-    zc = cdiv(a.nz, chunks);
-  }
+  if (zc <= 0) zc = auto_zchunk<real, BY>(gx * gy, a.nz);
   if (zc > ZMAX) zc = ZMAX;
   if (zc < 1) zc = 1;
   a.zchunk = zc;
@@ -441,6 +492,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
 extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream) {
   if (!a || !p || !a->T_in || !a->T_out || !a->dt || a->T_in == a->T_out) return GM_ERR_ARG;
   if (a->nx < 2 || a->ny < 2 || a->nz < 2 || a->ne_planes < 0 || a->ne_planes > a->nz - 1) return GM_ERR_ARG;
+  if ((long long)a->nx * a->ny * a->nz >= (1LL << 31)) return GM_ERR_TOO_LARGE;  // node ids are 32-bit
   if ((a->k_arr == nullptr) != (a->rc_arr == nullptr)) return GM_ERR_ARG;
   if (a->bc_mode == 2 && (!a->bc_new || !a->bc_old || !a->bc_map.elem[0] || !a->bc_map.w[0])) return GM_ERR_ARG;
   if ((a->accum == nullptr) != (a->max_accum == nullptr)) return GM_ERR_ARG;

@@ -29,12 +29,73 @@ from levels import Geometry
 PH_S1, PH_S2 = 1, 2
 
 
-class CoupleGeom:
-    """Per-axis tables of a fine level inside a coarse level (gm_couple_geom)."""
+class TableArena:
+    """Per-window tables of one move packed into a pinned host buffer and copied
+    to a device buffer with one non-blocking H2D copy.  Two pinned buffers
+    alternate so the host can fill the next move's tables while the previous
+    copy is in flight; the device buffer is rewritten in stream order."""
 
-    def __init__(self, fine_coords, coarse_coords, dtype, device, pad_ncb=None):
+    ALIGN = 256
+
+    def __init__(self, nbytes, device):
+        self.nbytes = int(nbytes)
+        self.dev = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        self.host = [torch.empty(self.nbytes, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+        self.hview = [h.numpy() for h in self.host]
+        self.evt = [None, None]
+        self.cur = 0
+        self.off = 0
+        self.open = False
+
+    def begin(self):
+        self.cur ^= 1
+        if self.evt[self.cur] is not None:
+            self.evt[self.cur].synchronize()
+        self.off = 0
+        self.open = True
+
+    def put(self, arr, dtype=None):
+        """Stage an array; returns its device address (valid after upload)."""
+        a = np.ascontiguousarray(arr if dtype is None else np.asarray(arr, dtype=dtype))
+        b = a.reshape(-1).view(np.uint8)
+        off = (self.off + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+        if off + b.size > self.nbytes:
+            raise N.GomeltError(f"table arena too small ({off + b.size} > {self.nbytes} bytes)")
+        self.hview[self.cur][off:off + b.size] = b
+        self.off = off + b.size
+        return self.dev.data_ptr() + off
+
+    def upload(self, stream):
+        n = self.off
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            self.dev[:n].copy_(self.host[self.cur][:n], non_blocking=True)
+        e = torch.cuda.Event()
+        e.record(s)
+        self.evt[self.cur] = e
+        self.open = False
+
+
+class ArenaMap3:
+    """gm_map3 whose per-axis tables live in the table arena."""
+
+    def __init__(self, arena, maps, src_nodes, np_dtype):
+        s = N.gm_map3()
+        self.n = [int(m.elem.size) for m in maps]
+        for d, m in enumerate(maps):
+            s.n[d] = self.n[d]
+            s.elem[d] = arena.put(m.elem, np.int32)
+            s.w[d] = arena.put(m.w.reshape(-1), np_dtype)
+        s.src_nx, s.src_ny = int(src_nodes[0]), int(src_nodes[1])
+        self.struct = s
+
+
+class CoupleGeom:
+    """Per-axis tables of a fine level inside a coarse level (gm_couple_geom),
+    staged in the table arena."""
+
+    def __init__(self, fine_coords, coarse_coords, np_dtype, arena):
         self.axes = []
-        self.tensors = []
         g = N.gm_couple_geom()
         for d in range(3):
             xq = quad_points_1d(fine_coords[d])
@@ -49,24 +110,17 @@ class CoupleGeom:
             cells = lo + np.arange(ncb)
             flo = np.searchsorted(node0, cells, side="left")
             fhi = np.searchsorted(node0, cells, side="right")
-            rmax = int((fhi - flo).max())
-            t_cw = torch.as_tensor(cw.reshape(-1), dtype=dtype, device=device)
-            t_n0 = torch.as_tensor(node0.astype(np.int32), device=device)
-            t_flo = torch.as_tensor(flo.astype(np.int32), device=device)
-            t_fhi = torch.as_tensor(fhi.astype(np.int32), device=device)
-            t_xq = torch.as_tensor(xq.reshape(-1), dtype=torch.float64, device=device)
-            self.tensors += [t_cw, t_n0, t_flo, t_fhi, t_xq]
             a = g.ax[d]
             a.nfe = xq.shape[0]
-            a.cw = t_cw.data_ptr()
-            a.node0 = C.cast(t_n0.data_ptr(), C.POINTER(C.c_int))
+            a.cw = arena.put(cw.reshape(-1), np_dtype)
+            a.node0 = C.cast(arena.put(node0, np.int32), C.POINTER(C.c_int))
             a.cb_lo = lo
             a.ncb = ncb
-            a.flo = C.cast(t_flo.data_ptr(), C.POINTER(C.c_int))
-            a.fhi = C.cast(t_fhi.data_ptr(), C.POINTER(C.c_int))
-            a.rmax = rmax
+            a.flo = C.cast(arena.put(flo, np.int32), C.POINTER(C.c_int))
+            a.fhi = C.cast(arena.put(fhi, np.int32), C.POINTER(C.c_int))
+            a.rmax = int((fhi - flo).max())
             a.H = float(H)
-            self.axes.append(dict(lo=lo, ncb=ncb, xq=t_xq))
+            self.axes.append(dict(lo=lo, ncb=ncb, xq=arena.put(xq.reshape(-1), np.float64)))
         self.struct = g
         self.box_lo = [ax["lo"] for ax in self.axes]
         self.box_n = [ax["ncb"] + 1 for ax in self.axes]
@@ -97,6 +151,10 @@ class Engine:
         self.tmp = None
         self._work = None
         self.tables = None
+        self.np_dtype = np.float32 if dtype == torch.float32 else np.float64
+        axes = sum(sum(g.L[lv].nodes) for lv in (1, 2, 3)) + sum(g.L0_nodes)
+        self.arena = TableArena(1 << 20 | (256 * axes + 64 * 1024), self.dev)
+        self.rarena = TableArena(8 * 8 * (self.N2 * self.N3 * 7 + self.N2 + 1) + 4096, self.dev)
 
     # ------------------------------------------------------------------
     # helpers
@@ -112,8 +170,8 @@ class Engine:
         return t[:n]
 
     def _map(self, src_level_coords, src_nodes, tgt_coords):
-        return kern.DeviceMap3([axis_map(src_level_coords[d], tgt_coords[d]) for d in range(3)], src_nodes,
-                               self.dtype, self.dev)
+        return ArenaMap3(self.arena, [axis_map(src_level_coords[d], tgt_coords[d]) for d in range(3)], src_nodes,
+                         self.np_dtype)
 
     def _interp(self, terms, n, out, base=None, out_term=None, which=0):
         a = N.gm_interp_args()
@@ -132,18 +190,22 @@ class Engine:
         N.call("gm_interp", C.byref(a), kern.stream_ptr(self.stream))
 
     def _idx_tensor(self, arrs, nodes, what):
-        """Upload per-axis node-index arrays after checking they address the grid."""
+        """Stage per-axis node-index arrays (device int pointers) after checking
+        they address the grid."""
         for d in range(3):
             a = np.asarray(arrs[d])
             if a.size == 0 or a.min() < 0 or a.max() >= nodes[d]:
                 raise N.GomeltError(f"{what}: axis {d} indices [{a.min() if a.size else '-'}, "
                                     f"{a.max() if a.size else '-'}] outside [0, {nodes[d]})")
-        return [torch.as_tensor(np.asarray(a).astype(np.int32), device=self.dev) for a in arrs]
+        return [C.cast(self.arena.put(a, np.int32), C.POINTER(C.c_int)) for a in arrs]
 
     # ------------------------------------------------------------------
     # per-window tables (rebuilt after every move)
     # ------------------------------------------------------------------
     def build_tables(self):
+        own = not self.arena.open
+        if own:
+            self.arena.begin()
         g = self.geo
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         t = {}
@@ -153,9 +215,9 @@ class Engine:
         t["r21"] = self._map(L2.coords, L2.nodes, L2.overlap_coords)  # Level 2 at Level-1 overlap nodes
         t["r32_idx"] = self._idx_tensor(L3.overlap_nodes, L2.nodes, "Level-3 overlap in Level 2")
         t["r21_idx"] = self._idx_tensor(L2.overlap_nodes, L1.nodes, "Level-2 overlap in Level 1")
-        t["c32"] = CoupleGeom(L3.coords, L2.coords, self.dtype, self.dev)
-        t["c31"] = CoupleGeom(L3.coords, L1.coords, self.dtype, self.dev)
-        t["c21"] = CoupleGeom(L2.coords, L1.coords, self.dtype, self.dev)
+        t["c32"] = CoupleGeom(L3.coords, L2.coords, self.np_dtype, self.arena)
+        t["c31"] = CoupleGeom(L3.coords, L1.coords, self.np_dtype, self.arena)
+        t["c21"] = CoupleGeom(L2.coords, L1.coords, self.np_dtype, self.arena)
         t["l0_3"] = self._idx_tensor(g.L0_overlap, g.L0_nodes, "Level-3 window in Level 0")
         t["l0_2"] = self._idx_tensor(g.L0_overlap_L2, g.L0_nodes, "Level-2 window in Level 0")
         c31, c21 = t["c31"], t["c21"]
@@ -165,6 +227,8 @@ class Engine:
         self.tables = t
         nmax = max(t["c32"].partials, t["c31"].partials, t["c21"].partials)
         self._buf("partials", nmax)
+        if own:
+            self.arena.upload(self.stream)
         return t
 
     # ------------------------------------------------------------------
@@ -175,41 +239,42 @@ class Engine:
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         old3 = [c.copy() for c in L3.coords]
         old2 = [c.copy() for c in L2.coords]
-        old_l0 = [a.copy() for a in g.L0_overlap]
         new3, new2, move_v = g.move(v, vstart)
         n3, n2 = L3.nodes, L2.nodes
+        self.arena.begin()
+        m3 = [self._map(L1.coords, L1.nodes, new3), self._map(old2, L2.nodes, new3), self._map(old3, L3.nodes, new3)]
+        m2 = [self._map(L1.coords, L1.nodes, new2), self._map(old2, L2.nodes, new2)]
+        L3.coords = new3
+        L2.coords = new2
+        t = self.build_tables()
+        self.arena.upload(self.stream)
         # Level 3: T = I_L1(T1) + I_L2(T'2) + I_L3old(T'3); T'3 = I_L3old(T'3)
         T3n = self._buf("mvT3", L3.nn)
         Tp3n = self._buf("mvTp3", L3.nn)
-        self._interp([(self._map(L1.coords, L1.nodes, new3), self.T[1], 1.0),
-                      (self._map(old2, L2.nodes, new3), self.Tp[2], 1.0),
-                      (self._map(old3, L3.nodes, new3), self.Tp[3], 1.0)], n3, T3n, out_term=Tp3n, which=2)
+        self._interp([(m3[0], self.T[1], 1.0), (m3[1], self.Tp[2], 1.0), (m3[2], self.Tp[3], 1.0)], n3, T3n,
+                     out_term=Tp3n, which=2)
         # Level 2: T'2 = I_L2old(T'2); T = I_L1(T1) + T'2
         T2n = self._buf("mvT2", L2.nn)
         Tp2n = self._buf("mvTp2", L2.nn)
-        self._interp([(self._map(L1.coords, L1.nodes, new2), self.T[1], 1.0),
-                      (self._map(old2, L2.nodes, new2), self.Tp[2], 1.0)], n2, T2n, out_term=Tp2n, which=1)
-        self.T[3].copy_(T3n)
-        self.Tp[3].copy_(Tp3n)
-        self.T[2].copy_(T2n)
-        self.Tp[2].copy_(Tp2n)
-        L3.coords = new3
-        L2.coords = new2
+        self._interp([(m2[0], self.T[1], 1.0), (m2[1], self.Tp[2], 1.0)], n2, T2n, out_term=Tp2n, which=1)
+        self.T[3], T3n = T3n, self.T[3]
+        self.Tp[3], Tp3n = Tp3n, self.Tp[3]
+        self.T[2], T2n = T2n, self.T[2]
+        self.Tp[2], Tp2n = Tp2n, self.Tp[2]
+        self._work["mvT3"], self._work["mvTp3"], self._work["mvT2"], self._work["mvTp2"] = T3n, Tp3n, T2n, Tp2n
         # Level-0 gather of the window phases (:2500-2502)
-        l0_3 = self._idx_tensor(g.L0_overlap, g.L0_nodes, "Level-3 window in Level 0")
-        l0_2 = self._idx_tensor(g.L0_overlap_L2, g.L0_nodes, "Level-2 window in Level 0")
         ph3n = self._buf("mvph3", L3.nn, torch.uint8)
-        self._l0_gather(l0_3, n3, ph3n, self.ph[3] if self.s2_prev_lo is not None else None, self.s2_prev_lo, n3)
-        self.ph[3].copy_(ph3n)
-        self._l0_gather(l0_2, n2, self.ph[2], None, None, None)
-        self.build_tables()
+        self._l0_gather(t["l0_3"], n3, ph3n, self.ph[3] if self.s2_prev_lo is not None else None, self.s2_prev_lo,
+                        n3)
+        self.ph[3], self._work["mvph3"] = ph3n, self.ph[3]
+        self._l0_gather(t["l0_2"], n2, self.ph[2], None, None, None)
         return move_v
 
     def _l0_gather(self, idx, n, ph_out, prev_ph, prev_lo, prev_n):
         a = N.gm_l0_args()
         for d in range(3):
             a.n[d] = int(n[d])
-            a.idx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+            a.idx[d] = idx[d]
         a.l0_nx, a.l0_ny = self.geo.L0_nodes[0], self.geo.L0_nodes[1]
         a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
         a.ph = C.cast(ph_out.data_ptr(), C.POINTER(C.c_uint8))
@@ -226,7 +291,7 @@ class Engine:
         a = N.gm_l0_args()
         for d in range(3):
             a.n[d] = g.L[3].nodes[d]
-            a.idx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+            a.idx[d] = idx[d]
         a.l0_nx, a.l0_ny = g.L0_nodes[0], g.L0_nodes[1]
         a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
         a.ph = C.cast(self.ph[3].data_ptr(), C.POINTER(C.c_uint8))
@@ -288,7 +353,7 @@ class Engine:
         a.npos = int(npos)
         a.rows = kern.ptr(rows)
         for d in range(3):
-            a.xq[d] = C.cast(cg.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
+            a.xq[d] = C.cast(cg.axes[d]["xq"], C.POINTER(C.c_double))
             a.out_lo[d] = int(out_lo[d])
             a.out_n[d] = int(out_n[d])
         h = L3.spacing()
@@ -305,7 +370,7 @@ class Engine:
         a.dtype = kern.dtype_code(fine_T)
         for d in range(3):
             a.n[d] = rmap.n[d]
-            a.cidx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+            a.cidx[d] = idx[d]
         a.map = rmap.struct
         a.cnx, a.cny = coarse_nodes[0], coarse_nodes[1]
         a.fine = kern.ptr(fine_T)
@@ -329,7 +394,7 @@ class Engine:
         rmap, idx = self.tables["r21"], self.tables["r21_idx"]
         for d in range(3):
             a.n[d] = rmap.n[d]
-            a.cidx[d] = C.cast(idx[d].data_ptr(), C.POINTER(C.c_int))
+            a.cidx[d] = idx[d]
         a.map = rmap.struct
         a.cnx, a.cny = g.L[1].nodes[0], g.L[1].nodes[1]
         a.fine_ph = C.cast(self.ph[2].data_ptr(), C.POINTER(C.c_uint8))
@@ -354,13 +419,13 @@ class Engine:
         if self.tmp is None:
             raise N.GomeltError("active Level-1 region not set (call set_layer first)")
         dts = np.concatenate([[rows_h[:, 5].sum()], rows_h[:, 5].reshape(N2, N3).sum(axis=1)])
-        if rows_device is not None:
-            rows = rows_device
-        else:
-            rows = self._buf("rows", rows_h.size, torch.float64).view(N2 * N3, 7)
-            rows.copy_(torch.from_numpy(rows_h), non_blocking=False)
-        dtd = self._buf("dts", N2 + 1, torch.float64)
-        dtd.copy_(torch.from_numpy(dts))
+        need = 8 * (rows_h.size + dts.size) + 2 * TableArena.ALIGN
+        if need > self.rarena.nbytes:
+            self.rarena = TableArena(2 * need, self.dev)
+        self.rarena.begin()
+        rows = rows_device.data_ptr() if rows_device is not None else self.rarena.put(rows_h, np.float64)
+        dtd = self.rarena.put(dts, np.float64)
+        self.rarena.upload(self.stream)
         out_hist = None
         if history:
             out_hist = (torch.empty(N2, L2.nn, dtype=self.dtype, device=self.dev),
@@ -393,7 +458,6 @@ class Engine:
         c32, c31, c21 = tb["c32"], tb["c31"], tb["c21"]
         nn1, nn2, nn3 = L1.nn, L2.nn, L3.nn
         u8 = torch.uint8
-        pi = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_int))  # noqa: E731
         pu = lambda t: C.cast(t.data_ptr(), C.POINTER(C.c_uint8))  # noqa: E731
         p = N.gm_subcycle_plan()
         p.dtype = kern.dtype_code(self.T[3])
@@ -406,17 +470,17 @@ class Engine:
         p.acc3, p.macc3 = self.acc3.data_ptr(), self.macc3.data_ptr()
         p.bc12, p.bc23, p.r32, p.r21 = tb["bc12"].struct, tb["bc23"].struct, tb["r32"].struct, tb["r21"].struct
         for d in range(3):
-            p.r32_idx[d] = pi(tb["r32_idx"][d])
-            p.r21_idx[d] = pi(tb["r21_idx"][d])
-            p.xq32[d] = C.cast(c32.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
-            p.xq31[d] = C.cast(c31.axes[d]["xq"].data_ptr(), C.POINTER(C.c_double))
+            p.r32_idx[d] = tb["r32_idx"][d]
+            p.r21_idx[d] = tb["r21_idx"][d]
+            p.xq32[d] = C.cast(c32.axes[d]["xq"], C.POINTER(C.c_double))
+            p.xq31[d] = C.cast(c31.axes[d]["xq"], C.POINTER(C.c_double))
             p.rhs1_lo[d], p.rhs1_n[d] = c21.box_lo[d], c21.box_n[d]
             p.rhs2_lo[d], p.rhs2_n[d] = c32.box_lo[d], c32.box_n[d]
-            p.l0_idx3[d] = pi(tb["l0_3"][d])
+            p.l0_idx3[d] = tb["l0_3"][d]
         p.c32, p.c31, p.c21 = c32.struct, c31.struct, c21.struct
         p.L0 = pu(self.L0)
         p.L0_nx, p.L0_ny = g.L0_nodes[0], g.L0_nodes[1]
-        p.rows, p.dts = rows.data_ptr(), dtd.data_ptr()
+        p.rows, p.dts = rows, dtd
         p.T1p, p.T1c = self._buf("T1p", nn1).data_ptr(), self._buf("T1c", nn1).data_ptr()
         p.T2w[0], p.T2w[1] = self._buf("T2a", nn2).data_ptr(), self._buf("T2b", nn2).data_ptr()
         p.T3w[0], p.T3w[1] = self._buf("T3a", nn3).data_ptr(), self._buf("T3b", nn3).data_ptr()
