@@ -178,6 +178,7 @@ SIGNATURES = {
     "gm_couple": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
     "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
+    "gm_couple_noalloc": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
 }
 
 

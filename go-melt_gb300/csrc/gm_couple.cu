@@ -448,3 +448,54 @@ extern "C" int gm_coarse_source(const gm_coarse_source_args* g, const gm_props* 
   if (g->dtype == GM_F64) return do_source<double>(g, p, st);
   return GM_ERR_ARG;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of gm_couple.
+//
+// Some callers cannot allocate device memory at the moment they need the
+// coupling terms: code that runs while a framework owns the device allocator
+// (for example inside another runtime's custom call), a loop that must not
+// pay the device-wide synchronisation that cudaMalloc/cudaFree can imply, or
+// code that has no way to keep a scratch buffer alive between calls.  For
+// them gm_couple_noalloc keeps gm_couple's partial sums in this fixed array,
+// which every GPU that loads the library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_couple_scratch[GM_COUPLE_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
+
+// Device address of g_couple_scratch on the current device, looked up once per
+// device (host code cannot use the symbol itself as a device pointer).
+int scratch_address(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GM_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (g_scratch_addr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_couple_scratch) != cudaSuccess || p == nullptr) return GM_ERR_CUDA;
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return GM_OK;
+}
+}  // namespace
+
+extern "C" int gm_couple_noalloc(const gm_couple_args* g, const gm_props* p, void* stream) {
+  if (!g || !p || !geom_ok(&g->geom)) return GM_ERR_ARG;
+  const size_t esz = g->dtype == GM_F64 ? sizeof(double) : sizeof(float);
+  const long long need = gm_couple_partials_size(&g->geom);
+  if (need < 0) return GM_ERR_ARG;
+  if ((unsigned long long)need * esz > (unsigned long long)GM_COUPLE_NOALLOC_SCRATCH_BYTES) return GM_ERR_TOO_LARGE;
+  void* scratch = nullptr;
+  const int rc = scratch_address(&scratch);
+  if (rc != GM_OK) return rc;
+  gm_couple_args a = *g;  // same arguments; the caller's partials/partials_cap are not used
+  a.partials = scratch;
+  a.partials_cap = (long long)(GM_COUPLE_NOALLOC_SCRATCH_BYTES / esz);
+  return gm_couple(&a, p, stream);
+}

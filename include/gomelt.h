@@ -272,6 +272,24 @@ typedef struct gm_couple_args {
 
 int gm_couple(const gm_couple_args* a, const gm_props* p, void* stream);
 
+/* Allocation-free form of gm_couple (this entry point has no counterpart in
+ * the reference, which leaves all memory to JAX).  For callers that cannot
+ * allocate device memory when they need the coupling terms -- e.g. code running
+ * while another framework owns the device allocator, or a loop that must not
+ * pay the synchronisation cudaMalloc/cudaFree may cause -- the partial sums
+ * live in a library-owned __device__ array of GM_COUPLE_NOALLOC_SCRATCH_BYTES
+ * (4 MiB: 1 Mi float or 512 Ki double partials), which every GPU that loads
+ * the library keeps until exit.  Arguments are those of gm_couple; `partials`
+ * and `partials_cap` are ignored.  Returns GM_ERR_TOO_LARGE when the coupling
+ * needs more partials than the array holds (gm_couple_partials_size * element
+ * size > 4 MiB).  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The array is shared by all calls and keeps the last call's contents; every
+ * call overwrites all partials it reads, so nothing needs clearing, but calls
+ * that overlap on the GPU (different streams, no ordering) race on it. */
+#define GM_COUPLE_NOALLOC_SCRATCH_BYTES (4u << 20)
+int gm_couple_noalloc(const gm_couple_args* a, const gm_props* p, void* stream);
+
 /* Coarse laser source averaged over npos laser rows (computeLevelSource
  * :2667-2730; with npos = 1 the Fc/Fm of computeSources :928-988), added into
  * `out` (coarse node box as in gm_couple).  rows: device array of npos rows of
