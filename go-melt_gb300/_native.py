@@ -52,6 +52,11 @@ class gm_level_args(C.Structure):
     ]
 
 
+class gm_ring_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("nodes", C.c_int * 3), ("map", gm_map3), ("srcA", vp), ("srcB", vp),
+                ("outA", vp), ("outB", vp)]
+
+
 class gm_state_props_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_longlong), ("T", vp), ("ph_in", C.POINTER(C.c_uint8)),
                 ("ph_out", C.POINTER(C.c_uint8)), ("k_out", vp), ("rc_out", vp), ("substrate", C.c_longlong)]
@@ -126,14 +131,15 @@ class gm_subcycle_plan(C.Structure):
         ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
-        ("zchunk", C.c_int)]
+        ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2)]
 
 
 def subcycle_kernel_count(N2: int, N3: int) -> int:
-    """Kernels gm_subcycle launches: set-up and Level 1 (8), two passes of
-    N2 Level-2 steps (coupling 2, source 2, Level-2 solve, N3 Level-3 solves,
-    restriction, T'), the T'2/mass/corrector block (7) and the tail (3)."""
-    return 18 + 2 * N2 * (7 + N3)
+    """Kernels gm_subcycle launches: set-up and Level 1 (8), two passes of a
+    Level-2 ring prolongation plus N2 Level-2 steps (coupling 2, source 2,
+    Level-2 solve, Level-3 ring, N3 Level-3 solves, restriction, T'), the
+    T'2/mass/corrector block (7) and the tail (3)."""
+    return 18 + 2 * (1 + N2 * (8 + N3))
 
 
 _lib = None
@@ -178,6 +184,7 @@ SIGNATURES = {
     "gm_couple": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
     "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
+    "gm_ring_prolong": [C.POINTER(gm_ring_args), vp],
     "gm_couple_noalloc": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
 }
 

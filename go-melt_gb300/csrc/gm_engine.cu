@@ -8,7 +8,9 @@
 //   Level-1 predictor (:3294-3305)
 //   pass 1: per Level-2 step: Level-2 RHS (source of its rows + L3 T' flux),
 //           Level-2 solve with the blended Level-1 ring, N3 Level-3 solves with
-//           the blended Level-2 ring, restriction + T'3 (:3307-3430)
+//           the blended Level-2 ring, restriction + T'3 (:3307-3430); the two
+//           coarse fields of each blend are prolongated onto the ring once
+//           (per pass for Level 2, per Level-2 step for Level 3)
 //   T'2, Level-1 mass terms, Level-1 corrector (:3432-3456)
 //   pass 2: as pass 1 from the saved state, plus the Level-2 mass term and the
 //           Level-3 melt-time update (:3458-3622)
@@ -74,12 +76,12 @@ void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tou
   if (bc_mode == 1) {
     for (int i = 0; i < 5; ++i) a.face[i] = p.face[i];
     a.inactive_amb = 1;
-  } else if (bc_mode == 2) {
+  } else if (bc_mode == 2 || bc_mode == 3) {
     a.bc_new = bnew;
     a.bc_old = bold;
     a.bc_alpha = alpha;
     a.bc_beta = 1.0 - alpha;
-    a.bc_map = *map;
+    if (map) a.bc_map = *map;
   }
   a.clamp = 1;
   a.accum = acc;
@@ -189,6 +191,21 @@ void copy(Ctx& c, void* dst, const void* src, long long bytes) {
     c.rc = GM_ERR_CUDA;
 }
 
+// Both coarse fields of a blend prolongated onto a fine level's ring once
+// (gm_ring_prolong); the level steps then use bc_mode 3.
+void ring(Ctx& c, const gm_window& fine, const gm_map3& map, const void* A, const void* B, void* outA, void* outB) {
+  gm_ring_args r;
+  memset(&r, 0, sizeof(r));
+  r.dtype = c.p->dtype;
+  for (int d = 0; d < 3; ++d) r.nodes[d] = fine.nodes[d];
+  r.map = map;
+  r.srcA = A;
+  r.srcB = B;
+  r.outA = outA;
+  r.outB = outB;
+  GM_TRY(gm_ring_prolong(&r, c.st));
+}
+
 struct PassOut {
   void* T2;
   uint8_t* ph2;
@@ -208,6 +225,7 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
   uint8_t* ph3c = p.L3.ph;
   void* Tp3c = p.L3.Tp;
   const long long nrhs2 = (long long)p.rhs2_n[0] * p.rhs2_n[1] * p.rhs2_n[2];
+  ring(c, p.L2, p.bc12, T1new, p.L1.T, p.ring2[0], p.ring2[1]);
   for (int l2 = 0; l2 < N2; ++l2) {
     void* hist_l2 = at(p.tp3hist, l2 * n3, c.esz);
     const double* dt2 = p.dts + 1 + l2;
@@ -219,15 +237,16 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
     source(c, p.c32, p.xq32, p.rows + (long long)l2 * N3 * 7, N3, p.rhs2, p.rhs2_lo, p.rhs2_n);
     void* T2n = p.T2w[l2 % 2];
     uint8_t* ph2n = p.ph2w[l2 % 2];
-    level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 2, &p.bc12,
-          T1new, p.L1.T, (l2 + 1) / (double)N2, nullptr, nullptr);
+    level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 3, nullptr,
+          p.ring2[0], p.ring2[1], (l2 + 1) / (double)N2, nullptr, nullptr);
+    ring(c, p.L3, p.bc23, T2n, T2c, p.ring3[0], p.ring3[1]);
     for (int l3 = 0; l3 < N3; ++l3) {
       const int i = l2 * N3 + l3;
       void* Tn = p.T3w[i % 2];
       uint8_t* phn = p.ph3w[i % 2];
       const double* row = p.rows + (long long)i * 7;
-      level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 2, &p.bc23, T2n,
-            T2c, (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr);
+      level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 3, nullptr,
+            p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr);
       T3c = Tn;
       ph3c = phn;
     }
@@ -253,7 +272,7 @@ bool plan_ok(const gm_subcycle_plan* p) {
   if (!p->L2.Tp || !p->L3.Tp || !p->acc3 || !p->macc3) return false;
   if (!p->T1p || !p->T1c || !p->T2w[0] || !p->T2w[1] || !p->T3w[0] || !p->T3w[1] || !p->tp3w[0] || !p->tp3w[1] ||
       !p->Tp2w || !p->rhs1 || !p->rhs2 || !p->tp3hist || !p->ph2w[0] || !p->ph2w[1] || !p->ph3w[0] || !p->ph3w[1] ||
-      !p->partials || !p->src_scratch || !p->L0)
+      !p->partials || !p->src_scratch || !p->L0 || !p->ring2[0] || !p->ring2[1] || !p->ring3[0] || !p->ring3[1])
     return false;
   if ((p->L2all == nullptr) != (p->L3all == nullptr) || (p->L2all == nullptr) != (p->L3pall == nullptr)) return false;
   return true;

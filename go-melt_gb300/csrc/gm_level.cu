@@ -92,22 +92,21 @@ __device__ __forceinline__ void bfly_inv(real v[8]) {
 
 // 1-D source factor of node i: sum over the (up to two) elements touching the
 // node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
-// The offset xq - v is formed in double (coordinates are absolute); the
-// exponential is evaluated in the kernel's precision.
+// rel = origin - v (formed in double by the caller), so the Gauss-point
+// offset rel + h*(e + (1 +- 1/sqrt3)/2) is small and exact enough in the
+// kernel's precision.
 template <typename real>
-__device__ __forceinline__ real src_factor(int i, int n, double o, double h, double v, double inv_r2) {
-  const double xi[2] = {-0.57735026918962576451, 0.57735026918962576451};
+__device__ __forceinline__ real src_factor(int i, int n, real rel, real h, real inv_r2) {
+  const real g0 = (real)0.21132486540518711775, g1 = (real)0.78867513459481288225;  // (1 -+ 1/sqrt3)/2
   real s = 0;
   for (int e = i - 1; e <= i; ++e) {
     if (e < 0 || e >= n - 1) continue;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const double xq = o + e * h + 0.5 * (1.0 + xi[q]) * h;
-      const double d = xq - v;
-      const real g = exp((real)(-3.0 * d * d * inv_r2));
-      const real phi = (real)((i == e) ? 0.5 * (1.0 - xi[q]) : 0.5 * (1.0 + xi[q]));
-      s += phi * g;
-    }
+    const real d0 = rel + h * ((real)e + g0);
+    const real d1 = rel + h * ((real)e + g1);
+    const real q0 = exp((real)-3 * d0 * d0 * inv_r2);
+    const real q1 = exp((real)-3 * d1 * d1 * inv_r2);
+    // node i is local node 0 of element e when i == e: weights (1-xi)/2 = g1 at xi=-1/sqrt3, g0 at +1/sqrt3
+    s += (i == e) ? (g1 * q0 + g0 * q1) : (g0 * q0 + g1 * q1);
   }
   return s;
 }
@@ -161,6 +160,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
   const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
   const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
   const real dt = (real)(*a.dt);
+  const real inv_dt = (real)1 / dt;
   const Props<real>& P = a.p;
 
   // ---- per-thread staging slots (constant over the plane loop) ----
@@ -222,18 +222,19 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
   fetch(Z0 + 1);
   real srcP = 0;
   if (a.laser != nullptr) {
-    const double vx = a.laser[0], vy = a.laser[1], vz = a.laser[2];
+    const real rx = (real)(a.ox - a.laser[0]), ry = (real)(a.oy - a.laser[1]), rz = (real)(a.oz - a.laser[2]);
+    const real ir2 = (real)a.inv_r2, id2 = (real)a.inv_d2;
     srcP = (real)(a.src_c * a.laser[6]);
     for (int i = tid; i < PX + PY + (Z1 - Z0); i += NT) {
       if (i < PX) {
         const int g = X0 - 1 + i;
-        sSx[i] = (g >= 0 && g < nx) ? src_factor<real>(g, nx, a.ox, a.hx, vx, a.inv_r2) : (real)0;
+        sSx[i] = (g >= 0 && g < nx) ? src_factor<real>(g, nx, rx, (real)a.hx, ir2) : (real)0;
       } else if (i < PX + PY) {
         const int g = Y0 - 1 + (i - PX);
-        sSy[i - PX] = (g >= 0 && g < ny) ? src_factor<real>(g, ny, a.oy, a.hy, vy, a.inv_r2) : (real)0;
+        sSy[i - PX] = (g >= 0 && g < ny) ? src_factor<real>(g, ny, ry, (real)a.hy, ir2) : (real)0;
       } else {
         const int g = Z0 + (i - PX - PY);
-        sSz[i - PX - PY] = src_factor<real>(g, nz, a.oz, a.hz, vz, a.inv_d2);
+        sSz[i - PX - PY] = src_factor<real>(g, nz, rz, (real)a.hz, id2);
       }
     }
   }
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
         R[4 + c] = tu[c];
       }
       const real kbar = (ksl + ksu) * (real)0.125;
-      me = a.wvol * ((csl + csu) * (real)0.125) / dt;
+      me = a.wvol * ((csl + csu) * (real)0.125) * inv_dt;
       bfly_fwd(R);
 #pragma unroll
       for (int m = 0; m < 8; ++m) R[m] *= a.lam[m] * kbar;
@@ -355,6 +356,8 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
         if (ix == 0) Tn = a.face[0];
         if (ix == nx - 1) Tn = a.face[1];
         if (ke == 0) Tn = a.face[4];
+      } else if (a.bc_mode == 3 && (ring_xy || ke == 0)) {
+        Tn = a.bc_alpha * a.bc_new[id] + a.bc_beta * a.bc_old[id];
       } else if (a.bc_mode == 2 && (ring_xy || ke == 0)) {
         real w8[8];
         const int b = map3_weights(a.bc_map, ix, iy, ke, w8);
@@ -495,6 +498,8 @@ extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* st
   if ((long long)a->nx * a->ny * a->nz >= (1LL << 31)) return GM_ERR_TOO_LARGE;  // node ids are 32-bit
   if ((a->k_arr == nullptr) != (a->rc_arr == nullptr)) return GM_ERR_ARG;
   if (a->bc_mode == 2 && (!a->bc_new || !a->bc_old || !a->bc_map.elem[0] || !a->bc_map.w[0])) return GM_ERR_ARG;
+  if (a->bc_mode == 3 && (!a->bc_new || !a->bc_old)) return GM_ERR_ARG;
+  if (a->bc_mode < 0 || a->bc_mode > 3) return GM_ERR_ARG;
   if ((a->accum == nullptr) != (a->max_accum == nullptr)) return GM_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (a->dtype == GM_F32) return gm::launch_level<float>(a, p, st);
@@ -531,8 +536,8 @@ __global__ void fine_source_kernel(int nx, int ny, int nz, double ox, double oy,
   const double c = src_c * laser[6];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int ix = (int)(i % nx), iy = (int)((i / nx) % ny), iz = (int)(i / ((long long)nx * ny));
-    F[i] += (real)(c * src_factor<double>(ix, nx, ox, hx, vx, 1.0 / rsq) *
-                   src_factor<double>(iy, ny, oy, hy, vy, 1.0 / rsq) * src_factor<double>(iz, nz, oz, hz, vz, 1.0 / dsq));
+    F[i] += (real)(c * src_factor<double>(ix, nx, ox - vx, hx, 1.0 / rsq) *
+                   src_factor<double>(iy, ny, oy - vy, hy, 1.0 / rsq) * src_factor<double>(iz, nz, oz - vz, hz, 1.0 / dsq));
   }
 }
 

@@ -310,3 +310,71 @@ extern "C" int gm_clamp_min(int dtype, void* T, long long n, double lo, void* st
     return GM_ERR_ARG;
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
+
+// Prolongation onto the Dirichlet ring of a fine level (faces x0, x1, y0, y1
+// and the bottom plane; computeL2Temperature :2937-2955, computeSolutions_L3
+// :3039-3052): outA = I(srcA), outB = I(srcB) at the ring nodes only, written
+// at their node ids in full-size arrays.  The reference blends the coarse
+// field first, I(alpha*Tn + beta*To); the level kernel forms
+// alpha*I(Tn) + beta*I(To), the same linear combination, so both
+// prolongations are computed once for all fine steps that share Tn and To.
+template <typename real>
+__global__ void ring_kernel(int nx, int ny, int nz, const Map3<real> m, const real* srcA, const real* srcB,
+                            real* outA, real* outB) {
+  const long long nb = (long long)nx * ny;                // bottom plane
+  const long long nxf = 2LL * ny * (nz - 1);              // x faces above the bottom
+  const long long nyf = 2LL * (nx > 2 ? nx - 2 : 0) * (nz - 1);  // y faces, x interior
+  const long long tot = nb + nxf + nyf;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < tot; r += (long long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    if (r < nb) {
+      ix = (int)(r % nx);
+      iy = (int)(r / nx);
+      iz = 0;
+    } else if (r < nb + nxf) {
+      const long long q = r - nb;
+      iz = 1 + (int)(q % (nz - 1));
+      const long long q2 = q / (nz - 1);
+      iy = (int)(q2 % ny);
+      ix = (q2 / ny) ? nx - 1 : 0;
+    } else {
+      const long long q = r - nb - nxf;
+      iz = 1 + (int)(q % (nz - 1));
+      const long long q2 = q / (nz - 1);
+      ix = 1 + (int)(q2 % (nx - 2));
+      iy = (q2 / (nx - 2)) ? ny - 1 : 0;
+    }
+    real w8[8];
+    const int b = map3_weights(m, ix, iy, iz, w8);
+    const int sx = 1, sy = m.src_nx, sz = m.src_nx * m.src_ny;
+    const int off[8] = {0, sx, sx + sy, sy, sz, sx + sz, sx + sy + sz, sy + sz};
+    real a = 0, c = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      a += w8[j] * srcA[b + off[j]];
+      if (srcB) c += w8[j] * srcB[b + off[j]];
+    }
+    const long long id = ix + (long long)iy * nx + (long long)iz * nx * ny;
+    outA[id] = a;
+    if (outB) outB[id] = c;
+  }
+}
+
+extern "C" int gm_ring_prolong(const gm_ring_args* g, void* stream) {
+  if (!g || !g->srcA || !g->outA || (g->srcB == nullptr) != (g->outB == nullptr)) return GM_ERR_ARG;
+  if (g->nodes[0] < 2 || g->nodes[1] < 2 || g->nodes[2] < 2 || !map_ok(g->map, g->nodes)) return GM_ERR_ARG;
+  const long long nx = g->nodes[0], ny = g->nodes[1], nz = g->nodes[2];
+  const long long tot = nx * ny + 2 * ny * (nz - 1) + 2 * (nx - 2) * (nz - 1);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->dtype == GM_F32)
+    ring_kernel<float><<<grid_for(tot), 256, 0, st>>>(g->nodes[0], g->nodes[1], g->nodes[2], make_map3<float>(g->map),
+                                                      (const float*)g->srcA, (const float*)g->srcB, (float*)g->outA,
+                                                      (float*)g->outB);
+  else if (g->dtype == GM_F64)
+    ring_kernel<double><<<grid_for(tot), 256, 0, st>>>(g->nodes[0], g->nodes[1], g->nodes[2],
+                                                       make_map3<double>(g->map), (const double*)g->srcA,
+                                                       (const double*)g->srcB, (double*)g->outA, (double*)g->outB);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}

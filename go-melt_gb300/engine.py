@@ -301,8 +301,24 @@ class Engine:
     # ------------------------------------------------------------------
     # building blocks
     # ------------------------------------------------------------------
+    def _ring(self, lev, A, B):
+        """Prolongate the coarse fields A and B onto the Dirichlet ring of
+        level `lev` (gm_ring_prolong); returns the two ring arrays that a
+        `_level(..., ring=...)` call blends."""
+        L = self.geo.L[lev]
+        outA, outB = self._buf(f"ring{lev}a", L.nn), self._buf(f"ring{lev}b", L.nn)
+        a = N.gm_ring_args()
+        a.dtype = kern.dtype_code(A)
+        for d in range(3):
+            a.nodes[d] = L.nodes[d]
+        a.map = (self.tables["bc12"] if lev == 2 else self.tables["bc23"]).struct
+        a.srcA, a.srcB = kern.ptr(A), kern.ptr(B)
+        a.outA, a.outB = kern.ptr(outA), kern.ptr(outB)
+        N.call("gm_ring_prolong", C.byref(a), kern.stream_ptr(self.stream))
+        return outA, outB
+
     def _level(self, lev, T_in, T_out, dt, ph_in, ph_out, *, rhs=None, box=None, laser=None, bc_new=None,
-               bc_old=None, alpha=0.0, accum=False, clamp=True):
+               bc_old=None, alpha=0.0, accum=False, clamp=True, ring=None):
         g = self.geo
         L = g.L[lev]
         kw = {}
@@ -310,6 +326,9 @@ class Engine:
             ne_planes = self.tmp[0] // (L.elements[0] * L.elements[1])
             c = g.conditions
             kw.update(bc_mode=1, face=[c["x"][0], c["x"][1], c["y"][0], c["y"][1], c["z"][0]], inactive_amb=1)
+        elif ring is not None:
+            ne_planes = L.elements[2]
+            kw.update(bc_mode=3, bc_new=ring[0], bc_old=ring[1], bc_alpha=alpha, bc_beta=1.0 - alpha)
         else:
             ne_planes = L.elements[2]
             m = self.tables["bc12"] if lev == 2 else self.tables["bc23"]
@@ -499,6 +518,8 @@ class Engine:
         if out_hist is not None:
             p.L2all, p.L3all, p.L3pall = (t.data_ptr() for t in out_hist)
         p.zchunk = int(getattr(self, "zchunk", 0))
+        p.ring2[0], p.ring2[1] = self._buf("ring2a", nn2).data_ptr(), self._buf("ring2b", nn2).data_ptr()
+        p.ring3[0], p.ring3[1] = self._buf("ring3a", nn3).data_ptr(), self._buf("ring3b", nn3).data_ptr()
         return p
 
     # ------------------------------------------------------------------

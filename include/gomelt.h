@@ -85,7 +85,8 @@ typedef struct gm_level_args {
   int box[6];                  /* box: x0,x1,y0,y1,z0,z1 (half-open) */
   const double* laser;         /* device laser row (x,y,z,...,P at [6]); NULL: no source */
   int surface;                 /* 1: conv/rad/evap flux on the top active plane */
-  int bc_mode;                 /* 0: none, 1: constant faces, 2: prolongated coarse field */
+  int bc_mode;                 /* 0: none, 1: constant faces, 2: prolongated coarse field,
+                                  3: bc_new/bc_old are prolongated ring arrays of this level */
   double face[5];              /* bc_mode 1: x0, x1, y0, y1, z0 face values */
   int inactive_amb;            /* 1: nodes above the active region set to T_amb */
   const void* bc_new;          /* bc_mode 2: coarse field alpha*bc_new + beta*bc_old */
@@ -204,6 +205,25 @@ typedef struct gm_l0_args {
   const uint8_t* prev_ph; /* gather only; NULL: no S2 anywhere */
   int prev_lo[3], prev_n[3];
 } gm_l0_args;
+
+/* Prolongation of one or two coarse fields onto the Dirichlet ring of a fine
+ * level (faces x0, x1, y0, y1 and the bottom plane), written at the ring
+ * nodes' ids in full-size arrays: outA = I(srcA), outB = I(srcB) (the
+ * interpolate_w_matrix + assignBCsFine of computeL2Temperature :2937-2955 and
+ * computeSolutions_L3 :3039-3052, with the coarse blend applied afterwards by
+ * gm_level_step's bc_mode 3).  map: coarse grid -> fine nodes; srcB/outB
+ * optional together. */
+typedef struct gm_ring_args {
+  int dtype;
+  int nodes[3];
+  gm_map3 map;
+  const void* srcA;
+  const void* srcB;
+  void* outA;
+  void* outB;
+} gm_ring_args;
+
+int gm_ring_prolong(const gm_ring_args* a, void* stream);
 
 /* T = max(T, lo) over n values (the T >= T_amb clamp of stepGOMELT,
  * :2360-2362, :2380-2382). */
@@ -368,6 +388,8 @@ typedef struct gm_subcycle_plan {
   void* L3all;               /* optional (N2*nn3): Level-3 T */
   void* L3pall;              /* optional (N2*nn3): Level-3 T' */
   int zchunk;                /* level-kernel tuning (0: automatic) */
+  void* ring2[2];            /* work: Level-2 ring prolongations (nn2 each) */
+  void* ring3[2];            /* work: Level-3 ring prolongations (nn3 each) */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
