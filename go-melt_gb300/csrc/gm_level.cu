@@ -21,6 +21,8 @@
 // carry from one plane to the next.  Each CTA writes 31 x (BY-1) node columns.
 #include <math.h>
 
+#include <type_traits>
+
 #include "gm_common.cuh"
 
 namespace gm {
@@ -120,10 +122,11 @@ __device__ __forceinline__ float fast_div<float>(float a, float b) {
   return __fdividef(a, b);
 }
 
-// Phase and properties with selects (same values as node_props).
+// Phase and properties with selects (same values as node_props).  Returns the
+// new phase bits (bit0 S1, bit1 S2).
 template <typename real>
-__device__ __forceinline__ uint8_t node_props_sel(const Props<real>& p, real T, uint8_t ph_old, bool substrate,
-                                                  real& k, real& rc) {
+__device__ __forceinline__ uint32_t node_props_sel(const Props<real>& p, real T, uint32_t ph_old, bool substrate,
+                                                   real& k, real& rc) {
   const bool s2 = T >= p.T_liquidus;
   const bool s3 = (T > p.T_solidus) && (T < p.T_liquidus);
   const bool s1 = (ph_old & PH_S1) || s2 || substrate;
@@ -131,34 +134,85 @@ __device__ __forceinline__ uint8_t node_props_sel(const Props<real>& p, real T, 
   const real cs = p.cp_solid_a1 * T + p.cp_solid_a0;
   k = s2 ? p.k_fluid : (s1 ? kb : p.k_powder);
   rc = p.rho * (s2 ? p.cp_fluid : (s3 ? p.cp_mushy : cs));
-  return (uint8_t)((s1 ? PH_S1 : 0) | (s2 ? PH_S2 : 0));
+  return (s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u);
 }
 
+// One staged node (or one exchanged corner sum) as a single 16/32-byte
+// shared-memory record.
+template <typename real>
+struct alignas(4 * sizeof(real)) V4 {
+  real x, y, z, w;
+};
+__device__ __forceinline__ float bits_as_real(uint32_t u, float) { return __uint_as_float(u); }
+__device__ __forceinline__ double bits_as_real(uint32_t u, double) { return __longlong_as_double((long long)u); }
+__device__ __forceinline__ uint32_t real_bits(float r) { return __float_as_uint(r); }
+__device__ __forceinline__ uint32_t real_bits(double r) { return (uint32_t)__double_as_longlong(r); }
+
+// Feature flags of a level-step instantiation.  LF_GENERIC compiles every
+// feature with run-time checks; the other combinations are the ones the
+// subcycle orchestrator issues, with every check resolved at compile time.
+enum : int {
+  LF_LASER = 1 << 0,
+  LF_BOX = 1 << 1,
+  LF_FULL = 1 << 2,
+  LF_KARR = 1 << 3,
+  LF_ACCUM = 1 << 4,
+  LF_SURF = 1 << 5,
+  LF_CLAMP = 1 << 6,
+  LF_INACT = 1 << 7,
+  LF_BC1 = 1 << 8,
+  LF_BC2 = 1 << 9,
+  LF_BC3 = 1 << 10,
+  LF_PHIN = 1 << 11,
+  LF_PHOUT = 1 << 12,
+  LF_GENERIC = 1 << 20
+};
+constexpr int LF_L3 = LF_LASER | LF_SURF | LF_CLAMP | LF_BC3 | LF_PHIN | LF_PHOUT;  // Level-3 step
+constexpr int LF_L3ACC = LF_L3 | LF_ACCUM;                                         // ... with melt time
+constexpr int LF_L2 = LF_BOX | LF_SURF | LF_CLAMP | LF_BC3 | LF_PHIN | LF_PHOUT;   // Level-2 step
+constexpr int LF_L1 = LF_BOX | LF_SURF | LF_CLAMP | LF_INACT | LF_BC1 | LF_PHIN | LF_PHOUT;  // Level-1 step
+
 // Pipeline per CTA (one barrier per node plane):
-//   smem ring of 3 node planes (T, k, rho*c, new phase); at the start of
-//   iteration ke it holds planes ke and ke+1, registers hold plane ke+2
-//   (loaded during the previous iteration).  Iteration ke reads the upper
-//   corners (plane ke+1), writes plane ke+2 into the free slot, issues the
-//   loads of plane ke+3, computes element plane ke, exchanges corner sums
-//   (shuffle in x, shared memory in y), passes the barrier and finalizes node
-//   plane ke.  Lower-plane corner values are carried in registers; all
-//   per-thread indexing is computed once, outside the plane loop.
-template <typename real, int BY>
-__global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<real> a) {
+//   two shared-memory slots of staged node planes (T, k, rho*c, phase bits),
+//   plane p in slot p&1; the loop is unrolled by two so that every slot
+//   address is a compile-time offset.  Iteration ke reads the upper corners
+//   (plane ke+1, slot (ke+1)&1), stages plane ke+2 (loaded into registers
+//   during the previous iteration) into slot ke&1, whose plane ke was last
+//   read before the previous barrier, issues the loads of plane ke+3 and of
+//   the per-node inputs of node plane ke+1 (ring values, RHS box, melt time),
+//   computes element plane ke, exchanges corner sums (shuffle in x, shared
+//   memory in y), passes the barrier and finalizes node plane ke.  Lower-plane
+//   corner values are carried in registers.  Staged phase bits: bit0/1 the
+//   new S1/S2, bit2 the old S2 (melt-time reset).
+template <typename real, int BY, int FL>
+__global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
+  constexpr bool G = (FL & LF_GENERIC) != 0;
   constexpr int TX = 32, PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
   constexpr int NSLOT = (NP + NT - 1) / NT;
-  __shared__ real sT[3][PY * PX];
-  __shared__ real sK[3][PY * PX];
-  __shared__ real sC[3][PY * PX];
-  __shared__ uint8_t sP[3][PY * PX];
-  __shared__ real sX[2][3][BY][TX];
+  static_assert(NT <= NP, "slot 0 covers every thread");
+  __shared__ V4<real> sN[2][NP];
+  __shared__ V4<real> sX[2][BY][TX];
   __shared__ real sSx[PX], sSy[PY], sSz[ZMAX];
+
+  const bool hLaser = G ? a.laser != nullptr : (FL & LF_LASER) != 0;
+  const bool hBox = G ? a.rhs_box != nullptr : (FL & LF_BOX) != 0;
+  const bool hF = G && a.F_full != nullptr;
+  const bool hCorr = G && a.corr_full != nullptr;
+  const bool hKarr = G && a.k_arr != nullptr;
+  const bool hAcc = G ? a.accum != nullptr : (FL & LF_ACCUM) != 0;
+  const bool hSurf = G ? a.surface != 0 : (FL & LF_SURF) != 0;
+  const bool hClamp = G ? a.clamp != 0 : (FL & LF_CLAMP) != 0;
+  const bool hInact = G ? a.inactive_amb != 0 : (FL & LF_INACT) != 0;
+  const bool hPhin = G ? a.ph_in != nullptr : (FL & LF_PHIN) != 0;
+  const bool hPhout = G ? a.ph_out != nullptr : (FL & LF_PHOUT) != 0;
+  const int bcm = G ? a.bc_mode : ((FL & LF_BC1) ? 1 : ((FL & LF_BC3) ? 3 : 0));
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int nxy = nx * ny;
   const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
-  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);  // zchunk is even: Z0 is even
+  const int subs = a.substrate > (long long)nxy * nz ? nxy * nz : (int)a.substrate;
   const real dt = (real)(*a.dt);
   const real inv_dt = (real)1 / dt;
   const Props<real>& P = a.p;
@@ -166,7 +220,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
   // ---- per-thread staging slots (constant over the plane loop) ----
   int sbase[NSLOT];  // node id of the slot in plane 0, or -1 outside the grid / tile
   real pfT[NSLOT];
-  uint8_t pfP[NSLOT];
+  uint32_t pfP[NSLOT];
 #pragma unroll
   for (int s = 0; s < NSLOT; ++s) {
     const int i = tid + s * NT;
@@ -185,7 +239,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
       if (pin && sbase[s] >= 0) {
         const int id = sbase[s] + pl * nxy;
         pfT[s] = a.T_in[id];
-        if (a.ph_in) pfP[s] = a.ph_in[id];
+        if (hPhin) pfP[s] = a.ph_in[id];
       }
     }
   };
@@ -194,34 +248,35 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
 #pragma unroll
     for (int s = 0; s < NSLOT; ++s) {
       const int i = tid + s * NT;
-      if (i < NP) {
+      if (s == 0 || i < NP) {
         real k = 0, c = 0;
-        uint8_t ph = 0;
+        uint32_t ph = 0;
         if (pin && sbase[s] >= 0) {
           const int id = sbase[s] + pl * nxy;
-          ph = node_props_sel(P, pfT[s], pfP[s], (long long)id < a.substrate, k, c);
-          if (a.k_arr) {
+          ph = node_props_sel(P, pfT[s], pfP[s], id < subs, k, c) | ((pfP[s] & PH_S2) << 1);
+          if (hKarr) {
             k = a.k_arr[id];
             c = a.rc_arr[id];
           }
         }
-        sT[slot][i] = pfT[s];
-        sK[slot][i] = k;
-        sC[slot][i] = c;
-        sP[slot][i] = ph;
+        V4<real> r;
+        r.x = pfT[s];
+        r.y = k;
+        r.z = c;
+        r.w = bits_as_real(ph, real(0));
+        sN[slot][i] = r;
       }
     }
   };
 
-  // ---- prologue: planes Z0-1, Z0 in shared memory, plane Z0+1 in registers ----
-  int s_lo = 0, s_up = 1, s_nx = 2;  // ring slots of planes ke, ke+1, ke+2
+  // ---- prologue: planes Z0-1 (slot 1), Z0 (slot 0) staged, plane Z0+1 in registers ----
   fetch(Z0 - 1);
-  store(Z0 - 1, s_lo);
+  store(Z0 - 1, 1);
   fetch(Z0);
-  store(Z0, s_up);
+  store(Z0, 0);
   fetch(Z0 + 1);
   real srcP = 0;
-  if (a.laser != nullptr) {
+  if (hLaser) {
     const real rx = (real)(a.ox - a.laser[0]), ry = (real)(a.oy - a.laser[1]), rz = (real)(a.oz - a.laser[2]);
     const real ir2 = (real)a.inv_r2, id2 = (real)a.inv_d2;
     srcP = (real)(a.src_c * a.laser[6]);
@@ -246,39 +301,65 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
   const bool out_col = tx < TX - 1 && ty < BY - 1 && ix < nx && iy < ny;
   const int top_el = a.ne_planes - 1;
   const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
-  const int c00 = ty * PX + tx;  // smem offset of this element's (0,0) corner
+  const int c00 = ty * PX + tx;  // slot offset of this element's (0,0) corner
   const int nid0 = ix + iy * nx;  // node id of this thread's output column in plane 0
   const bool ring_xy = ix == 0 || ix == nx - 1 || iy == 0 || iy == ny - 1;
-  const bool box_xy = a.rhs_box != nullptr && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3];
+  const bool box_xy = hBox && ix >= a.box[0] && ix < a.box[1] && iy >= a.box[2] && iy < a.box[3];
   const int box_off = box_xy ? (ix - a.box[0]) + (iy - a.box[2]) * (a.box[1] - a.box[0]) : 0;
   const int box_pl = (a.box[1] - a.box[0]) * (a.box[3] - a.box[2]);
-  const real srcxy = (a.laser != nullptr && out_col) ? srcP * sSx[tx + 1] * sSy[ty + 1] : (real)0;
+  const real srcxy = (hLaser && out_col) ? srcP * sSx[tx + 1] * sSy[ty + 1] : (real)0;
 
-  // carried lower-plane corners (plane Z0-1)
+  // carried lower-plane corners (plane Z0-1, slot 1)
   real tl[4], ksl = 0, csl = 0;
-  uint8_t phl;
+  uint32_t phl = 0;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const int o = c00 + (c >> 1) * PX + (c & 1);
-    tl[c] = sT[s_lo][o];
-    ksl += sK[s_lo][o];
-    csl += sC[s_lo][o];
+    const V4<real> r = sN[1][c00 + (c >> 1) * PX + (c & 1)];
+    tl[c] = r.x;
+    ksl += r.y;
+    csl += r.z;
+    if (c == 3) phl = real_bits(r.w);
   }
-  phl = sP[s_lo][c00 + PX + 1];
+  __syncthreads();  // slot 1 is restaged in the first iteration
 
+  // per-node inputs of the node plane finalized next (loaded one iteration ahead)
+  real cRhs = 0, cBA = 0, cBB = 0, cAcc = 0, cMacc = 0, cF = 0, cC = 0;
   real carryU = 0, carryM = 0;
-  for (int ke = Z0 - 1; ke < Z1; ++ke) {
+
+  auto body = [&](auto par, int ke) {
+    constexpr int PAR = decltype(par)::value;  // ke & 1
     real tu[4], ksu = 0, csu = 0;
+    uint32_t phu = 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const int o = c00 + (c >> 1) * PX + (c & 1);
-      tu[c] = sT[s_up][o];
-      ksu += sK[s_up][o];
-      csu += sC[s_up][o];
+      const V4<real> r = sN[PAR ^ 1][c00 + (c >> 1) * PX + (c & 1)];
+      tu[c] = r.x;
+      ksu += r.y;
+      csu += r.z;
+      if (c == 3) phu = real_bits(r.w);
     }
-    const uint8_t phu = sP[s_up][c00 + PX + 1];
-    store(ke + 2, s_nx);
+    store(ke + 2, PAR);
     fetch(ke + 3);
+
+    // inputs of node plane ke+1 (used by the next iteration's finalize)
+    real nRhs = 0, nBA = 0, nBB = 0, nAcc = 0, nMacc = 0, nF = 0, nC = 0;
+    {
+      const int pl = ke + 1;
+      if (out_col && pl < Z1) {
+        const int idn = nid0 + pl * nxy;
+        if (box_xy && pl >= a.box[4] && pl < a.box[5]) nRhs = a.rhs_box[box_off + (pl - a.box[4]) * box_pl];
+        if (bcm == 3 && (ring_xy || pl == 0)) {
+          nBA = a.bc_new[idn];
+          nBB = a.bc_old[idn];
+        }
+        if (hAcc) {
+          nAcc = a.accum[idn];
+          nMacc = a.max_accum[idn];
+        }
+        if (hF) nF = a.F_full[idn];
+        if (hCorr) nC = a.corr_full[idn];
+      }
+    }
 
     // ---- element (ex, ey, ke) ----
     real R[8];
@@ -296,7 +377,7 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
 #pragma unroll
       for (int m = 0; m < 8; ++m) R[m] *= a.lam[m] * kbar;
       bfly_inv(R);
-      if (a.surface && ke == top_el) {
+      if (hSurf && ke == top_el) {
         // top face: 2x2 Gauss points on the face of the upper corners
 #pragma unroll
         for (int qy = 0; qy < 2; ++qy)
@@ -325,16 +406,21 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
       cx[j] = R[1 + 2 * ay + 4 * az] + __shfl_down_sync(0xffffffffu, R[2 * ay + 4 * az], 1);
     }
     const real mx = me + __shfl_down_sync(0xffffffffu, me, 1);
-    const int xb = ke & 1;
-    sX[xb][0][ty][tx] = cx[0];  // ay=0, lower
-    sX[xb][1][ty][tx] = cx[2];  // ay=0, upper
-    sX[xb][2][ty][tx] = mx;
+    {
+      V4<real> w;
+      w.x = cx[0];  // ay=0, lower
+      w.y = cx[2];  // ay=0, upper
+      w.z = mx;
+      w.w = 0;
+      sX[PAR][ty][tx] = w;
+    }
     __syncthreads();
     real lowN = cx[1], upN = cx[3], mN = mx;
     if (ty + 1 < BY) {
-      lowN += sX[xb][0][ty + 1][tx];
-      upN += sX[xb][1][ty + 1][tx];
-      mN += sX[xb][2][ty + 1][tx];
+      const V4<real> n = sX[PAR][ty + 1][tx];
+      lowN += n.x;
+      upN += n.y;
+      mN += n.z;
     }
 
     // ---- finalize node plane ke ----
@@ -343,22 +429,22 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
       real Rt = -(carryU + lowN);
       const real M = carryM + mN;
       const real Told = tl[3];
-      const uint8_t phn = phl;
-      if (a.laser != nullptr) Rt += srcxy * sSz[ke - Z0];
-      if (box_xy && ke >= a.box[4] && ke < a.box[5]) Rt += a.rhs_box[box_off + (ke - a.box[4]) * box_pl];
-      if (a.F_full) Rt += a.F_full[id];
-      if (a.corr_full) Rt += a.corr_full[id];
+      const uint32_t phn = phl;
+      if (hLaser) Rt += srcxy * sSz[ke - Z0];
+      if (hBox) Rt += cRhs;
+      if (hF) Rt += cF;
+      if (hCorr) Rt += cC;
       real Tn = Told + fast_div(Rt, M);
-      if (a.inactive_amb && ke > a.ne_planes) Tn = P.T_amb;
-      if (a.bc_mode == 1) {
+      if (hInact && ke > a.ne_planes) Tn = P.T_amb;
+      if (bcm == 1) {
         if (iy == 0) Tn = a.face[2];
         if (iy == ny - 1) Tn = a.face[3];
         if (ix == 0) Tn = a.face[0];
         if (ix == nx - 1) Tn = a.face[1];
         if (ke == 0) Tn = a.face[4];
-      } else if (a.bc_mode == 3 && (ring_xy || ke == 0)) {
-        Tn = a.bc_alpha * a.bc_new[id] + a.bc_beta * a.bc_old[id];
-      } else if (a.bc_mode == 2 && (ring_xy || ke == 0)) {
+      } else if (bcm == 3) {
+        if (ring_xy || ke == 0) Tn = a.bc_alpha * cBA + a.bc_beta * cBB;
+      } else if (G && bcm == 2 && (ring_xy || ke == 0)) {
         real w8[8];
         const int b = map3_weights(a.bc_map, ix, iy, ke, w8);
         const int sx = 1, sy = a.bc_map.src_nx, sz = a.bc_map.src_nx * a.bc_map.src_ny;
@@ -371,16 +457,15 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
         }
         Tn = v;
       }
-      if (a.clamp) Tn = fmax(Tn, P.T_amb);
+      if (hClamp) Tn = fmax(Tn, P.T_amb);
       a.T_out[id] = Tn;
-      if (a.ph_out) a.ph_out[id] = phn;
-      if (a.accum) {
-        const bool prev2 = a.ph_in ? (a.ph_in[id] & PH_S2) != 0 : false;
+      if (hPhout) a.ph_out[id] = (uint8_t)(phn & 3u);
+      if (hAcc) {
+        const bool prev2 = (phn & 4u) != 0;
         const bool s2 = (phn & PH_S2) != 0;
-        const real acc = a.accum[id];
-        const real racc = (s2 && !prev2) ? acc : (real)0;
-        a.max_accum[id] = fmax(racc, a.max_accum[id]);
-        a.accum[id] = (acc + dt * (s2 ? (real)1 : (real)0)) - racc;
+        const real racc = (s2 && !prev2) ? cAcc : (real)0;
+        a.max_accum[id] = fmax(racc, cMacc);
+        a.accum[id] = (cAcc + dt * (s2 ? (real)1 : (real)0)) - racc;
       }
     }
     carryU = upN;
@@ -390,29 +475,37 @@ __global__ void __launch_bounds__(32 * BY, 3) level_step_kernel(const LevelK<rea
     ksl = ksu;
     csl = csu;
     phl = phu;
-    const int t = s_lo;  // rotate the ring: ke+1 -> lower, ke+2 -> upper
-    s_lo = s_up;
-    s_up = s_nx;
-    s_nx = t;
+    cRhs = nRhs;
+    cBA = nBA;
+    cBB = nBB;
+    cAcc = nAcc;
+    cMacc = nMacc;
+    cF = nF;
+    cC = nC;
+  };
+
+  for (int ke = Z0 - 1; ke < Z1; ke += 2) {
+    body(std::integral_constant<int, 1>(), ke);
+    if (ke + 1 < Z1) body(std::integral_constant<int, 0>(), ke + 1);
   }
 }
 
 // Node planes per CTA when the caller does not choose: minimise
 // (waves of CTAs) x (planes per CTA + 1 halo plane) for the resident CTA
-// slots of this GPU.
-template <typename real, int BY>
+// slots of this GPU.  Even, so that every chunk starts on an even plane.
+template <typename real, int BY, int FL>
 static int auto_zchunk(int tiles_xy, int nz) {
   static int slots = 0;
   if (slots == 0) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, level_step_kernel<real, BY>, 32 * BY, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, level_step_kernel<real, BY, FL>, 32 * BY, 0);
     slots = (sms > 0 ? sms : 152) * (per > 0 ? per : 1);
   }
-  int best = nz < ZMAX ? nz : ZMAX;
+  int best = ZMAX;
   long long best_cost = -1;
-  for (int zc = 2; zc <= ZMAX && zc <= nz; ++zc) {
+  for (int zc = 2; zc <= ZMAX; zc += 2) {
     const long long ctas = (long long)tiles_xy * cdiv(nz, zc);
     const long long waves = (ctas + slots - 1) / slots;
     const long long cost = waves * (zc + 1);
@@ -420,8 +513,39 @@ static int auto_zchunk(int tiles_xy, int nz) {
       best_cost = cost;
       best = zc;
     }
+    if (zc >= nz) break;
   }
   return best;
+}
+
+static int level_flags(const gm_level_args* g) {
+  int f = 0;
+  if (g->laser) f |= LF_LASER;
+  if (g->rhs_box) f |= LF_BOX;
+  if (g->F_full || g->corr_full) f |= LF_FULL;
+  if (g->k_arr) f |= LF_KARR;
+  if (g->accum) f |= LF_ACCUM;
+  if (g->surface) f |= LF_SURF;
+  if (g->clamp) f |= LF_CLAMP;
+  if (g->inactive_amb) f |= LF_INACT;
+  if (g->bc_mode == 1) f |= LF_BC1;
+  if (g->bc_mode == 2) f |= LF_BC2;
+  if (g->bc_mode == 3) f |= LF_BC3;
+  if (g->ph_in) f |= LF_PHIN;
+  if (g->ph_out) f |= LF_PHOUT;
+  return f;
+}
+
+template <typename real, int FL>
+static void launch_variant(const LevelK<real>& a, int gx, int gy, int zc_req, cudaStream_t st) {
+  constexpr int BY = 8;
+  int zc = zc_req > 0 ? zc_req : auto_zchunk<real, BY, FL>(gx * gy, a.nz);
+  zc += zc & 1;
+  if (zc > ZMAX) zc = ZMAX;
+  LevelK<real> b = a;
+  b.zchunk = zc;
+  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(32, BY);
+  level_step_kernel<real, BY, FL><<<grid, block, 0, st>>>(b);
 }
 
 template <typename real>
@@ -478,15 +602,23 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
 
-  constexpr int BY = 8;
-  const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, BY - 1);
-  int zc = g->zchunk;
-  if (zc <= 0) zc = auto_zchunk<real, BY>(gx * gy, a.nz);
-  if (zc > ZMAX) zc = ZMAX;
-  if (zc < 1) zc = 1;
-  a.zchunk = zc;
-  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(32, BY);
-  level_step_kernel<real, BY><<<grid, block, 0, st>>>(a);
+  const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, 7);
+  switch (level_flags(g)) {
+    case LF_L3:
+      launch_variant<real, LF_L3>(a, gx, gy, g->zchunk, st);
+      break;
+    case LF_L3ACC:
+      launch_variant<real, LF_L3ACC>(a, gx, gy, g->zchunk, st);
+      break;
+    case LF_L2:
+      launch_variant<real, LF_L2>(a, gx, gy, g->zchunk, st);
+      break;
+    case LF_L1:
+      launch_variant<real, LF_L1>(a, gx, gy, g->zchunk, st);
+      break;
+    default:
+      launch_variant<real, LF_GENERIC>(a, gx, gy, g->zchunk, st);
+  }
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
