@@ -85,6 +85,27 @@ __device__ __forceinline__ uint8_t node_props(const Props<real>& p, real T, uint
   return (uint8_t)((s1 ? PH_S1 : 0) | (s2 ? PH_S2 : 0));
 }
 
+// Phase and properties with selects (same values as node_props).  Returns the
+// new phase bits (bit0 S1, bit1 S2).
+template <typename real>
+__device__ __forceinline__ uint32_t node_props_sel(const Props<real>& p, real T, uint32_t ph_old, bool substrate,
+                                                   real& k, real& rc) {
+  const bool s2 = T >= p.T_liquidus;
+  const bool s3 = (T > p.T_solidus) && (T < p.T_liquidus);
+  const bool s1 = (ph_old & PH_S1) || s2 || substrate;
+  const real kb = p.k_bulk_a1 * T + p.k_bulk_a0;
+  const real cs = p.cp_solid_a1 * T + p.cp_solid_a0;
+  k = s2 ? p.k_fluid : (s1 ? kb : p.k_powder);
+  rc = p.rho * (s2 ? p.cp_fluid : (s3 ? p.cp_mushy : cs));
+  return (s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u);
+}
+
+// One staged node (or one exchanged corner sum) as a single 16/32-byte
+// shared-memory record.
+template <typename real>
+struct alignas(4 * sizeof(real)) V4 {
+  real x, y, z, w;
+};
 // Flux into the top surface at one Gauss point [W/mm^2]
 // (computeConvRadBC, go_melt/computeFunctions.py:2263-2290).
 template <typename real>

@@ -51,7 +51,6 @@ template <typename real>
 struct CoupleK {
   int fnx, fny;
   CoupleAxis<real> ax[3];
-  real ih[3];
   const real* T;
   const uint8_t* ph;
   long long substrate;
@@ -62,6 +61,7 @@ struct CoupleK {
   const real* dTb;
   const double* dt;
   real wq;
+  real cf[3];  // -2 wq / (H_d h_d): constant factor of the flux term along axis d
   real* partials;
   long long nitems;
   int nchunk;
@@ -75,14 +75,54 @@ __device__ __forceinline__ real warp_sum(real v) {
   return v;
 }
 
+// 2x2 Gauss-side transform of values d[b1][b2] given at the corners of a
+// face: out[q1][q2] = sum_b psi[b1][q1] psi[b2][q2] d[b1][b2], psi the 1-D
+// linear shape functions at the two Gauss points.
+template <typename real>
+__device__ __forceinline__ void psi2(const real d[2][2], real out[2][2]) {
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;
+  real u[2][2];  // u[q1][b2]
+#pragma unroll
+  for (int b2 = 0; b2 < 2; ++b2) {
+    u[0][b2] = PQ * d[0][b2] + MQ * d[1][b2];
+    u[1][b2] = MQ * d[0][b2] + PQ * d[1][b2];
+  }
+#pragma unroll
+  for (int q1 = 0; q1 < 2; ++q1) {
+    out[q1][0] = PQ * u[q1][0] + MQ * u[q1][1];
+    out[q1][1] = MQ * u[q1][0] + PQ * u[q1][1];
+  }
+}
+
+// Contraction with two 1-D coarse weight sets:
+// out[A1][A2] = sum_q phA[A1][q1] phB[A2][q2] G[q1][q2].
+template <typename real>
+__device__ __forceinline__ void contract2(const real phA[2][2], const real phB[2][2], const real G[2][2],
+                                          real out[2][2]) {
+  real v[2][2];  // v[A1][q2]
+#pragma unroll
+  for (int A1 = 0; A1 < 2; ++A1)
+#pragma unroll
+    for (int q2 = 0; q2 < 2; ++q2) v[A1][q2] = phA[A1][0] * G[0][q2] + phA[A1][1] * G[1][q2];
+#pragma unroll
+  for (int A1 = 0; A1 < 2; ++A1)
+#pragma unroll
+    for (int A2 = 0; A2 < 2; ++A2) out[A1][A2] = phB[A2][0] * v[A1][0] + phB[A2][1] * v[A1][1];
+}
+
+// One warp per item = (coarse element, fine sub-box of at most 4x4x4
+// elements).  The sub-box's nodes are staged once (T' or dT', k, rho*c) at
+// fixed strides 1, 5, 25; each lane then handles up to two fine elements.
+// All per-element products are sum-factorised along the axes.
 template <typename real>
 __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
-  __shared__ real sTp[4][SBN], sD[4][SBN], sK[4][SBN], sC[4][SBN];
+  constexpr int S1 = SB + 1, S2 = S1 * S1;
+  __shared__ V4<real> sR[4][SBN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;
-  const real psi[2][2] = {{PQ, MQ}, {MQ, PQ}};  // psi[a][q]
   const bool flux = a.Tp != nullptr, mass = a.dTa != nullptr;
   const real wdt = mass ? a.wq / (real)(*a.dt) : (real)0;
+  const int fnxy = a.fnx * a.fny;
   const long long nw = (long long)gridDim.x * 4;
   for (long long item = blockIdx.x * 4LL + warp; item < a.nitems; item += nw) {
     const int chunk = (int)(item % a.nchunk);
@@ -101,27 +141,32 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[i] = 0;
     if (nbx > 0 && nby > 0 && nbz > 0) {
-      const int mx = nbx + 1, my = nby + 1, mz = nbz + 1;
-      for (int i = lane; i < mx * my * mz; i += 32) {
-        const int lx = i % mx, ly = (i / mx) % my, lz = i / (mx * my);
-        const long long id = (e0x + lx) + (long long)(e0y + ly) * a.fnx + (long long)(e0z + lz) * a.fnx * a.fny;
-        real k, c;
-        const real T = a.T[id];
-        node_props(a.p, T, a.ph ? a.ph[id] : (uint8_t)0, id < a.substrate, k, c);
-        if (a.k_arr) {
-          k = a.k_arr[id];
-          c = a.rc_arr[id];
+      for (int i = lane; i < SBN; i += 32) {
+        const int lx = i % S1, ly = (i / S1) % S1, lz = i / S2;
+        if (lx <= nbx && ly <= nby && lz <= nbz) {
+          const int id = (e0x + lx) + (e0y + ly) * a.fnx + (e0z + lz) * fnxy;
+          real k, c;
+          node_props_sel(a.p, a.T[id], a.ph ? (uint32_t)a.ph[id] : 0u, id < a.substrate, k, c);
+          if (a.k_arr) {
+            k = a.k_arr[id];
+            c = a.rc_arr[id];
+          }
+          V4<real> r;
+          r.x = flux ? a.Tp[id] : (real)0;
+          r.y = mass ? a.dTa[id] - a.dTb[id] : (real)0;
+          r.z = k;
+          r.w = c;
+          sR[warp][i] = r;
         }
-        sK[warp][i] = k;
-        sC[warp][i] = c;
-        if (flux) sTp[warp][i] = a.Tp[id];
-        if (mass) sD[warp][i] = a.dTa[id] - a.dTb[id];
       }
       __syncwarp();
-      for (int f = lane; f < nbx * nby * nbz; f += 32) {
-        const int fx = f % nbx, fy = (f / nbx) % nby, fz = f / (nbx * nby);
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {
+        const int f = lane + 32 * rr;
+        const int fx = f & 3, fy = (f >> 2) & 3, fz = f >> 4;
+        if (fx >= nbx || fy >= nby || fz >= nbz) continue;
         const int ex = e0x + fx, ey = e0y + fy, ez = e0z + fz;
-        real ph[3][2][2];  // ph[d][A][s]
+        real ph[3][2][2];  // ph[d][A][s]: 1-D coarse weight of local coarse node A at Gauss side s
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
           ph[0][0][s] = a.ax[0].cw[(ex * 2 + s) * 2 + 0];
@@ -131,58 +176,45 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
           ph[2][0][s] = a.ax[2].cw[(ez * 2 + s) * 2 + 0];
           ph[2][1][s] = a.ax[2].cw[(ez * 2 + s) * 2 + 1];
         }
-        int cid[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) cid[c] = (fx + (c & 1)) + (fy + ((c >> 1) & 1)) * mx + (fz + (c >> 2)) * mx * my;
-        real ks = 0, cs = 0;
+        const int base = fx + S1 * fy + S2 * fz;
+        real t[8], dd[8], ks = 0, cs = 0;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-          ks += sK[warp][cid[c]];
-          cs += sC[warp][cid[c]];
+          const V4<real> r = sR[warp][base + (c & 1) + S1 * ((c >> 1) & 1) + S2 * (c >> 2)];
+          t[c] = r.x;
+          dd[c] = r.y;
+          ks += r.z;
+          cs += r.w;
         }
         if (flux) {
           const real kb = ks * (real)0.125;
-          real t[8];
+          // corner differences along each axis, indexed by the other two corner bits
+          real dX[2][2], dY[2][2], dZ[2][2];
 #pragma unroll
-          for (int c = 0; c < 8; ++c) t[c] = sTp[warp][cid[c]];
-          // gradients at the Gauss points: G_x depends on (qy,qz) only, etc.
-          real Gx[2][2], Gy[2][2], Gz[2][2];
+          for (int b1 = 0; b1 < 2; ++b1)
 #pragma unroll
-          for (int q1 = 0; q1 < 2; ++q1)
-#pragma unroll
-            for (int q2 = 0; q2 < 2; ++q2) {
-              real gx = 0, gy = 0, gz = 0;
-#pragma unroll
-              for (int b1 = 0; b1 < 2; ++b1)
-#pragma unroll
-                for (int b2 = 0; b2 < 2; ++b2) {
-                  const real w = psi[b1][q1] * psi[b2][q2];
-                  gx += w * (t[1 + 2 * b1 + 4 * b2] - t[2 * b1 + 4 * b2]);  // (ay,az)=(b1,b2)
-                  gy += w * (t[b1 + 2 + 4 * b2] - t[b1 + 4 * b2]);          // (ax,az)
-                  gz += w * (t[b1 + 2 * b2 + 4] - t[b1 + 2 * b2]);          // (ax,ay)
-                }
-              Gx[q1][q2] = kb * a.ih[0] * gx;
-              Gy[q1][q2] = kb * a.ih[1] * gy;
-              Gz[q1][q2] = kb * a.ih[2] * gz;
+            for (int b2 = 0; b2 < 2; ++b2) {
+              dX[b1][b2] = t[1 + 2 * b1 + 4 * b2] - t[2 * b1 + 4 * b2];  // (ay, az)
+              dY[b1][b2] = t[b1 + 2 + 4 * b2] - t[b1 + 4 * b2];          // (ax, az)
+              dZ[b1][b2] = t[b1 + 2 * b2 + 4] - t[b1 + 2 * b2];          // (ax, ay)
             }
-          // contraction with the coarse gradients (factor 2: the term does not
-          // depend on the Gauss side along its own axis)
+          // gradients at the Gauss points (G_x depends on (qy, qz) only, etc.)
+          real Gx[2][2], Gy[2][2], Gz[2][2];
+          psi2(dX, Gx);
+          psi2(dY, Gy);
+          psi2(dZ, Gz);
+          // contraction with the coarse gradients (the factor 2 of the Gauss
+          // side along the term's own axis is in cf)
+          real X[2][2], Y[2][2], Z[2][2];
+          contract2(ph[1], ph[2], Gx, X);
+          contract2(ph[0], ph[2], Gy, Y);
+          contract2(ph[0], ph[1], Gz, Z);
+          const real sx = kb * a.cf[0], sy = kb * a.cf[1], sz = kb * a.cf[2];
 #pragma unroll
           for (int A1 = 0; A1 < 2; ++A1)
 #pragma unroll
             for (int A2 = 0; A2 < 2; ++A2) {
-              real X = 0, Y = 0, Z = 0;
-#pragma unroll
-              for (int q1 = 0; q1 < 2; ++q1)
-#pragma unroll
-                for (int q2 = 0; q2 < 2; ++q2) {
-                  X += ph[1][A1][q1] * ph[2][A2][q2] * Gx[q1][q2];
-                  Y += ph[0][A1][q1] * ph[2][A2][q2] * Gy[q1][q2];
-                  Z += ph[0][A1][q1] * ph[1][A2][q2] * Gz[q1][q2];
-                }
-              const real fX = (real)-2 * a.wq * a.ax[0].invH * X;
-              const real fY = (real)-2 * a.wq * a.ax[1].invH * Y;
-              const real fZ = (real)-2 * a.wq * a.ax[2].invH * Z;
+              const real fX = sx * X[A1][A2], fY = sy * Y[A1][A2], fZ = sz * Z[A1][A2];
               // X -> nodes (Ax, A1=Ay, A2=Az); Y -> (A1=Ax, Ay, A2=Az); Z -> (A1=Ax, A2=Ay, Az)
               acc[1 + 2 * A1 + 4 * A2] += fX;
               acc[0 + 2 * A1 + 4 * A2] -= fX;
@@ -194,26 +226,46 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
         }
         if (mass) {
           const real cb = cs * (real)0.125;
-          real d[8];
-#pragma unroll
-          for (int c = 0; c < 8; ++c) d[c] = sD[warp][cid[c]];
-          // trilinear values at the 8 Gauss points, then the coarse N contraction
+          // trilinear values at the 8 Gauss points: one 1-D psi transform per axis
           real m[8];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const int qx = q & 1, qy = (q >> 1) & 1, qz = q >> 2;
-            real v = 0;
-#pragma unroll
-            for (int c = 0; c < 8; ++c) v += psi[c & 1][qx] * psi[(c >> 1) & 1][qy] * psi[c >> 2][qz] * d[c];
-            m[q] = cb * v;
+          for (int j = 0; j < 4; ++j) {  // x: pairs (c, c+1)
+            const real d0 = dd[2 * j], d1 = dd[2 * j + 1];
+            m[2 * j] = PQ * d0 + MQ * d1;
+            m[2 * j + 1] = MQ * d0 + PQ * d1;
           }
 #pragma unroll
-          for (int A = 0; A < 8; ++A) {
-            const int Ax = A & 1, Ay = (A >> 1) & 1, Az = A >> 2;
-            real v = 0;
+          for (int j = 0; j < 4; ++j) {  // y: pairs (c, c+2)
+            const int c0 = (j & 1) + 4 * (j >> 1);
+            const real d0 = m[c0], d1 = m[c0 + 2];
+            m[c0] = PQ * d0 + MQ * d1;
+            m[c0 + 2] = MQ * d0 + PQ * d1;
+          }
 #pragma unroll
-            for (int q = 0; q < 8; ++q) v += ph[0][Ax][q & 1] * ph[1][Ay][(q >> 1) & 1] * ph[2][Az][q >> 2] * m[q];
-            acc[A] -= wdt * v;
+          for (int j = 0; j < 4; ++j) {  // z: pairs (c, c+4)
+            const real d0 = m[j], d1 = m[j + 4];
+            m[j] = cb * (PQ * d0 + MQ * d1);
+            m[j + 4] = cb * (MQ * d0 + PQ * d1);
+          }
+          // contraction with the coarse shape functions, one axis at a time
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {  // x
+            const real q0 = m[2 * j], q1 = m[2 * j + 1];
+            m[2 * j] = ph[0][0][0] * q0 + ph[0][0][1] * q1;
+            m[2 * j + 1] = ph[0][1][0] * q0 + ph[0][1][1] * q1;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {  // y
+            const int c0 = (j & 1) + 4 * (j >> 1);
+            const real q0 = m[c0], q1 = m[c0 + 2];
+            m[c0] = ph[1][0][0] * q0 + ph[1][0][1] * q1;
+            m[c0 + 2] = ph[1][1][0] * q0 + ph[1][1][1] * q1;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {  // z
+            const real q0 = m[j], q1 = m[j + 4];
+            acc[j] -= wdt * (ph[2][0][0] * q0 + ph[2][0][1] * q1);
+            acc[j + 4] -= wdt * (ph[2][1][0] * q0 + ph[2][1][1] * q1);
           }
         }
       }
@@ -229,31 +281,36 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
 }
 
 // Sum the partials onto the coarse nodes of the box and add them into an
-// output array covering the node box [ob0, ob0+on) per axis.
+// output array covering the node box [ob0, ob0+on) per axis.  One thread per
+// coarse node when every coarse element has one partial set; one warp per
+// coarse node when the partial sets of a coarse element are many.
 template <typename real>
 __global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, int lo0, int lo1, int lo2,
                                      const real* partials, real* out, int ob0, int ob1, int ob2, int on0, int on1,
                                      real scale) {
   const long long tot = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-       t += (long long)gridDim.x * blockDim.x) {
+  const bool per_warp = nchunk > 1;
+  const int lane = threadIdx.x & 31;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long first = per_warp ? t0 >> 5 : t0;
+  const long long stride = per_warp ? ((long long)gridDim.x * blockDim.x) >> 5 : (long long)gridDim.x * blockDim.x;
+  for (long long t = first; t < tot; t += stride) {
     const int bx = (int)(t % (ncbx + 1)), by = (int)((t / (ncbx + 1)) % (ncby + 1)),
               bz = (int)(t / ((long long)(ncbx + 1) * (ncby + 1)));
     real s = 0;
-    for (int cz = bz - 1; cz <= bz; ++cz) {
-      if (cz < 0 || cz >= ncbz) continue;
-      for (int cy = by - 1; cy <= by; ++cy) {
-        if (cy < 0 || cy >= ncby) continue;
-        for (int cx = bx - 1; cx <= bx; ++cx) {
-          if (cx < 0 || cx >= ncbx) continue;
-          const int A = (bx - cx) + 2 * (by - cy) + 4 * (bz - cz);
-          const long long base = (((long long)cz * ncby + cy) * ncbx + cx) * nchunk;
-          for (int c = 0; c < nchunk; ++c) s += partials[(base + c) * 8 + A];
-        }
-      }
+    const int j0 = per_warp ? lane : 0, js = per_warp ? 32 : 1;
+    for (int j = j0; j < 8 * nchunk; j += js) {
+      const int A = j / nchunk, c = j - A * nchunk;  // local node A of the neighbouring coarse element
+      const int cx = bx - (A & 1), cy = by - ((A >> 1) & 1), cz = bz - (A >> 2);
+      if (cx < 0 || cx >= ncbx || cy < 0 || cy >= ncby || cz < 0 || cz >= ncbz) continue;
+      const long long base = (((long long)cz * ncby + cy) * ncbx + cx) * nchunk;
+      s += partials[(base + c) * 8 + A];
     }
-    const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
-    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * s;
+    if (per_warp) s = warp_sum(s);
+    if (!per_warp || lane == 0) {
+      const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
+      out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * s;
+    }
   }
 }
 
@@ -369,7 +426,6 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
   fill_axes<real>(&g->geom, a.ax, &a.nchunk);
   a.fnx = g->fine_nodes[0];
   a.fny = g->fine_nodes[1];
-  for (int d = 0; d < 3; ++d) a.ih[d] = (real)(1.0 / g->fine_h[d]);
   a.T = (const real*)g->T;
   a.ph = g->ph;
   a.substrate = g->substrate;
@@ -380,6 +436,8 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
   a.dTb = (const real*)g->dTb;
   a.dt = g->dt;
   a.wq = (real)(g->fine_h[0] * g->fine_h[1] * g->fine_h[2] / 8.0);
+  for (int d = 0; d < 3; ++d)
+    a.cf[d] = (real)(-2.0 * (g->fine_h[0] * g->fine_h[1] * g->fine_h[2] / 8.0) / (g->geom.ax[d].H * g->fine_h[d]));
   a.partials = (real*)g->partials;
   a.nitems = (long long)a.ax[0].ncb * a.ax[1].ncb * a.ax[2].ncb * a.nchunk;
   a.p = make_props<real>(*pr);
@@ -389,7 +447,7 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
   if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
   const int ncbx = a.ax[0].ncb, ncby = a.ax[1].ncb, ncbz = a.ax[2].ncb;
   const long long nodes = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
-  couple_gather_kernel<real><<<grid1(nodes), 256, 0, st>>>(
+  couple_gather_kernel<real><<<grid1(a.nchunk > 1 ? nodes * 32 : nodes), 256, 0, st>>>(
       ncbx, ncby, ncbz, a.nchunk, g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, a.partials,
       (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1], (real)g->scale);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
@@ -408,6 +466,7 @@ extern "C" int gm_couple(const gm_couple_args* g, const gm_props* p, void* strea
   if ((g->dTa == nullptr) != (g->dTb == nullptr) || (g->dTa && !g->dt)) return GM_ERR_ARG;
   if ((g->k_arr == nullptr) != (g->rc_arr == nullptr)) return GM_ERR_ARG;
   if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
+  if ((long long)g->fine_nodes[0] * g->fine_nodes[1] * g->fine_nodes[2] >= (1LL << 31)) return GM_ERR_TOO_LARGE;
   const long long need = gm_couple_partials_size(&g->geom);
   if (need < 0 || need > g->partials_cap) return GM_ERR_TOO_LARGE;
   cudaStream_t st = (cudaStream_t)stream;

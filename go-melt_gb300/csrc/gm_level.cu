@@ -13,12 +13,13 @@
 // 8-point Hadamard basis of the element's corner values, so K_ref*T_e is a
 // forward butterfly, 7 scalings and a backward butterfly.
 //
-// Thread mapping: a CTA of 32 x BY threads owns a 32 x BY tile of element
-// columns and marches up a range of node planes.  Node planes are staged in a
-// 3-deep shared-memory ring (T, k, rho*c, new phase).  Element corner
-// contributions are combined onto nodes without atomics: x-neighbours by warp
-// shuffle, y-neighbours through shared memory, z-neighbours by a register
-// carry from one plane to the next.  Each CTA writes 31 x (BY-1) node columns.
+// Thread mapping: a CTA of TX x BY threads (a tile row is a warp or a
+// half-warp) owns a TX x BY tile of element columns and marches up a range of
+// node planes.  Node planes are staged in two shared-memory slots (T, k,
+// rho*c, phase bits).  Element corner contributions are combined onto nodes
+// without atomics: x-neighbours by shuffle, y-neighbours through shared
+// memory, z-neighbours by a register carry from one plane to the next.  Each
+// CTA writes (TX-1) x (BY-1) node columns.
 #include <math.h>
 
 #include <type_traits>
@@ -92,6 +93,27 @@ __device__ __forceinline__ void bfly_inv(real v[8]) {
   }
 }
 
+// x/y butterfly of one face (4 corner values, index x + 2y): the first two
+// stages of bfly_fwd, which act on each face separately.
+template <typename real>
+__device__ __forceinline__ void face_fwd(real v[4]) {
+  real a = v[0], b = v[1];
+  v[0] = a + b;
+  v[1] = b - a;
+  a = v[2];
+  b = v[3];
+  v[2] = a + b;
+  v[3] = b - a;
+  a = v[0];
+  b = v[2];
+  v[0] = a + b;
+  v[2] = b - a;
+  a = v[1];
+  b = v[3];
+  v[1] = a + b;
+  v[3] = b - a;
+}
+
 // 1-D source factor of node i: sum over the (up to two) elements touching the
 // node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
 // rel = origin - v (formed in double by the caller), so the Gauss-point
@@ -122,27 +144,6 @@ __device__ __forceinline__ float fast_div<float>(float a, float b) {
   return __fdividef(a, b);
 }
 
-// Phase and properties with selects (same values as node_props).  Returns the
-// new phase bits (bit0 S1, bit1 S2).
-template <typename real>
-__device__ __forceinline__ uint32_t node_props_sel(const Props<real>& p, real T, uint32_t ph_old, bool substrate,
-                                                   real& k, real& rc) {
-  const bool s2 = T >= p.T_liquidus;
-  const bool s3 = (T > p.T_solidus) && (T < p.T_liquidus);
-  const bool s1 = (ph_old & PH_S1) || s2 || substrate;
-  const real kb = p.k_bulk_a1 * T + p.k_bulk_a0;
-  const real cs = p.cp_solid_a1 * T + p.cp_solid_a0;
-  k = s2 ? p.k_fluid : (s1 ? kb : p.k_powder);
-  rc = p.rho * (s2 ? p.cp_fluid : (s3 ? p.cp_mushy : cs));
-  return (s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u);
-}
-
-// One staged node (or one exchanged corner sum) as a single 16/32-byte
-// shared-memory record.
-template <typename real>
-struct alignas(4 * sizeof(real)) V4 {
-  real x, y, z, w;
-};
 __device__ __forceinline__ float bits_as_real(uint32_t u, float) { return __uint_as_float(u); }
 __device__ __forceinline__ double bits_as_real(uint32_t u, double) { return __longlong_as_double((long long)u); }
 __device__ __forceinline__ uint32_t real_bits(float r) { return __float_as_uint(r); }
@@ -184,10 +185,11 @@ constexpr int LF_L1 = LF_BOX | LF_SURF | LF_CLAMP | LF_INACT | LF_BC1 | LF_PHIN 
 //   memory in y), passes the barrier and finalizes node plane ke.  Lower-plane
 //   corner values are carried in registers.  Staged phase bits: bit0/1 the
 //   new S1/S2, bit2 the old S2 (melt-time reset).
-template <typename real, int BY, int FL>
-__global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
+template <typename real, int TX, int BY, int FL>
+__global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
   constexpr bool G = (FL & LF_GENERIC) != 0;
-  constexpr int TX = 32, PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
+  constexpr int PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
+  static_assert(TX == 16 || TX == 32, "a tile row is a warp or a half-warp");
   constexpr int NSLOT = (NP + NT - 1) / NT;
   static_assert(NT <= NP, "slot 0 covers every thread");
   __shared__ V4<real> sN[2][NP];
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int nxy = nx * ny;
   const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
-  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);  // zchunk is even: Z0 is even
+  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
   const int subs = a.substrate > (long long)nxy * nz ? nxy * nz : (int)a.substrate;
   const real dt = (real)(*a.dt);
   const real inv_dt = (real)1 / dt;
@@ -269,11 +271,11 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
     }
   };
 
-  // ---- prologue: planes Z0-1 (slot 1), Z0 (slot 0) staged, plane Z0+1 in registers ----
+  // ---- prologue: planes Z0-1 (slot 0), Z0 (slot 1) staged, plane Z0+1 in registers ----
   fetch(Z0 - 1);
-  store(Z0 - 1, 1);
+  store(Z0 - 1, 0);
   fetch(Z0);
-  store(Z0, 0);
+  store(Z0, 1);
   fetch(Z0 + 1);
   real srcP = 0;
   if (hLaser) {
@@ -309,25 +311,28 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
   const int box_pl = (a.box[1] - a.box[0]) * (a.box[3] - a.box[2]);
   const real srcxy = (hLaser && out_col) ? srcP * sSx[tx + 1] * sSy[ty + 1] : (real)0;
 
-  // carried lower-plane corners (plane Z0-1, slot 1)
-  real tl[4], ksl = 0, csl = 0;
+  // carried lower face of the element plane (plane Z0-1, slot 0): its x/y
+  // butterfly modes fl, the output node's temperature, sums of k and rho*c
+  real fl[4], tl3, ksl = 0, csl = 0;
   uint32_t phl = 0;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const V4<real> r = sN[1][c00 + (c >> 1) * PX + (c & 1)];
-    tl[c] = r.x;
+    const V4<real> r = sN[0][c00 + (c >> 1) * PX + (c & 1)];
+    fl[c] = r.x;
     ksl += r.y;
     csl += r.z;
     if (c == 3) phl = real_bits(r.w);
   }
-  __syncthreads();  // slot 1 is restaged in the first iteration
+  tl3 = fl[3];
+  face_fwd(fl);
+  __syncthreads();  // slot 0 is restaged in the first iteration
 
   // per-node inputs of the node plane finalized next (loaded one iteration ahead)
   real cRhs = 0, cBA = 0, cBB = 0, cAcc = 0, cMacc = 0, cF = 0, cC = 0;
   real carryU = 0, carryM = 0;
 
   auto body = [&](auto par, int ke) {
-    constexpr int PAR = decltype(par)::value;  // ke & 1
+    constexpr int PAR = decltype(par)::value;  // (ke - Z0 + 1) & 1: plane p lives in slot (p - Z0 + 1) & 1
     real tu[4], ksu = 0, csu = 0;
     uint32_t phu = 0;
 #pragma unroll
@@ -362,20 +367,25 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
     }
 
     // ---- element (ex, ey, ke) ----
+    real fu[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) fu[c] = tu[c];
+    face_fwd(fu);
     real R[8];
     real me = 0;
     const bool el_ok = col_ok && ke >= 0 && ke < a.ne_planes;
     if (el_ok) {
+      // Hadamard modes: z butterfly of the two faces' x/y modes; mode 0 (the
+      // constant) has eigenvalue 0
+      R[0] = 0;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        R[c] = tl[c];
-        R[4 + c] = tu[c];
-      }
+      for (int c = 1; c < 4; ++c) R[c] = fl[c] + fu[c];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) R[4 + c] = fu[c] - fl[c];
       const real kbar = (ksl + ksu) * (real)0.125;
       me = a.wvol * ((csl + csu) * (real)0.125) * inv_dt;
-      bfly_fwd(R);
 #pragma unroll
-      for (int m = 0; m < 8; ++m) R[m] *= a.lam[m] * kbar;
+      for (int m = 1; m < 8; ++m) R[m] *= a.lam[m] * kbar;
       bfly_inv(R);
       if (hSurf && ke == top_el) {
         // top face: 2x2 Gauss points on the face of the upper corners
@@ -403,9 +413,9 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int ay = j & 1, az = j >> 1;
-      cx[j] = R[1 + 2 * ay + 4 * az] + __shfl_down_sync(0xffffffffu, R[2 * ay + 4 * az], 1);
+      cx[j] = R[1 + 2 * ay + 4 * az] + __shfl_down_sync(0xffffffffu, R[2 * ay + 4 * az], 1, TX);
     }
-    const real mx = me + __shfl_down_sync(0xffffffffu, me, 1);
+    const real mx = me + __shfl_down_sync(0xffffffffu, me, 1, TX);
     {
       V4<real> w;
       w.x = cx[0];  // ay=0, lower
@@ -428,7 +438,7 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
       const int id = nid0 + ke * nxy;
       real Rt = -(carryU + lowN);
       const real M = carryM + mN;
-      const real Told = tl[3];
+      const real Told = tl3;
       const uint32_t phn = phl;
       if (hLaser) Rt += srcxy * sSz[ke - Z0];
       if (hBox) Rt += cRhs;
@@ -471,7 +481,8 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
     carryU = upN;
     carryM = mN;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) tl[c] = tu[c];
+    for (int c = 0; c < 4; ++c) fl[c] = fu[c];
+    tl3 = tu[3];
     ksl = ksu;
     csl = csu;
     phl = phu;
@@ -485,35 +496,47 @@ __global__ void __launch_bounds__(32 * BY, sizeof(real) == 4 ? 3 : 2) level_step
   };
 
   for (int ke = Z0 - 1; ke < Z1; ke += 2) {
-    body(std::integral_constant<int, 1>(), ke);
-    if (ke + 1 < Z1) body(std::integral_constant<int, 0>(), ke + 1);
+    body(std::integral_constant<int, 0>(), ke);
+    if (ke + 1 < Z1) body(std::integral_constant<int, 1>(), ke + 1);
   }
 }
 
-// Node planes per CTA when the caller does not choose: minimise
-// (waves of CTAs) x (planes per CTA + 1 halo plane) for the resident CTA
-// slots of this GPU.  Even, so that every chunk starts on an even plane.
-template <typename real, int BY, int FL>
+// Tile of one CTA: 16 x 16 element columns (15 x 15 output node columns).
+constexpr int LT_X = 16, LT_Y = 16;
+
+// Node planes per CTA when the caller does not choose.  The kernel is bound
+// by instruction issue, so the time of a launch follows the busiest SM:
+// (CTAs per SM) x (planes per CTA + 1 halo plane), divided by an issue
+// efficiency that drops when fewer than three CTAs share an SM.  Among equal
+// costs the smallest total work wins.
+template <typename real, int TX, int BY, int FL>
 static int auto_zchunk(int tiles_xy, int nz) {
-  static int slots = 0;
-  if (slots == 0) {
-    int dev = 0, sms = 0, per = 0;
+  static int sms = 0, per = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0, p = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, level_step_kernel<real, BY, FL>, 32 * BY, 0);
-    slots = (sms > 0 ? sms : 152) * (per > 0 ? per : 1);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, level_step_kernel<real, TX, BY, FL>, TX * BY, 0);
+    per = p > 0 ? p : 1;
+    sms = n > 0 ? n : 152;
   }
-  int best = ZMAX;
-  long long best_cost = -1;
-  for (int zc = 2; zc <= ZMAX; zc += 2) {
-    const long long ctas = (long long)tiles_xy * cdiv(nz, zc);
-    const long long waves = (ctas + slots - 1) / slots;
-    const long long cost = waves * (zc + 1);
-    if (best_cost < 0 || cost < best_cost) {
+  static const double eff[4] = {1.0, 0.55, 0.85, 1.0};
+  int best = nz < ZMAX ? nz : ZMAX;
+  double best_cost = -1;
+  long long best_total = 0;
+  for (int nch = cdiv(nz, ZMAX); nch <= nz; ++nch) {
+    const int zc = cdiv(nz, nch);
+    if (cdiv(nz, zc) != nch) continue;  // the same split as a smaller chunk count
+    const long long ctas = (long long)tiles_xy * nch;
+    const long long per_sm = (ctas + sms - 1) / sms;
+    const long long res = per_sm < per ? per_sm : per;
+    const double cost = (double)(per_sm * (zc + 1)) / eff[res < 3 ? res : 3];
+    const long long total = ctas * (zc + 1);
+    if (best_cost < 0 || cost < best_cost - 1e-9 || (cost < best_cost + 1e-9 && total < best_total)) {
       best_cost = cost;
+      best_total = total;
       best = zc;
     }
-    if (zc >= nz) break;
   }
   return best;
 }
@@ -537,15 +560,14 @@ static int level_flags(const gm_level_args* g) {
 }
 
 template <typename real, int FL>
-static void launch_variant(const LevelK<real>& a, int gx, int gy, int zc_req, cudaStream_t st) {
-  constexpr int BY = 8;
-  int zc = zc_req > 0 ? zc_req : auto_zchunk<real, BY, FL>(gx * gy, a.nz);
-  zc += zc & 1;
+static void launch_variant(const LevelK<real>& a, int zc_req, cudaStream_t st) {
+  const int gx = cdiv(a.nx, LT_X - 1), gy = cdiv(a.ny, LT_Y - 1);
+  int zc = zc_req > 0 ? zc_req : auto_zchunk<real, LT_X, LT_Y, FL>(gx * gy, a.nz);
   if (zc > ZMAX) zc = ZMAX;
   LevelK<real> b = a;
   b.zchunk = zc;
-  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(32, BY);
-  level_step_kernel<real, BY, FL><<<grid, block, 0, st>>>(b);
+  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(LT_X, LT_Y);
+  level_step_kernel<real, LT_X, LT_Y, FL><<<grid, block, 0, st>>>(b);
 }
 
 template <typename real>
@@ -602,22 +624,21 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
 
-  const int gx = cdiv(a.nx, 31), gy = cdiv(a.ny, 7);
   switch (level_flags(g)) {
     case LF_L3:
-      launch_variant<real, LF_L3>(a, gx, gy, g->zchunk, st);
+      launch_variant<real, LF_L3>(a, g->zchunk, st);
       break;
     case LF_L3ACC:
-      launch_variant<real, LF_L3ACC>(a, gx, gy, g->zchunk, st);
+      launch_variant<real, LF_L3ACC>(a, g->zchunk, st);
       break;
     case LF_L2:
-      launch_variant<real, LF_L2>(a, gx, gy, g->zchunk, st);
+      launch_variant<real, LF_L2>(a, g->zchunk, st);
       break;
     case LF_L1:
-      launch_variant<real, LF_L1>(a, gx, gy, g->zchunk, st);
+      launch_variant<real, LF_L1>(a, g->zchunk, st);
       break;
     default:
-      launch_variant<real, LF_GENERIC>(a, gx, gy, g->zchunk, st);
+      launch_variant<real, LF_GENERIC>(a, g->zchunk, st);
   }
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }

@@ -23,7 +23,7 @@ import torch
 
 import _native as N
 import kern
-from geometry import axis_map, quad_points_1d
+from geometry import axis_map, couple_axis
 from levels import Geometry
 
 PH_S1, PH_S2 = 1, 2
@@ -98,33 +98,31 @@ class CoupleGeom:
         self.axes = []
         g = N.gm_couple_geom()
         for d in range(3):
-            xq = quad_points_1d(fine_coords[d])
-            c = np.asarray(coarse_coords[d], dtype=np.float64)
-            H = c[1] - c[0]
-            nce = c.size - 1
-            I = np.clip(np.floor((xq - c[0]) / H).astype(np.int64), 0, nce - 1)
-            cw = np.stack([(c[I + 1] - xq) / H, (xq - c[I]) / H], axis=-1)  # (nfe, 2, 2)
-            node0 = I[:, 0]
-            lo = int(node0.min())
-            ncb = int(node0.max()) - lo + 1
-            cells = lo + np.arange(ncb)
-            flo = np.searchsorted(node0, cells, side="left")
-            fhi = np.searchsorted(node0, cells, side="right")
+            r = couple_axis(fine_coords[d], coarse_coords[d])
             a = g.ax[d]
-            a.nfe = xq.shape[0]
-            a.cw = arena.put(cw.reshape(-1), np_dtype)
-            a.node0 = C.cast(arena.put(node0, np.int32), C.POINTER(C.c_int))
-            a.cb_lo = lo
-            a.ncb = ncb
-            a.flo = C.cast(arena.put(flo, np.int32), C.POINTER(C.c_int))
-            a.fhi = C.cast(arena.put(fhi, np.int32), C.POINTER(C.c_int))
-            a.rmax = int((fhi - flo).max())
-            a.H = float(H)
-            self.axes.append(dict(lo=lo, ncb=ncb, xq=arena.put(xq.reshape(-1), np.float64)))
+            a.nfe = r["xq"].shape[0]
+            a.cw = arena.put(r["cw"].reshape(-1), np_dtype)
+            a.node0 = C.cast(arena.put(r["node0"]), C.POINTER(C.c_int))
+            a.cb_lo = r["lo"]
+            a.ncb = r["ncb"]
+            a.flo = C.cast(arena.put(r["flo"]), C.POINTER(C.c_int))
+            a.fhi = C.cast(arena.put(r["fhi"]), C.POINTER(C.c_int))
+            a.rmax = r["rmax"]
+            a.H = r["H"]
+            self.axes.append(dict(lo=r["lo"], ncb=r["ncb"], xq=arena.put(r["xq"].reshape(-1))))
         self.struct = g
         self.box_lo = [ax["lo"] for ax in self.axes]
         self.box_n = [ax["ncb"] + 1 for ax in self.axes]
         self.partials = int(N.lib().gm_couple_partials_size(C.byref(g)))
+
+
+class MovePlan:
+    """Host half of one window move (see Engine.plan_move)."""
+
+    __slots__ = ("v", "move_v", "m3", "m2", "tables", "table_bytes")
+
+    def __init__(self, v, move_v, m3, m2, tables, table_bytes):
+        self.v, self.move_v, self.m3, self.m2, self.tables, self.table_bytes = v, move_v, m3, m2, tables, table_bytes
 
 
 class Engine:
@@ -147,6 +145,8 @@ class Engine:
         self.acc3 = torch.zeros(g.L[3].nn, **f)
         self.macc3 = torch.zeros(g.L[3].nn, **f)
         self.s2_prev_lo = None  # Level-0 start of the window last written (S2 snapshot)
+        self._pending = None  # MovePlan made by plan_move and not yet applied
+        self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
         self.tmp = None
         self._work = None
@@ -202,7 +202,7 @@ class Engine:
     # ------------------------------------------------------------------
     # per-window tables (rebuilt after every move)
     # ------------------------------------------------------------------
-    def build_tables(self):
+    def build_tables(self, assign=True):
         own = not self.arena.open
         if own:
             self.arena.begin()
@@ -224,7 +224,8 @@ class Engine:
         for d in range(3):
             if c31.box_lo[d] < c21.box_lo[d] or c31.box_lo[d] + c31.box_n[d] > c21.box_lo[d] + c21.box_n[d]:
                 raise N.GomeltError("Level-3 window reaches outside Level 2's footprint in Level 1")
-        self.tables = t
+        if assign:
+            self.tables = t
         nmax = max(t["c32"].partials, t["c31"].partials, t["c21"].partials)
         self._buf("partials", nmax)
         if own:
@@ -234,19 +235,44 @@ class Engine:
     # ------------------------------------------------------------------
     # moveEverything (:2400-2510)
     # ------------------------------------------------------------------
-    def move(self, v, vstart):
+    def plan_move(self, v, vstart):
+        """Host half of move(): the new window positions, the remap maps and
+        the per-window tables, staged in the table arena's next pinned buffer.
+        It needs no device state, so a driver can plan move i+1 while move i
+        and its subcycle run on the device, then apply it with
+        ``move(v, vstart, plan)``.  Plan only after the previous move's
+        subcycle (or step) has been issued: planning moves the host geometry.
+        At most one plan is outstanding."""
+        if self._pending is not None:
+            raise N.GomeltError("a planned move is still pending")
         g = self.geo
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         old3 = [c.copy() for c in L3.coords]
         old2 = [c.copy() for c in L2.coords]
         new3, new2, move_v = g.move(v, vstart)
-        n3, n2 = L3.nodes, L2.nodes
         self.arena.begin()
         m3 = [self._map(L1.coords, L1.nodes, new3), self._map(old2, L2.nodes, new3), self._map(old3, L3.nodes, new3)]
         m2 = [self._map(L1.coords, L1.nodes, new2), self._map(old2, L2.nodes, new2)]
         L3.coords = new3
         L2.coords = new2
-        t = self.build_tables()
+        t = self.build_tables(assign=False)
+        self._pending = MovePlan(np.array(v, dtype=np.float64), move_v, m3, m2, t, self.arena.off)
+        return self._pending
+
+    def move(self, v, vstart, plan=None):
+        """moveEverything: apply ``plan`` (from plan_move for the same v), or
+        plan and apply now.  Enqueues one table upload and the remap kernels."""
+        if plan is None:
+            plan = self.plan_move(v, vstart)
+        elif plan is not self._pending or not np.array_equal(plan.v, np.asarray(v, dtype=np.float64)):
+            raise N.GomeltError("move(): plan is not the pending plan for this laser position")
+        self._pending = None
+        g = self.geo
+        L2, L3 = g.L[2], g.L[3]
+        n3, n2 = L3.nodes, L2.nodes
+        m3, m2, t, move_v = plan.m3, plan.m2, plan.tables, plan.move_v
+        self.tables = t
+        self.last_table_bytes = plan.table_bytes
         self.arena.upload(self.stream)
         # Level 3: T = I_L1(T1) + I_L2(T'2) + I_L3old(T'3); T'3 = I_L3old(T'3)
         T3n = self._buf("mvT3", L3.nn)

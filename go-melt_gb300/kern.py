@@ -42,8 +42,8 @@ class DeviceMap3:
     """Three AxisMaps uploaded to the device, plus the gm_map3 struct."""
 
     def __init__(self, maps, src_nodes, dtype, device="cuda"):
-        self.e = [torch.as_tensor(m.elem, dtype=torch.int32, device=device).contiguous() for m in maps]
-        self.w = [torch.as_tensor(m.w.reshape(-1), dtype=dtype, device=device).contiguous() for m in maps]
+        self.e = [torch.tensor(m.elem, dtype=torch.int32, device=device) for m in maps]
+        self.w = [torch.tensor(m.w.reshape(-1), dtype=dtype, device=device) for m in maps]
         self.n = [int(m.elem.size) for m in maps]
         self.src_nodes = [int(x) for x in src_nodes]
         s = N.gm_map3()
