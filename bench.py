@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the Level-3 level-step kernel --steps times (for profiling)")
+    ap.add_argument("--precision", action="store_true",
+                    help="FP32 against FP64 on the 2.5 um Level-3 window: T error and melt pool")
+    ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the FP32-vs-FP64 check")
     return ap.parse_args()
 
 
@@ -63,12 +66,12 @@ def dist_env():
     return ws, rank, local
 
 
-def workload():
+def workload(config=1):
     import createPath
     import levels
     import workloads
 
-    cfg = workloads.config1()
+    cfg = workloads.config2() if config == 2 else workloads.config1()
     P = levels.setup_properties(cfg["properties"])
     nm = levels.setup_nonmesh(cfg["nonmesh"])
     r = cfg["raster"]
@@ -386,6 +389,14 @@ def run_ours(args):
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
     }
+    if args.fp64_steps > 0:
+        del eng
+        torch.cuda.empty_cache()
+        chk = compare_fp64(cfg, P, nm, rows, args.fp64_steps, dev)
+        line["fp64_check"] = {"steps": chk["steps"], "L3_max_K": chk["L3_max_K"], "L3_rms_K": chk["L3_rms_K"],
+                              "L1_max_K": chk["L1_max_K"], "L2_max_K": chk["L2_max_K"],
+                              "L3_peak_K": chk["L3_peak_K"],
+                              "what": "same steps from the same start in FP32 and FP64 on this GPU"}
     if not args.no_cpu_baseline and ws == 1:
         v, secs, n = oracle_sample(cfg, rows, args.cpu_steps)
         line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": 1, "kind": "port",
@@ -394,6 +405,70 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def compare_fp64(cfg, P, nm, rows, nsteps, dev, iso=None, stream=None):
+    """The same nsteps multilevel steps in FP32 and FP64 from the same start:
+    max / RMS temperature difference per level (FP64 reductions on the device),
+    optionally the melt pool at the isotherm iso, and the time per step of
+    each precision."""
+    import numpy as np
+    import torch
+
+    import diagnostics
+    import engine
+
+    N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
+    n23 = N2 * N3
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    stream = stream or torch.cuda.Stream(device=dev)
+    out = {}
+    engs = {}
+    for name, dt in (("f32", torch.float32), ("f64", torch.float64)):
+        with torch.cuda.stream(stream):
+            e = engine.Engine(cfg, P, N2, N3, dtype=dt, device=dev, stream=stream)
+            e.set_layer(rows[0])
+            e.move(rows[0], vstart)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(nsteps):
+                c = rows[k * n23:(k + 1) * n23]
+                e.move(c[0], vstart)
+                e.subcycle(c)
+            torch.cuda.synchronize()
+            out[f"ms_per_step_{name}"] = 1000.0 * (time.perf_counter() - t0) / nsteps
+        engs[name] = e
+    dg = diagnostics.Diagnostics(dev)
+    a, b = engs["f32"], engs["f64"]
+    for lev in (1, 2, 3):
+        m, r = dg.field_error(a.T[lev], b.T[lev], stream=stream)
+        out[f"L{lev}_max_K"], out[f"L{lev}_rms_K"] = m, r
+    out["L3_peak_K"] = float(b.T[3].max())
+    if iso is not None:
+        L3 = b.geo.L[3]
+        for name, e in (("f32", a), ("f64", b)):
+            out[f"melt_pool_{name}"] = {k: v for k, v in dg.melt_pool(nodes=L3.nodes, h=L3.spacing(),
+                                                                        origin=L3.origin(), T=e.T[3], iso=iso,
+                                                                        stream=stream).items() if k != "extents"}
+        for k in ("length", "width", "depth"):
+            out[f"melt_pool_{k}_err_mm"] = abs(out["melt_pool_f32"][k] - out["melt_pool_f64"][k])
+    out["steps"] = nsteps
+    out["scan_mm"] = scan_mm(rows[:nsteps * n23])
+    return out
+
+
+def run_precision(args):
+    """FP32 against FP64 on the precision-study workload (2.5 um Level-3
+    window inside the part-scale Level 1 / 2)."""
+    import torch
+
+    cfg, P, nm, rows = workload(config=2)
+    dev = torch.device("cuda", 0)
+    r = compare_fp64(cfg, P, nm, rows, args.steps, dev, iso=P["T_liquidus"])
+    r.update({"precision_study": "L3 0.5x0.5x0.1 mm @ 2.5 um (200x200x40) in L1 200x200x50 @ 100 um, "
+                                 "L2 100x100x15 @ 20 um; N2 = N3 = 10, dt3 = 0.394 us; FP32 against FP64",
+              "iso_K": P["T_liquidus"]})
+    print(json.dumps(r), flush=True)
 
 
 def run_kernel_only(args):
@@ -427,6 +502,8 @@ def main():
     args = parse_args()
     if args.kernel_only:
         run_kernel_only(args)
+    elif args.precision:
+        run_precision(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -57,6 +57,18 @@ class gm_ring_args(C.Structure):
                 ("outA", vp), ("outB", vp)]
 
 
+class gm_energy_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("nodes", C.c_int * 3), ("h", C.c_double * 3), ("origin", C.c_double * 3),
+                ("ne_planes", C.c_int), ("T0", vp), ("T1", vp), ("ph", vp), ("substrate", C.c_longlong),
+                ("interval", C.c_double), ("rows", vp), ("npos", C.c_int), ("scratch", vp),
+                ("scratch_cap", C.c_longlong), ("out", vp)]
+
+
+class gm_meltpool_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("nodes", C.c_int * 3), ("h", C.c_double * 3), ("origin", C.c_double * 3),
+                ("T", vp), ("iso", C.c_double), ("scratch", vp), ("scratch_cap", C.c_longlong), ("out", vp)]
+
+
 class gm_state_props_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_longlong), ("T", vp), ("ph_in", C.POINTER(C.c_uint8)),
                 ("ph_out", C.POINTER(C.c_uint8)), ("k_out", vp), ("rc_out", vp), ("substrate", C.c_longlong)]
@@ -162,6 +174,8 @@ def lib():
             f.restype = C.c_int
         L.gm_couple_partials_size.argtypes = [C.POINTER(gm_couple_geom)]
         L.gm_couple_partials_size.restype = C.c_longlong
+        L.gm_diag_scratch_size.argtypes = [C.c_int]
+        L.gm_diag_scratch_size.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -185,6 +199,9 @@ SIGNATURES = {
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
     "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
     "gm_ring_prolong": [C.POINTER(gm_ring_args), vp],
+    "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],
+    "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
+    "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],
     "gm_couple_noalloc": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
 }
 

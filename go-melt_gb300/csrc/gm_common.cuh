@@ -106,6 +106,60 @@ template <typename real>
 struct alignas(4 * sizeof(real)) V4 {
   real x, y, z, w;
 };
+// 8-point Hadamard butterflies over the corner values of a brick element
+// (index x + 2y + 4z): forward (a, b) -> (a + b, b - a) per axis, inverse
+// (a, b) -> (a - b, a + b); inverse(forward(v)) = 8 v.
+template <typename real>
+__device__ __forceinline__ void bfly_fwd(real v[8]) {
+#pragma unroll
+  for (int s = 1; s < 8; s <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((i & s) == 0) {
+        const real a = v[i], b = v[i + s];
+        v[i] = a + b;
+        v[i + s] = b - a;
+      }
+    }
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void bfly_inv(real v[8]) {
+#pragma unroll
+  for (int s = 1; s < 8; s <<= 1) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if ((i & s) == 0) {
+        const real a = v[i], b = v[i + s];
+        v[i] = a - b;
+        v[i + s] = a + b;
+      }
+    }
+  }
+}
+
+// 1-D source factor of node i: sum over the (up to two) elements touching the
+// node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
+// rel = origin - v (formed in double by the caller), so the Gauss-point
+// offset rel + h*(e + (1 +- 1/sqrt3)/2) is small and exact enough in the
+// kernel's precision.
+template <typename real>
+__device__ __forceinline__ real src_factor(int i, int n, real rel, real h, real inv_r2) {
+  const real g0 = (real)0.21132486540518711775, g1 = (real)0.78867513459481288225;  // (1 -+ 1/sqrt3)/2
+  real s = 0;
+  for (int e = i - 1; e <= i; ++e) {
+    if (e < 0 || e >= n - 1) continue;
+    const real d0 = rel + h * ((real)e + g0);
+    const real d1 = rel + h * ((real)e + g1);
+    const real q0 = exp((real)-3 * d0 * d0 * inv_r2);
+    const real q1 = exp((real)-3 * d1 * d1 * inv_r2);
+    // node i is local node 0 of element e when i == e: weights (1-xi)/2 = g1 at xi=-1/sqrt3, g0 at +1/sqrt3
+    s += (i == e) ? (g1 * q0 + g0 * q1) : (g0 * q0 + g1 * q1);
+  }
+  return s;
+}
+
 // Flux into the top surface at one Gauss point [W/mm^2]
 // (computeConvRadBC, go_melt/computeFunctions.py:2263-2290).
 template <typename real>

@@ -63,36 +63,6 @@ struct LevelK {
 
 constexpr int ZMAX = 64;
 
-template <typename real>
-__device__ __forceinline__ void bfly_fwd(real v[8]) {
-#pragma unroll
-  for (int s = 1; s < 8; s <<= 1) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if ((i & s) == 0) {
-        const real a = v[i], b = v[i + s];
-        v[i] = a + b;
-        v[i + s] = b - a;
-      }
-    }
-  }
-}
-
-template <typename real>
-__device__ __forceinline__ void bfly_inv(real v[8]) {
-#pragma unroll
-  for (int s = 1; s < 8; s <<= 1) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if ((i & s) == 0) {
-        const real a = v[i], b = v[i + s];
-        v[i] = a - b;
-        v[i + s] = a + b;
-      }
-    }
-  }
-}
-
 // x/y butterfly of one face (4 corner values, index x + 2y): the first two
 // stages of bfly_fwd, which act on each face separately.
 template <typename real>
@@ -112,27 +82,6 @@ __device__ __forceinline__ void face_fwd(real v[4]) {
   b = v[3];
   v[1] = a + b;
   v[3] = b - a;
-}
-
-// 1-D source factor of node i: sum over the (up to two) elements touching the
-// node and their two Gauss points of N_local * exp(-3 (xq - v)^2 / r^2).
-// rel = origin - v (formed in double by the caller), so the Gauss-point
-// offset rel + h*(e + (1 +- 1/sqrt3)/2) is small and exact enough in the
-// kernel's precision.
-template <typename real>
-__device__ __forceinline__ real src_factor(int i, int n, real rel, real h, real inv_r2) {
-  const real g0 = (real)0.21132486540518711775, g1 = (real)0.78867513459481288225;  // (1 -+ 1/sqrt3)/2
-  real s = 0;
-  for (int e = i - 1; e <= i; ++e) {
-    if (e < 0 || e >= n - 1) continue;
-    const real d0 = rel + h * ((real)e + g0);
-    const real d1 = rel + h * ((real)e + g1);
-    const real q0 = exp((real)-3 * d0 * d0 * inv_r2);
-    const real q1 = exp((real)-3 * d1 * d1 * inv_r2);
-    // node i is local node 0 of element e when i == e: weights (1-xi)/2 = g1 at xi=-1/sqrt3, g0 at +1/sqrt3
-    s += (i == e) ? (g1 * q0 + g0 * q1) : (g0 * q0 + g1 * q1);
-  }
-  return s;
 }
 
 template <typename real>
@@ -501,8 +450,11 @@ __global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step
   }
 }
 
-// Tile of one CTA: 16 x 16 element columns (15 x 15 output node columns).
-constexpr int LT_X = 16, LT_Y = 16;
+// Tile of one CTA: 32 x 8 element columns (31 x 7 output node columns).
+// Measured on the 161 x 161 x 41-node Level-3 window against 16 x 16 tiles
+// over z-chunks of 4..41 planes: 17.1 us (32 x 8, 14 planes) vs 17.4 us
+// (16 x 16, 12 planes) per launch.
+constexpr int LT_X = 32, LT_Y = 8;
 
 // Node planes per CTA when the caller does not choose.  The kernel is bound
 // by instruction issue, so the time of a launch follows the busiest SM:

@@ -72,3 +72,13 @@ def config1():
                     "info_T": 0},
         "raster": {"x0": 8.0, "y0": 8.0, "length": 4.0, "hatch": 0.1, "ntracks": 40},
     }
+
+
+def config2():
+    """Precision study: config 1 with a fine Level-3 window of 0.5 x 0.5 x 0.1 mm
+    at 2.5 um (200 x 200 x 40 elements; Level-2 to Level-3 ratio 8), placed on
+    Level-2 nodes around the raster start.  dt3 = 0.394 us."""
+    c = config1()
+    c["Level3"] = {"elements": [200, 200, 40], "bounds": {"x": [9.76, 10.26], "y": [9.76, 10.26], "z": [-0.1, 0.0]}}
+    c["nonmesh"]["timestep_L3"] = dt_fine(0.0025)
+    return c

@@ -398,6 +398,75 @@ int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream);
 /* Library identification: returns a static string; never fails. */
 const char* gm_version(void);
 
+/* ------------------------------------------------------------------------
+ * Diagnostics (no counterpart in the reference; quantities the GB300 build
+ * reports beside its results).  All reduce in FP64 with two-stage,
+ * fixed-order reductions, and write their results to device memory (`out`).
+ * `scratch` holds gm_diag_scratch_size(npos) doubles of device memory.
+ * ------------------------------------------------------------------------ */
+long long gm_diag_scratch_size(int npos);
+
+/* Energy balance of a level window over an interval [t0, t0 + interval]
+ * from its fields at both ends (T0, T1) and the laser rows of the fine steps
+ * in between.  With interior nodes I = {1 <= ix <= nx-2, 1 <= iy <= ny-2,
+ * 1 <= iz <= ne_planes} (the nodes not on the Dirichlet ring),
+ * T_bar = (T0 + T1) / 2 and properties from T_bar and the phase ph of t0:
+ *   out[0] stored  = sum_{i in I} V_i (h(T1_i) - h(T0_i)),  V_i = sum_e wq
+ *                    (lumped volume), h(T) = rho * integral of c_p(T) dT of
+ *                    the phase model (c1 T + c0 below T_solidus, c_mushy up
+ *                    to T_liquidus, c_fluid above)
+ *   out[1] source  = sum_rows dt_r sum_{i in I} F_src,i(row r)
+ *   out[2] surface = interval * sum_{i in I} F_surf,i(T_bar)
+ *   out[3] conduct = -interval * sum_{i in I} (K(T_bar) T_bar)_i
+ * with the lumped mass, stiffness, laser source and surface flux of
+ * solveMatrixFreeFE / computeSourcesL3 / computeConvRadBC.  The residual
+ * |out[0] - out[1] - out[2] - out[3]| / (eta * sum_r dt_r P_r) is the
+ * relative energy-balance error that accepts or rejects a predicted field. */
+typedef struct gm_energy_args {
+  int dtype; /* of T0 and T1 */
+  int nodes[3];
+  double h[3];
+  double origin[3];
+  int ne_planes;
+  const void* T0;
+  const void* T1;
+  const uint8_t* ph; /* phase byte at t0 (may be NULL: powder) */
+  long long substrate;
+  double interval;
+  const double* rows; /* npos laser rows (x, y, z, -, -, dt, P) */
+  int npos;
+  double* scratch;
+  long long scratch_cap; /* doubles */
+  double* out;           /* 4 doubles */
+} gm_energy_args;
+
+int gm_energy_balance(const gm_energy_args* a, const gm_props* p, void* stream);
+
+/* Melt-pool extent at the isotherm T = iso: over the nodes with T >= iso,
+ * the min / max coordinate per axis, each extended to the linearly
+ * interpolated crossing towards every neighbour with T < iso.
+ * out = {xmin, xmax, ymin, ymax, zmin, zmax, count}; count 0 leaves the
+ * extents at +-inf.  Length / width / depth = xmax-xmin, ymax-ymin,
+ * z_top-zmin. */
+typedef struct gm_meltpool_args {
+  int dtype;
+  int nodes[3];
+  double h[3];
+  double origin[3];
+  const void* T;
+  double iso;
+  double* scratch;
+  long long scratch_cap; /* doubles */
+  double* out;           /* 7 doubles */
+} gm_meltpool_args;
+
+int gm_melt_pool(const gm_meltpool_args* a, void* stream);
+
+/* out = {max |A - B|, sqrt(mean (A - B)^2)} over n values (A, B of types
+ * dtype_a, dtype_b: e.g. an FP32 run against an FP64 run). */
+int gm_field_error(int dtype_a, const void* A, int dtype_b, const void* B, long long n, double* scratch,
+                   long long scratch_cap, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
