@@ -56,6 +56,11 @@ def parse_args():
     ap.add_argument("--precision", action="store_true",
                     help="FP32 against FP64 on the 2.5 um Level-3 window: T error and melt pool")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the FP32-vs-FP64 check")
+    ap.add_argument("--surrogate", action="store_true",
+                    help="Level-3 surrogate: snapshots of the batched instances, training, part-scale evaluation")
+    ap.add_argument("--train-steps", type=int, default=1500)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--instances", type=int, default=64)
     return ap.parse_args()
 
 
@@ -471,6 +476,88 @@ def run_precision(args):
     print(json.dumps(r), flush=True)
 
 
+def run_surrogate(args):
+    """Snapshots from the 64 batched single-track instances, BF16 training on
+    the device, evaluation on the part-scale raster against its plain run."""
+    import numpy as np
+    import torch
+
+    import engine
+    import surrogate
+    import surrogate_run as SR
+    import workloads
+
+    dev = torch.device("cuda", 0)
+    inst = workloads.config3(n=args.instances)
+    snaps, t_gen = SR.generate(inst, dev)
+    nodes0 = [81, 81, 21]
+    net = surrogate.UNet(dev, seed=0)
+    losses, t_train = SR.train(net, snaps, nodes0, (80, 80, 20), args.train_steps, args.batch, 1e-3, dev,
+                               log_every=max(1, args.train_steps // 10))
+    train_flops = 3.0 * net.flops((args.batch, 80, 80, 20)) * args.train_steps
+    # part-scale evaluation
+    cfg, P, nm, rows = workload()
+    st = SR.evaluate(net, cfg, dev, nsteps=max(2, args.steps // 4))
+    # inference alone on the part-scale window (CUDA events, back to back)
+    X, Y, Z = 160, 160, 40
+    x = torch.zeros(X * Y * Z, 16, dtype=torch.bfloat16, device=dev)
+    for _ in range(3):
+        net.forward(x, (1, X, Y, Z))
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(10):
+        net.forward(x, (1, X, Y, Z))
+    e.record()
+    torch.cuda.synchronize()
+    t_inf = s.elapsed_time(e) / 10
+    fl = net.flops((1, X, Y, Z))
+    # plain Level-3 work of one Level-2 step: 2 passes x N3 level steps (+ ring), timed alone
+    N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
+    n23 = N2 * N3
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        eng = engine.Engine(cfg, P, N2, N3, device=dev, stream=stream)
+        eng.set_layer(rows[0])
+        for k in range(4):
+            eng.move(rows[k * n23], vstart)
+            eng.subcycle(rows[k * n23:(k + 1) * n23])
+        stream.synchronize()
+        t0 = time.perf_counter()
+        for k in range(4, 14):
+            eng.move(rows[k * n23], vstart)
+            eng.subcycle(rows[k * n23:(k + 1) * n23])
+        stream.synchronize()
+        t_step = 1000.0 * (time.perf_counter() - t0) / 10
+    peak = None
+    try:
+        with open(PEAKS_FILE) as f:
+            pk = json.load(f)
+        peak = pk.get("bf16_tflops") or pk.get("bf16_tflops_sustained")
+    except (OSError, ValueError):
+        pass
+    med = lambda v: float(np.median(v)) if len(v) else None
+    acc = st["accepted"] / max(st["total"], 1)
+    line = {
+        "metric": "surrogate vs plain, part-scale raster (Level-3 surrogate per Level-2 step)",
+        "snapshots": snaps.n, "snapshot_gen_s": t_gen, "instances": len(inst),
+        "train": {"steps": args.train_steps, "batch": args.batch, "seconds": t_train,
+                  "tflops": train_flops / t_train / 1e12, "loss_first": losses[0][1] if losses else None,
+                  "loss_last": losses[-1][1] if losses else None, "curve": losses},
+        "inference": {"grid": [X, Y, Z], "ms": t_inf, "tflops": fl / (t_inf * 1e-3) / 1e12,
+                      "bf16_peak_tflops": peak, "frac": (fl / (t_inf * 1e-3) / 1e12 / peak) if peak else None},
+        "eval_level2_steps": st["total"], "accepted_frac": acc,
+        "max_err_K": {"median": med(st["max_err"]), "max": max(st["max_err"]) if st["max_err"] else None},
+        "rms_err_K": {"median": med(st["rms_err"])},
+        "energy_residual": {"surrogate_median": med(st["residual"]), "plain_median": med(st["plain_residual"]),
+                            "plain_max": max(st["plain_residual"]) if st["plain_residual"] else None},
+        "plain_ms_per_step": t_step, "plain_ms_per_level2_step": t_step / N2,
+        "surrogate_ms_per_level2_step": med(st["t_pred_ms"]),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_kernel_only(args):
     """The dominant kernel alone on the workload's Level-3 window after
     --warmup subcycle calls (the case the ncu summaries under profiles/ use)."""
@@ -504,6 +591,8 @@ def main():
         run_kernel_only(args)
     elif args.precision:
         run_precision(args)
+    elif args.surrogate:
+        run_surrogate(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -69,6 +69,30 @@ class gm_meltpool_args(C.Structure):
                 ("T", vp), ("iso", C.c_double), ("scratch", vp), ("scratch_cap", C.c_longlong), ("out", vp)]
 
 
+class gm_conv_args(C.Structure):
+    _fields_ = [("grid", C.c_int * 4), ("cin", C.c_int), ("cout", C.c_int), ("in_", vp), ("in_stride", C.c_int),
+                ("in_off", C.c_int), ("w", vp), ("bias", vp), ("relu", C.c_int), ("mask", vp),
+                ("mask_stride", C.c_int), ("mask_off", C.c_int), ("mirror", C.c_int), ("out", vp),
+                ("out_stride", C.c_int), ("out_off", C.c_int)]
+
+
+class gm_wgrad_args(C.Structure):
+    _fields_ = [("grid", C.c_int * 4), ("cin", C.c_int), ("cout", C.c_int), ("in_", vp), ("in_stride", C.c_int),
+                ("in_off", C.c_int), ("dy", vp), ("dy_stride", C.c_int), ("dy_off", C.c_int), ("dw", vp),
+                ("scratch", vp), ("scratch_cap", C.c_longlong)]
+
+
+class gm_adam_args(C.Structure):
+    _fields_ = [("n", C.c_longlong), ("w", vp), ("grad", vp), ("m", vp), ("v", vp), ("lr", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("c1", C.c_float),
+                ("c2", C.c_float), ("wd", C.c_float), ("wb", vp), ("wt", vp), ("cout", C.c_int), ("cin", C.c_int)]
+
+
+class gm_surr_args(C.Structure):
+    _fields_ = [("grid", C.c_int * 4), ("nodes", C.c_int * 3), ("T2i", vp), ("T3o", vp), ("T3n", vp), ("par", vp),
+                ("T_amb", C.c_double), ("scale", C.c_double), ("x", vp), ("target", vp), ("lmask", vp)]
+
+
 class gm_state_props_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_longlong), ("T", vp), ("ph_in", C.POINTER(C.c_uint8)),
                 ("ph_out", C.POINTER(C.c_uint8)), ("k_out", vp), ("rc_out", vp), ("substrate", C.c_longlong)]
@@ -176,6 +200,10 @@ def lib():
         L.gm_couple_partials_size.restype = C.c_longlong
         L.gm_diag_scratch_size.argtypes = [C.c_int]
         L.gm_diag_scratch_size.restype = C.c_longlong
+        L.gm_unet_wgrad_scratch.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_int]
+        L.gm_unet_wgrad_scratch.restype = C.c_longlong
+        L.gm_unet_head_scratch.argtypes = [C.c_longlong, C.c_int]
+        L.gm_unet_head_scratch.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -202,6 +230,19 @@ SIGNATURES = {
     "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],
     "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
     "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],
+    "gm_unet_conv3": [C.POINTER(gm_conv_args), vp],
+    "gm_unet_wgrad": [C.POINTER(gm_wgrad_args), vp],
+    "gm_unet_bias_grad": [C.POINTER(C.c_int), C.c_int, vp, C.c_int, C.c_int, vp, C.c_longlong, vp, vp],
+    "gm_unet_pool2": [C.POINTER(C.c_int), C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp],
+    "gm_unet_up2": [C.POINTER(C.c_int), C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp],
+    "gm_unet_add_slice": [C.c_longlong, C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int,
+                          vp],
+    "gm_unet_head": [C.c_longlong, C.c_int, vp, C.c_int, C.c_int, vp, C.c_float, vp, vp],
+    "gm_unet_head_bwd": [C.c_longlong, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_float, vp, C.c_int,
+                         C.c_int, vp, C.c_longlong, vp, vp],
+    "gm_unet_adam": [C.POINTER(gm_adam_args), vp],
+    "gm_surrogate_pack": [C.POINTER(gm_surr_args), vp],
+    "gm_surrogate_unpack": [C.POINTER(gm_surr_args), vp, vp, vp],
     "gm_couple_noalloc": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
 }
 
@@ -212,7 +253,8 @@ def check(code: int, what: str):
 
 
 # kernels launched by each entry point (for launch accounting)
-KERNELS_PER_CALL = {"gm_couple": 2, "gm_coarse_source": 2}
+KERNELS_PER_CALL = {"gm_couple": 2, "gm_coarse_source": 2, "gm_unet_wgrad": 2, "gm_unet_bias_grad": 2,
+                    "gm_unet_head_bwd": 2}
 _launches = [0]
 
 

@@ -82,3 +82,56 @@ def config2():
     c["Level3"] = {"elements": [200, 200, 40], "bounds": {"x": [9.76, 10.26], "y": [9.76, 10.26], "z": [-0.1, 0.0]}}
     c["nonmesh"]["timestep_L3"] = dt_fine(0.0025)
     return c
+
+
+def config3(n=64, seed=0):
+    """Batched single-track instances: Level-1 meshes of U{30..120} x U{30..120}
+    x U{8..20} elements at 100 um, Level-2 / Level-3 windows as in config 0
+    (1 x 1 x 0.2 mm at 20 um, 0.4 x 0.4 x 0.1 mm at 5 um); laser power
+    U[100, 400] W, speed U[0.5, 1.5] m/s, radius U[35, 70] um, track angle
+    U[0, 180) deg; the track is centred with length min(4 mm, what fits with
+    0.6 mm to every edge).  numpy default_rng(seed); returns n input dicts."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        ex, ey = (int(v) for v in rng.integers(30, 121, 2))
+        ez = int(rng.integers(8, 21))
+        P = float(rng.uniform(100.0, 400.0))
+        vel = float(rng.uniform(500.0, 1500.0))
+        r = float(rng.uniform(0.035, 0.070))
+        ang = float(rng.uniform(0.0, 180.0))
+        Lx, Ly = ex * 0.1, ey * 0.1
+        cx, cy = 0.5 * Lx, 0.5 * Ly
+        ux, uy = np.cos(np.radians(ang)), np.sin(np.radians(ang))
+        m = 0.6
+        lim = []
+        for u, L in ((ux, Lx), (uy, Ly)):
+            if abs(u) > 1e-9:
+                lim.append((L - 2 * m) / abs(u))
+        length = min([4.0] + lim)
+        x0, y0 = cx - 0.5 * length * ux, cy - 0.5 * length * uy
+        x1, y1 = cx + 0.5 * length * ux, cy + 0.5 * length * uy
+        # windows around the track start, on the coarser grids' nodes
+        bx2 = round(min(max(round((x0 - 0.5) / 0.1) * 0.1, 0.0), Lx - 1.0), 6)
+        by2 = round(min(max(round((y0 - 0.5) / 0.1) * 0.1, 0.0), Ly - 1.0), 6)
+        bx3 = round(min(max(bx2 + round((x0 - 0.2 - bx2) / 0.02) * 0.02, bx2), bx2 + 0.6), 6)
+        by3 = round(min(max(by2 + round((y0 - 0.2 - by2) / 0.02) * 0.02, by2), by2 + 0.6), 6)
+        props = dict(copy.deepcopy(MATERIAL), laser_power=P, laser_radius=r,
+                     laser_center=[bx3 + 0.2, by3 + 0.2, 0.0, 0, 0, 0, 0])
+        out.append({
+            "Level1": {"elements": [ex, ey, ez], "bounds": {"x": [0.0, Lx], "y": [0.0, Ly], "z": [-0.1 * ez, 0.0]},
+                       "conditions": _cond()},
+            "Level2": {"elements": [50, 50, 10],
+                       "bounds": {"x": [bx2, bx2 + 1.0], "y": [by2, by2 + 1.0], "z": [-0.2, 0.0]}},
+            "Level3": {"elements": [80, 80, 20],
+                       "bounds": {"x": [bx3, bx3 + 0.4], "y": [by3, by3 + 0.4], "z": [-0.1, 0.0]}},
+            "properties": props,
+            "nonmesh": {"timestep_L3": dt_fine(0.005), "subcycle_num_L2": 10, "subcycle_num_L3": 10,
+                        "laser_velocity": vel, "output_files": 0, "wait_time": 10, "dwell_time": 1e-4,
+                        "info_T": 0},
+            "gcode": f"G0 X{x0:.4f} Y{y0:.4f} Z0.0000\nG1 X{x1:.4f} Y{y1:.4f} Z0.0000\n",
+            "instance": {"power": P, "speed": vel, "radius": r, "angle": ang, "length": length},
+        })
+    return out

@@ -467,6 +467,123 @@ int gm_melt_pool(const gm_meltpool_args* a, void* stream);
 int gm_field_error(int dtype_a, const void* A, int dtype_b, const void* B, long long n, double* scratch,
                    long long scratch_cap, double* out, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Level-3 surrogate (no counterpart in the reference): BF16 tensor-core
+ * building blocks of a 3-D convolutional U-Net, trained and run on the
+ * device.  Activations are channels-last BF16 [B][Z][Y][X][C]; a tensor
+ * argument is a channel slice (offset, stride) of a wider tensor.  grid =
+ * {B, X, Y, Z}.  3x3x3 weights are BF16 [27][Cout][Cin] (tap = dx + 3 dy +
+ * 9 dz for offsets dx-1, dy-1, dz-1), zero padding at the sample borders.
+ * ------------------------------------------------------------------------ */
+typedef struct gm_conv_args {
+  int grid[4];
+  int cin, cout;         /* cin % 16 == 0; cout in {16, 32, 64, 96, 128, 192} */
+  const void* in;        /* BF16 */
+  int in_stride, in_off; /* even */
+  const void* w;         /* BF16 [27][cout][cin] */
+  const float* bias;     /* [cout] or NULL */
+  int relu;              /* y = max(y, 0) */
+  const void* mask;      /* BF16 or NULL: y = 0 where mask <= 0 */
+  int mask_stride, mask_off;
+  int mirror;            /* 1: tap offsets negated (data gradient with W^T) */
+  void* out;             /* BF16 */
+  int out_stride, out_off;
+} gm_conv_args;
+
+/* y[v][co] = act(bias[co] + sum_tap sum_ci x[v + d(tap)][ci] w[tap][co][ci])
+ * (mirror 0), or the data gradient dx[u][ci] = sum_tap dy[u - d(tap)] .
+ * w[tap][.][ci] with w passed as [27][Cin][Cout] (mirror 1). */
+int gm_unet_conv3(const gm_conv_args* a, void* stream);
+
+typedef struct gm_wgrad_args {
+  int grid[4];
+  int cin, cout; /* cin % 32 == 0 or cin == 16; cout % 16 == 0 */
+  const void* in;
+  int in_stride, in_off;
+  const void* dy;
+  int dy_stride, dy_off;
+  float* dw;     /* FP32 [27][cout][cin] */
+  float* scratch;
+  long long scratch_cap; /* floats: gm_unet_wgrad_scratch() */
+} gm_wgrad_args;
+
+/* dw[tap][co][ci] = sum_v dy[v][co] x[v + d(tap)][ci] (split over the
+ * voxels, partials summed in a fixed order). */
+long long gm_unet_wgrad_scratch(const int grid[4], int cin, int cout);
+int gm_unet_wgrad(const gm_wgrad_args* a, void* stream);
+
+/* db[c] = sum_v dy[v][c]; scratch: ceil(V / 4096) * C floats (at most 1024 * C). */
+int gm_unet_bias_grad(const int grid[4], int C, const void* dy, int stride, int off, float* scratch,
+                      long long scratch_cap, float* db, void* stream);
+
+/* 2x average pooling of grid (forward: out on grid / 2) or its gradient
+ * (backward: in on grid / 2, out on grid). */
+int gm_unet_pool2(const int grid[4], int C, const void* in, int in_stride, int in_off, void* out, int out_stride,
+                  int out_off, int backward, void* stream);
+
+/* 2x nearest upsampling onto grid (forward: in on grid / 2) or its gradient
+ * (backward: in on grid, out on grid / 2). */
+int gm_unet_up2(const int grid[4], int C, const void* in, int in_stride, int in_off, void* out, int out_stride,
+                int out_off, int backward, void* stream);
+
+/* b[v][c] += a[v][c] over V voxels and C channels (BF16 slices), where
+ * mask[v][c] > 0 if a mask slice is given. */
+int gm_unet_add_slice(long long V, int C, const void* a, int a_stride, int a_off, void* b, int b_stride, int b_off,
+                      const void* mask, int mask_stride, int mask_off, void* stream);
+
+/* Head: out[v] = b + sum_c w[c] x[v][c] (FP32 out), and its backward for the
+ * loss mean over voxels of lmask (pred - target)^2 (inv_count = 1 / sum lmask):
+ * dx (zero where x <= 0, the head's input being a ReLU output) and
+ * dwb = {dw[0..C), db, loss}.  C <= 32. */
+int gm_unet_head(long long V, int C, const void* in, int in_stride, int in_off, const float* w, float b, float* out,
+                 void* stream);
+long long gm_unet_head_scratch(long long V, int C);
+int gm_unet_head_bwd(long long V, int C, const void* in, int in_stride, int in_off, const float* w, const float* pred,
+                     const float* target, const float* lmask, float inv_count, void* dx, int dx_stride, int dx_off,
+                     float* scratch, long long scratch_cap, float* dwb, void* stream);
+
+/* Adam step on an FP32 master copy w (n values) with gradient grad, moments
+ * m, v; c1 = 1 - beta1^t, c2 = 1 - beta2^t; wd: L2 weight decay.  Writes the
+ * BF16 copy wb and, if wt is set, its [27][cin][cout] transpose. */
+typedef struct gm_adam_args {
+  long long n;
+  float* w;
+  const float* grad;
+  float* m;
+  float* v;
+  float lr, beta1, beta2, eps, c1, c2, wd;
+  void* wb;
+  void* wt;
+  int cout, cin;
+} gm_adam_args;
+
+int gm_unet_adam(const gm_adam_args* a, void* stream);
+
+/* Surrogate input / output on B windows of `nodes` nodes each (FP32 fields,
+ * sample b at offset b * nodes[0] * nodes[1] * nodes[2]).  The network grid
+ * {B, X, Y, Z} covers the nodes ix < X, iy < Y, 1 <= iz <= Z.  x: BF16
+ * [V][16] channels (I(T2) - T_amb) / S, (T3_start - T_amb) / S, node offset
+ * from the mid-step laser position (x, y) * inv_r, P / P_s, v / v_s, zeros;
+ * target = (T3_end - I(T2)) / S (if T3n and target are set); lmask = 1 off
+ * the Dirichlet ring (ix, iy >= 1).  par: 8 doubles per sample: window
+ * origin x, y, spacing h, laser x, y, inv_r, P / P_s, v / v_s.  Unpack:
+ * T3 = I(T2) + S * pred on the grid's nodes off the ring. */
+typedef struct gm_surr_args {
+  int grid[4];
+  int nodes[3];
+  const float* T2i;
+  const float* T3o;
+  const float* T3n;
+  const double* par;
+  double T_amb, scale;
+  void* x;
+  float* target;
+  float* lmask;
+} gm_surr_args;
+
+int gm_surrogate_pack(const gm_surr_args* a, void* stream);
+int gm_surrogate_unpack(const gm_surr_args* a, const float* pred, float* T3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
