@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--train-steps", type=int, default=1500)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--batched", action="store_true",
+                    help="batched single-track instances: per-instance vs batched level launches (CUDA graphs)")
     return ap.parse_args()
 
 
@@ -258,6 +260,7 @@ def run_ours(args):
         eng = engine.Engine(cfg, P, N2, N3, dtype=dtype, device=dev, stream=stream)
         eng.set_layer(rows[0])
         eng.move(rows[0], vstart)
+        tuned = eng.autotune(rows[0])  # launch shapes of the level steps, measured (set-up, untimed)
 
         def chunk(k):
             return rows[k * n23:(k + 1) * n23]
@@ -393,6 +396,8 @@ def run_ours(args):
                      "traffic": traffic, "kernel": "level_step_kernel (Level 3)", "kernel_ms": k_ms,
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
+        "autotuned": {f"L{lev}": {"tile": [v[0], v[1]], "zchunk": v[2], "us": round(v[3], 2)}
+                      for lev, v in tuned.items()},
     }
     if args.fp64_steps > 0:
         del eng
@@ -558,6 +563,103 @@ def run_surrogate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args):
+    """The 64 batched single-track instances after two plain steps each: one
+    fine step of every instance's Level 3 (uniform 81 x 81 x 21 windows) and
+    Level 1 (uneven meshes) as one launch per instance or as ONE batched
+    launch, each replayed from a CUDA graph of --steps fine steps."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import _native as N
+    import engine
+    import kern
+    import surrogate_run as SR
+    import workloads
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    inst = workloads.config3(n=args.instances)
+    engs, rowsv = [], []
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for cfg in inst:
+            P, nm, rows = SR._instance_rows(cfg)
+            e = engine.Engine(cfg, P, nm["subcycle_num_L2"], nm["subcycle_num_L3"], device=dev, stream=stream)
+            vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+            e.set_layer(rows[0])
+            for k in range(2):
+                e.move(rows[k * 100], vstart)
+                e.subcycle(rows[k * 100:(k + 1) * 100])
+            engs.append(e)
+            rowsv.append(torch.as_tensor(rows[199], device=dev))
+    stream.synchronize()
+    t_setup = time.perf_counter() - t0
+    out = {"metric": "batched instances: level steps per launch", "instances": len(engs), "setup_s": t_setup}
+    K = max(args.steps, 4)
+    for lev in (3, 1):
+        kws = []
+        for e, row in zip(engs, rowsv):
+            L = e.geo.L[lev]
+            T_out = torch.empty_like(e.T[lev])
+            ph_out = torch.empty_like(e.ph[lev])
+            if lev == 3:
+                ring = e._ring(3, e.T[2], e.T[2])
+                kw = e.level_kwargs(3, e.T[3], T_out, row[5:6], e.ph[3], ph_out, laser=row, ring=ring, alpha=0.5)
+            else:
+                kw = e.level_kwargs(1, e.T[1], T_out, row[5:6] * 100, e.ph[1], ph_out)
+            kws.append(kw)
+        nodes = sum(int(np.prod(kw["nodes"])) for kw in kws)
+        args_arr = (N.gm_level_args * len(kws))(*[kern.level_args(**kw) for kw in kws])
+        props = (N.gm_props * len(kws))(*[e.ps for e in engs])
+        nbytes = int(N.lib().gm_level_batched_desc_size(len(kws), N.GM_F32))
+        desc = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        info = N.gm_batch_info()
+        with torch.cuda.stream(stream):
+            N.call("gm_level_batched_prepare", C.cast(args_arr, C.c_void_p), len(kws), C.cast(props, C.c_void_p),
+                   desc.data_ptr(), nbytes, C.byref(info), kern.stream_ptr(stream))
+            if lev == 3:
+                tuned = kern.level_autotune(engs[0].ps, reps=5, stream=stream, **kws[0])
+                out["L3_autotuned_shape"] = {"tile": [tuned[0], tuned[1]], "zchunk": tuned[2], "us": tuned[3]}
+
+            def single():
+                for e, kw in zip(engs, kws):
+                    kern.level_step(e.ps, stream=stream, **kw)
+
+            def batched():
+                N.call("gm_level_batched_launch", desc.data_ptr(), C.byref(info), kern.stream_ptr(stream))
+
+            res = {}
+            for name, fn in (("per_instance", single), ("batched", batched)):
+                fn()
+                stream.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=stream):
+                    for _ in range(K):
+                        fn()
+                g.replay()
+                stream.synchronize()
+                best = None
+                for _ in range(3):
+                    s, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    s.record(stream)
+                    g.replay()
+                    e_.record(stream)
+                    stream.synchronize()
+                    t = s.elapsed_time(e_) / K
+                    best = t if best is None else min(best, t)
+                res[name] = {"ms_per_fine_step": best, "gnode_steps_per_s": nodes / (best * 1e-3) / 1e9,
+                             "launches_per_fine_step": len(kws) if name == "per_instance" else 1}
+                del g
+        res["speedup"] = res["per_instance"]["ms_per_fine_step"] / res["batched"]["ms_per_fine_step"]
+        res["nodes"] = nodes
+        res["shapes"] = "uniform 81x81x21" if lev == 3 else "uneven 31..121 x 31..121 x 9..21"
+        out[f"L{lev}"] = res
+    print(json.dumps(out), flush=True)
+
+
 def run_kernel_only(args):
     """The dominant kernel alone on the workload's Level-3 window after
     --warmup subcycle calls (the case the ncu summaries under profiles/ use)."""
@@ -593,6 +695,8 @@ def main():
         run_precision(args)
     elif args.surrogate:
         run_surrogate(args)
+    elif args.batched:
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -93,6 +93,14 @@ class gm_surr_args(C.Structure):
                 ("T_amb", C.c_double), ("scale", C.c_double), ("x", vp), ("target", vp), ("lmask", vp)]
 
 
+class gm_batch_info(C.Structure):
+    _fields_ = [("nb", C.c_int), ("dtype", C.c_int), ("variant", C.c_int), ("blocks", C.c_int)]
+
+
+class gm_tune_result(C.Structure):
+    _fields_ = [("tile_x", C.c_int), ("tile_y", C.c_int), ("zchunk", C.c_int), ("us", C.c_float)]
+
+
 class gm_state_props_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_longlong), ("T", vp), ("ph_in", C.POINTER(C.c_uint8)),
                 ("ph_out", C.POINTER(C.c_uint8)), ("k_out", vp), ("rc_out", vp), ("substrate", C.c_longlong)]
@@ -198,6 +206,8 @@ def lib():
             f.restype = C.c_int
         L.gm_couple_partials_size.argtypes = [C.POINTER(gm_couple_geom)]
         L.gm_couple_partials_size.restype = C.c_longlong
+        L.gm_level_batched_desc_size.argtypes = [C.c_int, C.c_int]
+        L.gm_level_batched_desc_size.restype = C.c_longlong
         L.gm_diag_scratch_size.argtypes = [C.c_int]
         L.gm_diag_scratch_size.restype = C.c_longlong
         L.gm_unet_wgrad_scratch.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_int]
@@ -227,6 +237,10 @@ SIGNATURES = {
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
     "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
     "gm_ring_prolong": [C.POINTER(gm_ring_args), vp],
+    "gm_level_step_batched": [vp, C.c_int, vp, vp, C.c_longlong, vp],
+    "gm_level_batched_prepare": [vp, C.c_int, vp, vp, C.c_longlong, C.POINTER(gm_batch_info), vp],
+    "gm_level_batched_launch": [vp, C.POINTER(gm_batch_info), vp],
+    "gm_level_autotune": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.c_int, C.POINTER(gm_tune_result), vp],
     "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],
     "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
     "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],
@@ -254,7 +268,7 @@ def check(code: int, what: str):
 
 # kernels launched by each entry point (for launch accounting)
 KERNELS_PER_CALL = {"gm_couple": 2, "gm_coarse_source": 2, "gm_unet_wgrad": 2, "gm_unet_bias_grad": 2,
-                    "gm_unet_head_bwd": 2}
+                    "gm_unet_head_bwd": 2, "gm_level_batched_prepare": 0}
 _launches = [0]
 
 

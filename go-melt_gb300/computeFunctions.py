@@ -733,6 +733,62 @@ def printLevelMaxMin(Ls, Lnames):
     print("")
 
 
+# ---------------------------------------------------------------------------
+# Output files (saveResult & co., :1945-2057, :3668-3693), written by vtk.py
+# ---------------------------------------------------------------------------
+def _host(a):
+    return a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+
+
+def saveResult(Level, save_str, record_lab, save_path, zoffset):
+    """:1945-1982: temperature and S1 of a level as a rectilinear grid
+    ``{save_path}{save_str}{record_lab:08}.vtr`` (z shifted by -zoffset)."""
+    import vtk
+
+    c = [np.asarray(Level["node_coords"][d], dtype=np.float64) for d in range(3)]
+    vtk.write_vtr(f"{save_path}{save_str}{record_lab:08}", c[0], c[1], c[2] - zoffset,
+                  {"Temperature (K)": _host(Level["T0"]), "State (Powder/Solid)": _host(Level["S1"])})
+
+
+def saveFinalResult(Level, save_str, save_path, zoffset):
+    """:1985-2021: as saveResult, file ``{save_path}{save_str}Final.vtr``."""
+    import vtk
+
+    c = [np.asarray(Level["node_coords"][d], dtype=np.float64) for d in range(3)]
+    vtk.write_vtr(f"{save_path}{save_str}Final", c[0], c[1], c[2] - zoffset,
+                  {"Temperature (K)": _host(Level["T0"]), "State (Powder/Solid)": _host(Level["S1"])})
+
+
+def saveState(Level, save_str, record_lab, save_path, zoffset):
+    """:2024-2057: S1 only (Level 0 written as its one-byte store)."""
+    import vtk
+
+    c = [np.asarray(Level["node_coords"][d], dtype=np.float64) for d in range(3)]
+    s1 = Level.engine.L0 if isinstance(Level, LevelView) and Level.lev == 0 else Level["S1"]
+    vtk.write_vtr(f"{save_path}{save_str}{record_lab:08}", c[0], c[1], c[2] - zoffset,
+                  {"State (Powder/Solid)": _host(s1)})
+
+
+def saveResults(Levels, Nonmesh, savenum):
+    """:3668-3682."""
+    if Nonmesh["output_files"] == 1:
+        if savenum == 1 or (np.mod(savenum, Nonmesh["Level1_record_step"]) == 1
+                            or Nonmesh["Level1_record_step"] == 1):
+            saveResult(Levels[1], "Level1_", savenum, Nonmesh["save_path"], 2e-3)
+        saveResult(Levels[2], "Level2_", savenum, Nonmesh["save_path"], 1e-3)
+        saveResult(Levels[3], "Level3_", savenum, Nonmesh["save_path"], 0)
+        print(f"Saved Levels_{savenum:08}")
+
+
+def saveResultsFinal(Levels, Nonmesh):
+    """:3685-3693."""
+    if Nonmesh["output_files"] == 1:
+        saveFinalResult(Levels[1], "Level1_", Nonmesh["save_path"], 2e-3)
+        saveFinalResult(Levels[2], "Level2_", Nonmesh["save_path"], 1e-3)
+        saveFinalResult(Levels[3], "Level3_", Nonmesh["save_path"], 0)
+        print("Saved Final Results")
+
+
 def save_object(obj, filename):
     with open(filename, "wb") as f:
         pickle.dump(obj, f, pickle.HIGHEST_PROTOCOL)

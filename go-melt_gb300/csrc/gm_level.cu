@@ -22,7 +22,10 @@
 // CTA writes (TX-1) x (BY-1) node columns.
 #include <math.h>
 
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "gm_common.cuh"
 
@@ -135,7 +138,7 @@ constexpr int LF_L1 = LF_BOX | LF_SURF | LF_CLAMP | LF_INACT | LF_BC1 | LF_PHIN 
 //   corner values are carried in registers.  Staged phase bits: bit0/1 the
 //   new S1/S2, bit2 the old S2 (melt-time reset).
 template <typename real, int TX, int BY, int FL>
-__global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
+__device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by, int bz) {
   constexpr bool G = (FL & LF_GENERIC) != 0;
   constexpr int PX = TX + 1, PY = BY + 1, NP = PX * PY, NT = TX * BY;
   static_assert(TX == 16 || TX == 32, "a tile row is a warp or a half-warp");
@@ -161,8 +164,8 @@ __global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int nxy = nx * ny;
-  const int X0 = blockIdx.x * (TX - 1), Y0 = blockIdx.y * (BY - 1);
-  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  const int X0 = bx * (TX - 1), Y0 = by * (BY - 1);
+  const int Z0 = bz * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
   const int subs = a.substrate > (long long)nxy * nz ? nxy * nz : (int)a.substrate;
   const real dt = (real)(*a.dt);
   const real inv_dt = (real)1 / dt;
@@ -450,6 +453,41 @@ __global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step
   }
 }
 
+template <typename real, int TX, int BY, int FL>
+__global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
+  level_body<real, TX, BY, FL>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Many level windows (instances of uneven sizes) in one launch: instance b
+// owns the linear blocks [first[b], first[b+1]) of the grid, laid out
+// (bx, by, bz) with bx fastest over its own tiles; its parameters are read
+// from tab[b] into shared memory once per block.
+template <typename real, int TX, int BY, int FL>
+__global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2)
+    level_step_batched_kernel(const LevelK<real>* __restrict__ tab, const int* __restrict__ first, int nb) {
+  __shared__ LevelK<real> sa;
+  __shared__ int sb[3];
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const int blk = blockIdx.x;
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {  // last instance with first[b] <= blk
+      const int mid = (lo + hi + 1) >> 1;
+      if (first[mid] <= blk)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    sa = tab[lo];
+    const int local = blk - first[lo];
+    const int gx = cdiv(sa.nx, TX - 1), gy = cdiv(sa.ny, BY - 1);
+    sb[0] = local % gx;
+    sb[1] = (local / gx) % gy;
+    sb[2] = local / (gx * gy);
+  }
+  __syncthreads();
+  level_body<real, TX, BY, FL>(sa, sb[0], sb[1], sb[2]);
+}
+
 // Tile of one CTA: 32 x 8 element columns (31 x 7 output node columns).
 // Measured on the 161 x 161 x 41-node Level-3 window against 16 x 16 tiles
 // over z-chunks of 4..41 planes: 17.1 us (32 x 8, 14 planes) vs 17.4 us
@@ -511,19 +549,63 @@ static int level_flags(const gm_level_args* g) {
   return f;
 }
 
-template <typename real, int FL>
-static void launch_variant(const LevelK<real>& a, int zc_req, cudaStream_t st) {
-  const int gx = cdiv(a.nx, LT_X - 1), gy = cdiv(a.ny, LT_Y - 1);
-  int zc = zc_req > 0 ? zc_req : auto_zchunk<real, LT_X, LT_Y, FL>(gx * gy, a.nz);
+// Launch shapes measured by gm_level_autotune, per (dtype, feature flags
+// without melt time, grid); gm_level_step uses them when the caller leaves
+// zchunk at 0.
+struct TuneKey {
+  int dtype, flags, nx, ny, nz;
+  bool operator<(const TuneKey& o) const {
+    if (dtype != o.dtype) return dtype < o.dtype;
+    if (flags != o.flags) return flags < o.flags;
+    if (nx != o.nx) return nx < o.nx;
+    if (ny != o.ny) return ny < o.ny;
+    return nz < o.nz;
+  }
+};
+struct TuneVal {
+  int tile_x, zchunk;
+};
+static std::map<TuneKey, TuneVal> g_tuned;
+static std::mutex g_tuned_mutex;
+
+static bool tuned_shape(const TuneKey& k, TuneVal* v) {
+  std::lock_guard<std::mutex> lock(g_tuned_mutex);
+  auto it = g_tuned.find(k);
+  if (it == g_tuned.end()) return false;
+  *v = it->second;
+  return true;
+}
+
+template <typename real, int FL, int TXv, int BYv>
+static void launch_shape(const LevelK<real>& a, int zc_req, cudaStream_t st) {
+  const int gx = cdiv(a.nx, TXv - 1), gy = cdiv(a.ny, BYv - 1);
+  int zc = zc_req > 0 ? zc_req : auto_zchunk<real, TXv, BYv, FL>(gx * gy, a.nz);
   if (zc > ZMAX) zc = ZMAX;
   LevelK<real> b = a;
   b.zchunk = zc;
-  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(LT_X, LT_Y);
-  level_step_kernel<real, LT_X, LT_Y, FL><<<grid, block, 0, st>>>(b);
+  dim3 grid(gx, gy, cdiv(a.nz, zc)), block(TXv, BYv);
+  level_step_kernel<real, TXv, BYv, FL><<<grid, block, 0, st>>>(b);
+}
+
+// tile_x 0: tuned shape if any, else 32 x 8 with the z-chunk model.
+template <typename real, int FL>
+static void launch_variant(const LevelK<real>& a, int zc_req, cudaStream_t st, int tile_x = 0, int dtype = 0,
+                           int flags = 0) {
+  if (tile_x == 0 && zc_req <= 0) {
+    TuneVal v;
+    if (tuned_shape(TuneKey{dtype, flags & ~LF_ACCUM, a.nx, a.ny, a.nz}, &v)) {
+      tile_x = v.tile_x;
+      zc_req = v.zchunk;
+    }
+  }
+  if (tile_x == 16)
+    launch_shape<real, FL, 16, 16>(a, zc_req, st);
+  else
+    launch_shape<real, FL, LT_X, LT_Y>(a, zc_req, st);
 }
 
 template <typename real>
-static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st) {
+static LevelK<real> make_levelk(const gm_level_args* g, const gm_props* pr) {
   LevelK<real> a;
   a.nx = g->nx;
   a.ny = g->ny;
@@ -575,30 +657,119 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   a.inv_d2 = 1.0 / (d * d);
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
+  a.zchunk = g->zchunk;
+  return a;
+}
 
-  switch (level_flags(g)) {
+// The feature combination of a call: one of the specialised instantiations,
+// or the generic one.
+static int variant_of(int flags) {
+  return (flags == LF_L3 || flags == LF_L3ACC || flags == LF_L2 || flags == LF_L1) ? flags : LF_GENERIC;
+}
+
+template <typename real>
+static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st, int tile_x = 0, int zc = 0) {
+  const LevelK<real> a = make_levelk<real>(g, pr);
+  const int fl = level_flags(g);
+  if (zc <= 0) zc = g->zchunk;
+  switch (variant_of(fl)) {
     case LF_L3:
-      launch_variant<real, LF_L3>(a, g->zchunk, st);
+      launch_variant<real, LF_L3>(a, zc, st, tile_x, g->dtype, fl);
       break;
     case LF_L3ACC:
-      launch_variant<real, LF_L3ACC>(a, g->zchunk, st);
+      launch_variant<real, LF_L3ACC>(a, zc, st, tile_x, g->dtype, fl);
       break;
     case LF_L2:
-      launch_variant<real, LF_L2>(a, g->zchunk, st);
+      launch_variant<real, LF_L2>(a, zc, st, tile_x, g->dtype, fl);
       break;
     case LF_L1:
-      launch_variant<real, LF_L1>(a, g->zchunk, st);
+      launch_variant<real, LF_L1>(a, zc, st, tile_x, g->dtype, fl);
       break;
     default:
-      launch_variant<real, LF_GENERIC>(a, g->zchunk, st);
+      launch_variant<real, LF_GENERIC>(a, zc, st, tile_x, g->dtype, fl);
   }
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
-}  // namespace gm
+// Batched launches (32 x 8 tiles).  The descriptor buffer holds a small
+// header {nb, dtype, variant, total blocks}, the per-instance LevelK array
+// and the block prefix first[nb + 1]; a launch reads only device memory, so
+// it can be captured in a CUDA graph and replayed.
+struct BatchHeader {
+  int nb, dtype, variant, blocks;
+};
+static size_t batch_tab_offset() { return 256; }
+template <typename real>
+static size_t batch_first_offset(int nb) {
+  return (batch_tab_offset() + sizeof(LevelK<real>) * nb + 255) / 256 * 256;
+}
 
-extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream) {
-  if (!a || !p || !a->T_in || !a->T_out || !a->dt || a->T_in == a->T_out) return GM_ERR_ARG;
+template <typename real>
+static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, void* desc, long long desc_bytes,
+                           cudaStream_t st, BatchHeader* hdr) {
+  std::vector<LevelK<real>> tabs(nb);
+  const int fl = level_flags(&g[0]);
+  std::vector<int> first(nb + 1);
+  first[0] = 0;
+  // one z-chunk for the whole batch: the cost model over all instances'
+  // tiles together (a lone small window would be split much finer)
+  long long tiles = 0;
+  int nzmax = 1;
+  for (int b = 0; b < nb; ++b) {
+    tiles += (long long)cdiv(g[b].nx, LT_X - 1) * cdiv(g[b].ny, LT_Y - 1);
+    nzmax = max(nzmax, g[b].nz);
+  }
+  const int zc_batch =
+      auto_zchunk<real, LT_X, LT_Y, LF_GENERIC>((int)min(tiles, (long long)(1 << 30)), nzmax);
+  for (int b = 0; b < nb; ++b) {
+    if (level_flags(&g[b]) != fl) return GM_ERR_ARG;
+    LevelK<real>& a = tabs[b];
+    a = make_levelk<real>(&g[b], &p[b]);
+    if (a.zchunk <= 0) a.zchunk = zc_batch;
+    if (a.zchunk > ZMAX) a.zchunk = ZMAX;
+    const long long blocks = (long long)cdiv(a.nx, LT_X - 1) * cdiv(a.ny, LT_Y - 1) * cdiv(a.nz, a.zchunk);
+    if (first[b] + blocks >= (1LL << 31)) return GM_ERR_TOO_LARGE;
+    first[b + 1] = first[b] + (int)blocks;
+  }
+  const size_t off = batch_first_offset<real>(nb);
+  if ((long long)(off + sizeof(int) * (nb + 1)) > desc_bytes) return GM_ERR_TOO_LARGE;
+  *hdr = BatchHeader{nb, g[0].dtype, variant_of(fl), first[nb]};
+  // pageable sources: each copy returns once the host data has been consumed
+  if (cudaMemcpyAsync(desc, hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync((char*)desc + batch_tab_offset(), tabs.data(), sizeof(LevelK<real>) * nb,
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync((char*)desc + off, first.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st) !=
+          cudaSuccess)
+    return GM_ERR_CUDA;
+  return GM_OK;
+}
+
+template <typename real>
+static int launch_batched(const BatchHeader& h, const void* desc, cudaStream_t st) {
+  const LevelK<real>* tab = (const LevelK<real>*)((const char*)desc + batch_tab_offset());
+  const int* first = (const int*)((const char*)desc + batch_first_offset<real>(h.nb));
+  const dim3 blk(LT_X, LT_Y);
+  switch (h.variant) {
+    case LF_L3:
+      level_step_batched_kernel<real, LT_X, LT_Y, LF_L3><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
+      break;
+    case LF_L3ACC:
+      level_step_batched_kernel<real, LT_X, LT_Y, LF_L3ACC><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
+      break;
+    case LF_L2:
+      level_step_batched_kernel<real, LT_X, LT_Y, LF_L2><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
+      break;
+    case LF_L1:
+      level_step_batched_kernel<real, LT_X, LT_Y, LF_L1><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
+      break;
+    default:
+      level_step_batched_kernel<real, LT_X, LT_Y, LF_GENERIC><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
+  }
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+static int check_level_args(const gm_level_args* a) {
+  if (!a || !a->T_in || !a->T_out || !a->dt || a->T_in == a->T_out) return GM_ERR_ARG;
   if (a->nx < 2 || a->ny < 2 || a->nz < 2 || a->ne_planes < 0 || a->ne_planes > a->nz - 1) return GM_ERR_ARG;
   if ((long long)a->nx * a->ny * a->nz >= (1LL << 31)) return GM_ERR_TOO_LARGE;  // node ids are 32-bit
   if ((a->k_arr == nullptr) != (a->rc_arr == nullptr)) return GM_ERR_ARG;
@@ -606,10 +777,122 @@ extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* st
   if (a->bc_mode == 3 && (!a->bc_new || !a->bc_old)) return GM_ERR_ARG;
   if (a->bc_mode < 0 || a->bc_mode > 3) return GM_ERR_ARG;
   if ((a->accum == nullptr) != (a->max_accum == nullptr)) return GM_ERR_ARG;
+  if (a->dtype != GM_F32 && a->dtype != GM_F64) return GM_ERR_ARG;
+  return GM_OK;
+}
+
+}  // namespace gm
+
+extern "C" int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream) {
+  if (!p) return GM_ERR_ARG;
+  const int rc = gm::check_level_args(a);
+  if (rc != GM_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (a->dtype == GM_F32) return gm::launch_level<float>(a, p, st);
-  if (a->dtype == GM_F64) return gm::launch_level<double>(a, p, st);
+  return gm::launch_level<double>(a, p, st);
+}
+
+extern "C" long long gm_level_batched_desc_size(int nb, int dtype) {
+  if (nb < 1) return -1;
+  const size_t off = dtype == GM_F64 ? gm::batch_first_offset<double>(nb) : gm::batch_first_offset<float>(nb);
+  return (long long)(off + sizeof(int) * (nb + 1));
+}
+
+extern "C" int gm_level_batched_prepare(const gm_level_args* a, int nb, const gm_props* p, void* desc,
+                                        long long desc_bytes, gm_batch_info* info, void* stream) {
+  if (!a || !p || !desc || nb < 1 || !info) return GM_ERR_ARG;
+  for (int b = 0; b < nb; ++b) {
+    const int rc = gm::check_level_args(&a[b]);
+    if (rc != GM_OK) return rc;
+    if (a[b].dtype != a[0].dtype) return GM_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  gm::BatchHeader h;
+  const int rc = a[0].dtype == GM_F32 ? gm::prepare_batched<float>(a, nb, p, desc, desc_bytes, st, &h)
+                                      : gm::prepare_batched<double>(a, nb, p, desc, desc_bytes, st, &h);
+  if (rc != GM_OK) return rc;
+  info->nb = h.nb;
+  info->dtype = h.dtype;
+  info->variant = h.variant;
+  info->blocks = h.blocks;
+  return GM_OK;
+}
+
+extern "C" int gm_level_batched_launch(const void* desc, const gm_batch_info* info, void* stream) {
+  if (!desc || !info || info->nb < 1 || info->blocks < 1) return GM_ERR_ARG;
+  const gm::BatchHeader h{info->nb, info->dtype, info->variant, info->blocks};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (h.dtype == GM_F32) return gm::launch_batched<float>(h, desc, st);
+  if (h.dtype == GM_F64) return gm::launch_batched<double>(h, desc, st);
   return GM_ERR_ARG;
+}
+
+extern "C" int gm_level_step_batched(const gm_level_args* a, int nb, const gm_props* p, void* desc,
+                                     long long desc_bytes, void* stream) {
+  gm_batch_info info;
+  const int rc = gm_level_batched_prepare(a, nb, p, desc, desc_bytes, &info, stream);
+  if (rc != GM_OK) return rc;
+  return gm_level_batched_launch(desc, &info, stream);
+}
+
+extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out,
+                                 void* stream) {
+  if (!p || reps < 1) return GM_ERR_ARG;
+  const int rc = gm::check_level_args(a);
+  if (rc != GM_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return GM_ERR_CUDA;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return GM_ERR_CUDA;
+  }
+  gm_level_args b = *a;
+  gm::TuneVal best{0, 0};
+  float best_us = -1.f;
+  int status = GM_OK;
+  const int tiles[2] = {gm::LT_X, 16};
+  for (int ti = 0; ti < 2 && status == GM_OK; ++ti) {
+    int last = -1;
+    for (int nch = gm::cdiv(a->nz, gm::ZMAX); nch <= a->nz && status == GM_OK; ++nch) {
+      const int zc = gm::cdiv(a->nz, nch);
+      if (zc == last || zc < 2) continue;
+      last = zc;
+      b.zchunk = zc;
+      for (int r = -1; r < reps && status == GM_OK; ++r) {  // one untimed launch first
+        if (r == 0) cudaEventRecord(e0, st);
+        status = a->dtype == GM_F32 ? gm::launch_level<float>(&b, p, st, tiles[ti], zc)
+                                    : gm::launch_level<double>(&b, p, st, tiles[ti], zc);
+      }
+      if (status != GM_OK) break;
+      cudaEventRecord(e1, st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        status = GM_ERR_CUDA;
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const float us = 1000.f * ms / reps;
+      if (best_us < 0 || us < best_us) {
+        best_us = us;
+        best = gm::TuneVal{tiles[ti], zc};
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status != GM_OK) return status;
+  {
+    std::lock_guard<std::mutex> lock(gm::g_tuned_mutex);
+    gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a) & ~gm::LF_ACCUM, a->nx, a->ny, a->nz}] = best;
+  }
+  if (out) {
+    out->tile_x = best.tile_x;
+    out->tile_y = best.tile_x == 16 ? 16 : gm::LT_Y;
+    out->zchunk = best.zchunk;
+    out->us = best_us;
+  }
+  return GM_OK;
 }
 
 extern "C" const char* gm_version(void) { return "gomelt-gb300 0.1 (sm_103a)"; }

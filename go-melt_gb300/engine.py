@@ -296,6 +296,34 @@ class Engine:
         self._l0_gather(t["l0_2"], n2, self.ph[2], None, None, None)
         return move_v
 
+    def autotune(self, row, reps=5):
+        """Measure the launch shape (tile, z-chunk) of the Level-3, Level-2 and
+        Level-1 steps as the subcycle issues them (gm_level_autotune); later
+        level steps of the same shapes use the fastest.  Needs the tables of a
+        move; writes only scratch outputs; synchronises the stream.  Returns
+        {level: (tile_x, tile_y, zchunk, us)}."""
+        g = self.geo
+        t = self.tables
+        if t is None:
+            raise N.GomeltError("autotune needs a move first")
+        rowd = torch.as_tensor(np.asarray(row, dtype=np.float64), device=self.dev)
+        out = {}
+        for lev in (3, 2, 1):
+            L = g.L[lev]
+            To = self._buf(f"tuneT{lev}", L.nn)
+            Po = self._buf(f"tunePh{lev}", L.nn, torch.uint8)
+            if lev == 3:
+                kw = self.level_kwargs(3, self.T[3], To, rowd[5:6], self.ph[3], Po, laser=rowd,
+                                       ring=self._ring(3, self.T[2], self.T[2]), alpha=0.5)
+            else:
+                cg = t["c32"] if lev == 2 else t["c21"]
+                box = [v for d in range(3) for v in (cg.box_lo[d], cg.box_lo[d] + cg.box_n[d])]
+                rhs = self._buf("rhs2" if lev == 2 else "rhs1", int(np.prod(cg.box_n)))
+                extra = dict(ring=self._ring(2, self.T[1], self.T[1]), alpha=0.5) if lev == 2 else {}
+                kw = self.level_kwargs(lev, self.T[lev], To, rowd[5:6], self.ph[lev], Po, rhs=rhs, box=box, **extra)
+            out[lev] = kern.level_autotune(self.ps, reps=reps, stream=self.stream, **kw)
+        return out
+
     def _l0_gather(self, idx, n, ph_out, prev_ph, prev_lo, prev_n):
         a = N.gm_l0_args()
         for d in range(3):
@@ -343,8 +371,12 @@ class Engine:
         N.call("gm_ring_prolong", C.byref(a), kern.stream_ptr(self.stream))
         return outA, outB
 
-    def _level(self, lev, T_in, T_out, dt, ph_in, ph_out, *, rhs=None, box=None, laser=None, bc_new=None,
-               bc_old=None, alpha=0.0, accum=False, clamp=True, ring=None):
+    def _level(self, lev, T_in, T_out, dt, ph_in, ph_out, **kw):
+        kern.level_step(self.ps, stream=self.stream, **self.level_kwargs(lev, T_in, T_out, dt, ph_in, ph_out, **kw))
+
+    def level_kwargs(self, lev, T_in, T_out, dt, ph_in, ph_out, *, rhs=None, box=None, laser=None, bc_new=None,
+                     bc_old=None, alpha=0.0, accum=False, clamp=True, ring=None):
+        """Arguments of kern.level_args for one level step of level `lev`."""
         g = self.geo
         L = g.L[lev]
         kw = {}
@@ -361,10 +393,9 @@ class Engine:
             kw.update(bc_mode=2, bc_new=bc_new, bc_old=bc_old, bc_alpha=alpha, bc_beta=1.0 - alpha, bc_map=m)
         if accum:
             kw.update(accum=self.acc3, max_accum=self.macc3)
-        kern.level_step(self.ps, T_in=T_in, T_out=T_out, nodes=L.nodes, h=L.spacing(), origin=L.origin(),
-                        ne_planes=ne_planes, dt=dt, ph_in=ph_in, ph_out=ph_out, substrate=self.substrate[lev],
-                        rhs_box=rhs, box=box, laser=laser, surface=1, clamp=1 if clamp else 0, stream=self.stream,
-                        **kw)
+        return dict(T_in=T_in, T_out=T_out, nodes=L.nodes, h=L.spacing(), origin=L.origin(), ne_planes=ne_planes,
+                    dt=dt, ph_in=ph_in, ph_out=ph_out, substrate=self.substrate[lev], rhs_box=rhs, box=box,
+                    laser=laser, surface=1, clamp=1 if clamp else 0, **kw)
 
     def _couple(self, cg, fine_lev, out, out_lo, out_n, *, T, ph, Tp=None, dTa=None, dTb=None, dt=None):
         g = self.geo

@@ -25,8 +25,8 @@ import torch
 
 from computeFunctions import (  # noqa: F401
     SetupLevels, SetupNonmesh, SetupProperties, calcStaticTmpNodesAndElements, getStaticNodesAndElements,
-    getStaticSubcycle, getSubstrateNodes, moveEverything, printLevelMaxMin, stepGOMELT, stepGOMELTDwellTime,
-    subcycleGOMELT)
+    getStaticSubcycle, getSubstrateNodes, moveEverything, printLevelMaxMin, saveResults, saveResultsFinal,
+    saveState, stepGOMELT, stepGOMELTDwellTime, subcycleGOMELT)
 from createPath import count_lines, parsingGcode
 
 
@@ -83,6 +83,8 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
 
     time_inc = record_inc = wait_inc = 0
     t_output = 0.0
+    savenum = int(time_inc / Nonmesh["record_step"]) + 1
+    saveResults(Levels, Nonmesh, savenum)
     laser_prev_z = float("inf")
     dwell_count = 0.0
     acc = AccumStore(eng)
@@ -202,6 +204,8 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
         t_output += float(laser_all[:, 5].sum())
         if record_inc >= Nonmesh["record_step"]:
             record_inc = 0
+            savenum = int(time_inc / Nonmesh["record_step"]) + 1
+            saveResults(Levels, Nonmesh, savenum)
         if Nonmesh["info_T"]:
             printLevelMaxMin(Levels, names)
         tend = time.time()
@@ -209,6 +213,8 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
               % (time_inc, total, t_output, tend - tstart, 1000 * (tend - t_loop),
                  1000 * (tend - tstart) / max(time_inc, 1)))
     fh.close()
+    saveState(Levels[0], "Level0_", Nonmesh["layer_num"], Nonmesh["save_path"], 0)
+    saveResultsFinal(Levels, Nonmesh)
     T = {lv: eng.T[lv].double().cpu().numpy() for lv in (1, 2, 3)}
     np.savez(os.path.join(Nonmesh["save_path"], "FinalTemperatureFields"), L1T=T[1], L2T=T[2], L3T=T[3])
     save_accum(acc, Nonmesh)

@@ -55,11 +55,26 @@ class DeviceMap3:
         self.struct = s
 
 
-def level_step(props: N.gm_props, *, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_out=None,
+def level_step(props: N.gm_props, *, stream=None, **kw):
+    """gm_level_step with the arguments of level_args."""
+    a = level_args(**kw)
+    N.call("gm_level_step", C.byref(a), C.byref(props), stream_ptr(stream))
+
+
+def level_autotune(props: N.gm_props, *, reps=5, stream=None, **kw):
+    """gm_level_autotune for the call level_args(**kw) describes; returns
+    (tile_x, tile_y, zchunk, microseconds)."""
+    a = level_args(**kw)
+    r = N.gm_tune_result()
+    N.call("gm_level_autotune", C.byref(a), C.byref(props), int(reps), C.byref(r), stream_ptr(stream), kernels=0)
+    return r.tile_x, r.tile_y, r.zchunk, r.us
+
+
+def level_args(*, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_out=None,
                substrate=0, k_arr=None, rc_arr=None, F_full=None, corr_full=None, rhs_box=None, box=None,
                laser=None, surface=0, bc_mode=0, face=None, inactive_amb=0, bc_new=None, bc_old=None,
                bc_alpha=0.0, bc_beta=0.0, bc_map: DeviceMap3 | None = None, clamp=0, accum=None, max_accum=None,
-               zchunk=0, stream=None):
+               zchunk=0):
     a = N.gm_level_args()
     a.dtype = dtype_code(T_in)
     a.nx, a.ny, a.nz = (int(x) for x in nodes)
@@ -91,4 +106,4 @@ def level_step(props: N.gm_props, *, T_in, T_out, nodes, h, origin, ne_planes, d
     a.clamp = int(clamp)
     a.accum, a.max_accum = ptr(accum), ptr(max_accum)
     a.zchunk = int(zchunk)
-    N.call("gm_level_step", C.byref(a), C.byref(props), stream_ptr(stream))
+    return a

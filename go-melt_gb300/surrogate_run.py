@@ -46,7 +46,12 @@ def _instance_rows(cfg):
 
     P = levels.setup_properties(cfg["properties"])
     nm = levels.setup_nonmesh(cfg["nonmesh"])
-    rows = np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)
+    if "gcode" in cfg:
+        gcode = cfg["gcode"]
+    else:
+        r = cfg["raster"]
+        gcode = createPath.serpentine_gcode(r["x0"], r["y0"], r["length"], r["hatch"], r["ntracks"])
+    rows = np.asarray(createPath.toolpath(nm, P, gcode), dtype=np.float64)
     return P, nm, rows
 
 

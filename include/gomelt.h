@@ -206,6 +206,43 @@ typedef struct gm_l0_args {
   int prev_lo[3], prev_n[3];
 } gm_l0_args;
 
+/* Many level steps (windows of uneven sizes, e.g. independent scan
+ * instances) in ONE launch: args[b] as for gm_level_step, props[b] per
+ * instance; all with the same dtype and the same features (laser, RHS box,
+ * bc_mode, melt time, ...).  desc: device buffer of at least
+ * gm_level_batched_desc_size(nb, dtype) bytes for the per-instance
+ * descriptors, rewritten in stream order by each call (the host side is
+ * consumed before the call returns).  No counterpart in the reference. */
+long long gm_level_batched_desc_size(int nb, int dtype);
+int gm_level_step_batched(const gm_level_args* args, int nb, const gm_props* props, void* desc,
+                          long long desc_bytes, void* stream);
+
+/* The same in two parts: prepare (host -> desc, stream-ordered copies) and
+ * launch (reads only desc: capturable in a CUDA graph and replayable while
+ * desc is unchanged).  info receives what the launch needs. */
+typedef struct gm_batch_info {
+  int nb, dtype, variant, blocks;
+} gm_batch_info;
+
+int gm_level_batched_prepare(const gm_level_args* args, int nb, const gm_props* props, void* desc,
+                             long long desc_bytes, gm_batch_info* info, void* stream);
+int gm_level_batched_launch(const void* desc, const gm_batch_info* info, void* stream);
+
+/* Autotuner: times gm_level_step for this call over the tile shapes (32 x 8,
+ * 16 x 16) and z-chunks (every distinct split of the node planes) with CUDA
+ * events, `reps` launches each after one untimed launch, and keeps the
+ * fastest for later calls with the same dtype, features and grid that leave
+ * zchunk at 0.  The timed launches write T_out / ph_out / melt time as the
+ * call would (so pass scratch outputs, or tune a call whose repetition is
+ * harmless); synchronises the stream; not for use during stream capture.
+ * No counterpart in the reference. */
+typedef struct gm_tune_result {
+  int tile_x, tile_y, zchunk;
+  float us;
+} gm_tune_result;
+
+int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out, void* stream);
+
 /* Prolongation of one or two coarse fields onto the Dirichlet ring of a fine
  * level (faces x0, x1, y0, y1 and the bottom plane), written at the ring
  * nodes' ids in full-size arrays: outA = I(srcA), outB = I(srcB) (the

@@ -31,6 +31,8 @@ def test_driver_final_fields(case, dtype, tol, tmp_path):
         ref = g[f"final.{k}"]
         err = np.max(np.abs(fin[k] - ref)) / np.max(np.abs(ref))
         assert err < tol, (k, err)
+    # the final Level-0 state file the reference always writes (go_melt.py:501)
+    assert any(f.startswith("Level0_") and f.endswith(".vtr") for f in os.listdir(tmp_path / "out"))
     for f in sorted(os.listdir(tmp_path / "out")):
         if f.startswith("accum_time"):
             ref = g[f"final.{f[:-4]}"]
