@@ -61,6 +61,7 @@ def parse_args():
     ap.add_argument("--train-steps", type=int, default=1500)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
     ap.add_argument("--batched", action="store_true",
                     help="batched single-track instances: per-instance vs batched level launches (CUDA graphs)")
     return ap.parse_args()
@@ -261,6 +262,7 @@ def run_ours(args):
         eng.set_layer(rows[0])
         eng.move(rows[0], vstart)
         tuned = eng.autotune(rows[0])  # launch shapes of the level steps, measured (set-up, untimed)
+        eng.use_graph = not args.no_graph  # each subcycle call as one CUDA graph
 
         def chunk(k):
             return rows[k * n23:(k + 1) * n23]
@@ -396,6 +398,7 @@ def run_ours(args):
                      "traffic": traffic, "kernel": "level_step_kernel (Level 3)", "kernel_ms": k_ms,
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
+        "subcycle_as_cuda_graph": not args.no_graph,
         "autotuned": {f"L{lev}": {"tile": [v[0], v[1]], "zchunk": v[2], "us": round(v[3], 2)}
                       for lev, v in tuned.items()},
     }

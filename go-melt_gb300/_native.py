@@ -175,7 +175,7 @@ class gm_subcycle_plan(C.Structure):
         ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
-        ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2)]
+        ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int)]
 
 
 def subcycle_kernel_count(N2: int, N3: int) -> int:

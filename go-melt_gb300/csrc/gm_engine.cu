@@ -280,8 +280,9 @@ bool plan_ok(const gm_subcycle_plan* p) {
 
 }  // namespace
 
-extern "C" int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
-  if (!plan_ok(p) || !props || (p->dtype != GM_F32 && p->dtype != GM_F64)) return GM_ERR_ARG;
+namespace {
+
+int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
   Ctx c;
   c.p = p;
   c.pr = props;
@@ -345,4 +346,60 @@ extern "C" int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, voi
   l0.ph = p->L3.ph;
   GM_TRY(gm_l0_scatter(&l0, c.st));
   return c.rc;
+}
+
+// Graph mode: the call's launches are captured from the stream, applied to
+// the executable graph of the previous call on this stream (same topology;
+// only parameters change between calls), and launched as one graph.  The
+// first call on a stream issues directly (it fills the launch-shape caches).
+struct GraphSlot {
+  void* stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int calls = 0;
+};
+thread_local GraphSlot g_slots[8];
+
+GraphSlot* slot_for(void* stream) {
+  for (auto& s : g_slots)
+    if (s.calls > 0 && s.stream == stream) return &s;
+  for (auto& s : g_slots)
+    if (s.calls == 0) {
+      s.stream = stream;
+      return &s;
+    }
+  return nullptr;
+}
+
+int subcycle_graph(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
+  GraphSlot* slot = slot_for(stream);
+  if (!slot || slot->calls++ == 0) return subcycle_issue(p, props, stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GM_ERR_CUDA;
+  const int rc = subcycle_issue(p, props, stream);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (rc != GM_OK || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != GM_OK ? rc : GM_ERR_CUDA;
+  }
+  int out = GM_OK;
+  if (slot->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(slot->exec, graph, &info) != cudaSuccess) {
+      cudaGetLastError();  // clear the update failure; instantiate anew
+      cudaGraphExecDestroy(slot->exec);
+      slot->exec = nullptr;
+    }
+  }
+  if (!slot->exec && cudaGraphInstantiate(&slot->exec, graph, 0) != cudaSuccess) out = GM_ERR_CUDA;
+  if (out == GM_OK && cudaGraphLaunch(slot->exec, st) != cudaSuccess) out = GM_ERR_LAUNCH;
+  cudaGraphDestroy(graph);
+  return out;
+}
+
+}  // namespace
+
+extern "C" int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
+  if (!plan_ok(p) || !props || (p->dtype != GM_F32 && p->dtype != GM_F64)) return GM_ERR_ARG;
+  return p->graph ? subcycle_graph(p, props, stream) : subcycle_issue(p, props, stream);
 }

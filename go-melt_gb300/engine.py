@@ -146,6 +146,7 @@ class Engine:
         self.macc3 = torch.zeros(g.L[3].nn, **f)
         self.s2_prev_lo = None  # Level-0 start of the window last written (S2 snapshot)
         self._pending = None  # MovePlan made by plan_move and not yet applied
+        self.use_graph = False  # run gm_subcycle as one CUDA graph per call
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
         self.tmp = None
@@ -320,7 +321,9 @@ class Engine:
                 box = [v for d in range(3) for v in (cg.box_lo[d], cg.box_lo[d] + cg.box_n[d])]
                 rhs = self._buf("rhs2" if lev == 2 else "rhs1", int(np.prod(cg.box_n)))
                 extra = dict(ring=self._ring(2, self.T[1], self.T[1]), alpha=0.5) if lev == 2 else {}
-                kw = self.level_kwargs(lev, self.T[lev], To, rowd[5:6], self.ph[lev], Po, rhs=rhs, box=box, **extra)
+                # the subcycle's Level-1 steps keep the phase (no phase output)
+                kw = self.level_kwargs(lev, self.T[lev], To, rowd[5:6], self.ph[lev], Po if lev == 2 else None,
+                                       rhs=rhs, box=box, **extra)
             out[lev] = kern.level_autotune(self.ps, reps=reps, stream=self.stream, **kw)
         return out
 
@@ -577,6 +580,7 @@ class Engine:
         p.zchunk = int(getattr(self, "zchunk", 0))
         p.ring2[0], p.ring2[1] = self._buf("ring2a", nn2).data_ptr(), self._buf("ring2b", nn2).data_ptr()
         p.ring3[0], p.ring3[1] = self._buf("ring3a", nn3).data_ptr(), self._buf("ring3b", nn3).data_ptr()
+        p.graph = 1 if self.use_graph else 0
         return p
 
     # ------------------------------------------------------------------

@@ -427,6 +427,9 @@ typedef struct gm_subcycle_plan {
   int zchunk;                /* level-kernel tuning (0: automatic) */
   void* ring2[2];            /* work: Level-2 ring prolongations (nn2 each) */
   void* ring3[2];            /* work: Level-3 ring prolongations (nn3 each) */
+  int graph;                 /* 1: capture the call's launches and run them as one CUDA graph, updated in
+                                place from call to call on the same stream (the first call on a stream
+                                issues directly) */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
