@@ -69,28 +69,44 @@ struct ConvK {
 
 constexpr int CV_WARPS = 8;
 
+// Voxel rows per warp: MT m16 tiles, so that a warp's accumulators stay at
+// 64 registers (MT * COUT / 8 * 4) and every weight fragment read from shared
+// memory feeds MT MMAs.
+template <int COUT>
+struct ConvShape {
+  static constexpr int NT = COUT / 8;
+  static constexpr int MT = NT >= 16 ? 1 : (16 / NT > 4 ? 4 : 16 / NT);
+  static constexpr int ROWS = 16 * MT;  // voxels per warp
+};
+
 template <int COUT>
 __global__ void __launch_bounds__(CV_WARPS * 32) conv3_kernel(const ConvK a) {
-  constexpr int NT = COUT / 8;
+  constexpr int NT = ConvShape<COUT>::NT, MT = ConvShape<COUT>::MT;
   extern __shared__ uint32_t smw[];  // one tap: COUT rows of (cin + 8) bf16
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int rs = (a.cin + 8) / 2;  // row stride in 32-bit words
   const long long V = (long long)a.g.B * a.g.X * a.g.Y * a.g.Z;
-  const long long v0 = ((long long)blockIdx.x * CV_WARPS + warp) * 16;
-  long long vr[2];
-  int xr[2], yr[2], zr[2];
-  long long br[2];
-  bool ok[2];
+  const long long v0 = ((long long)blockIdx.x * CV_WARPS + warp) * (16 * MT);
+  // per row: packed (x, y, z) (10 bits each; -1 when the row is past the end)
+  // and the first voxel of its sample (voxel counts < 2^31)
+  int xyz[MT][2], br[MT][2];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    vr[h] = v0 + g + 8 * h;
-    ok[h] = vr[h] < V;
-    vox_xyz(a.g, ok[h] ? vr[h] : 0, xr[h], yr[h], zr[h], br[h]);
-  }
-  float acc[NT][4];
+  for (int m = 0; m < MT; ++m)
 #pragma unroll
-  for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+    for (int h = 0; h < 2; ++h) {
+      const long long v = v0 + 16 * m + g + 8 * h;
+      int x, y, z;
+      long long b;
+      vox_xyz(a.g, v < V ? v : 0, x, y, z, b);
+      xyz[m][h] = v < V ? (x | (y << 10) | (z << 20)) : -1;
+      br[m][h] = (int)b;
+    }
+  float acc[MT][NT][4];
+#pragma unroll
+  for (int m = 0; m < MT; ++m)
+#pragma unroll
+    for (int n = 0; n < NT; ++n) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.f;
   const int kc = a.cin / 16;
   for (int tap = 0; tap < 27; ++tap) {
     __syncthreads();  // previous tap's weights are no longer read
@@ -103,52 +119,62 @@ __global__ void __launch_bounds__(CV_WARPS * 32) conv3_kernel(const ConvK a) {
     __syncthreads();
     const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
     const int sx = a.mirror ? -dx : dx, sy = a.mirror ? -dy : dy, sz = a.mirror ? -dz : dz;
-    const uint32_t* src[2];
+    const uint32_t* src[MT][2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int x = xr[h] + sx, y = yr[h] + sy, z = zr[h] + sz;
-      const bool in = ok[h] && x >= 0 && x < a.g.X && y >= 0 && y < a.g.Y && z >= 0 && z < a.g.Z;
-      const long long nb = br[h] + x + (long long)a.g.X * (y + (long long)a.g.Y * z);
-      src[h] = in ? reinterpret_cast<const uint32_t*>(a.in + nb * a.in_stride + a.in_off) : nullptr;
-    }
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int p = xyz[m][h];
+        const int x = (p & 1023) + sx, y = ((p >> 10) & 1023) + sy, z = ((p >> 20) & 1023) + sz;
+        const bool in = p >= 0 && x >= 0 && x < a.g.X && y >= 0 && y < a.g.Y && z >= 0 && z < a.g.Z;
+        const long long nb = br[m][h] + x + (long long)a.g.X * (y + (long long)a.g.Y * z);
+        src[m][h] = in ? reinterpret_cast<const uint32_t*>(a.in + nb * a.in_stride + a.in_off) : nullptr;
+      }
     for (int c = 0; c < kc; ++c) {
-      uint32_t af[4];
-      af[0] = src[0] ? src[0][c * 8 + t] : 0u;
-      af[1] = src[1] ? src[1][c * 8 + t] : 0u;
-      af[2] = src[0] ? src[0][c * 8 + 4 + t] : 0u;
-      af[3] = src[1] ? src[1][c * 8 + 4 + t] : 0u;
+      uint32_t af[MT][4];
+#pragma unroll
+      for (int m = 0; m < MT; ++m) {
+        af[m][0] = src[m][0] ? src[m][0][c * 8 + t] : 0u;
+        af[m][1] = src[m][1] ? src[m][1][c * 8 + t] : 0u;
+        af[m][2] = src[m][0] ? src[m][0][c * 8 + 4 + t] : 0u;
+        af[m][3] = src[m][1] ? src[m][1][c * 8 + 4 + t] : 0u;
+      }
 #pragma unroll
       for (int n = 0; n < NT; ++n) {
         const uint32_t* wr = smw + (n * 8 + g) * rs + c * 8;
-        mma16816(acc[n], af, wr[t], wr[4 + t]);
+        const uint32_t b0 = wr[t], b1 = wr[4 + t];
+#pragma unroll
+        for (int m = 0; m < MT; ++m) mma16816(acc[m][n], af[m], b0, b1);
       }
     }
   }
   // epilogue: bias, ReLU, mask, BF16 store
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    if (!ok[h]) continue;
-    const long long v = vr[h];
+  for (int m = 0; m < MT; ++m)
 #pragma unroll
-    for (int n = 0; n < NT; ++n) {
-      const int co = n * 8 + 2 * t;
-      float y0 = acc[n][2 * h], y1 = acc[n][2 * h + 1];
-      if (a.bias) {
-        y0 += a.bias[co];
-        y1 += a.bias[co + 1];
+    for (int h = 0; h < 2; ++h) {
+      if (xyz[m][h] < 0) continue;
+      const long long v = v0 + 16 * m + g + 8 * h;
+#pragma unroll
+      for (int n = 0; n < NT; ++n) {
+        const int co = n * 8 + 2 * t;
+        float y0 = acc[m][n][2 * h], y1 = acc[m][n][2 * h + 1];
+        if (a.bias) {
+          y0 += a.bias[co];
+          y1 += a.bias[co + 1];
+        }
+        if (a.relu) {
+          y0 = fmaxf(y0, 0.f);
+          y1 = fmaxf(y1, 0.f);
+        }
+        if (a.mask) {
+          const uint32_t mk = *reinterpret_cast<const uint32_t*>(a.mask + v * a.mask_stride + a.mask_off + co);
+          if (bf2f((uint16_t)(mk & 0xffffu)) <= 0.f) y0 = 0.f;
+          if (bf2f((uint16_t)(mk >> 16)) <= 0.f) y1 = 0.f;
+        }
+        *reinterpret_cast<uint32_t*>(a.out + v * a.out_stride + a.out_off + co) = pack_bf16(y0, y1);
       }
-      if (a.relu) {
-        y0 = fmaxf(y0, 0.f);
-        y1 = fmaxf(y1, 0.f);
-      }
-      if (a.mask) {
-        const uint32_t m = *reinterpret_cast<const uint32_t*>(a.mask + v * a.mask_stride + a.mask_off + co);
-        if (bf2f((uint16_t)(m & 0xffffu)) <= 0.f) y0 = 0.f;
-        if (bf2f((uint16_t)(m >> 16)) <= 0.f) y1 = 0.f;
-      }
-      *reinterpret_cast<uint32_t*>(a.out + v * a.out_stride + a.out_off + co) = pack_bf16(y0, y1);
     }
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -517,6 +543,8 @@ extern "C" int gm_unet_conv3(const gm_conv_args* c, void* stream) {
   if (c->mask && (c->mask_off % 2 || c->mask_stride % 2 || c->cout + c->mask_off > c->mask_stride)) return GM_ERR_ARG;
   for (int d = 0; d < 4; ++d)
     if (c->grid[d] < 1) return GM_ERR_ARG;
+  if (c->grid[1] > 1023 || c->grid[2] > 1023 || c->grid[3] > 1023) return GM_ERR_TOO_LARGE;
+  if ((long long)c->grid[0] * c->grid[1] * c->grid[2] * c->grid[3] >= (1LL << 31)) return GM_ERR_TOO_LARGE;
   ConvK a;
   a.g = grid5(c->grid);
   a.cin = c->cin;
@@ -534,17 +562,18 @@ extern "C" int gm_unet_conv3(const gm_conv_args* c, void* stream) {
   a.mask = (const uint16_t*)c->mask;
   a.out = (uint16_t*)c->out;
   const long long V = (long long)a.g.B * a.g.X * a.g.Y * a.g.Z;
-  const long long blocks = (V + CV_WARPS * 16 - 1) / (CV_WARPS * 16);
   const size_t smem = (size_t)c->cout * (c->cin + 8) * 2;
   cudaStream_t st = (cudaStream_t)stream;
 #define GM_CONV_CASE(N)                                                                                   \
-  case N:                                                                                                 \
+  case N: {                                                                                               \
+    const long long rows = (long long)CV_WARPS * ConvShape<N>::ROWS;                                      \
     if (smem > 48 * 1024 &&                                                                               \
         cudaFuncSetAttribute(conv3_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != \
             cudaSuccess)                                                                                  \
       return GM_ERR_LAUNCH;                                                                               \
-    conv3_kernel<N><<<(unsigned)blocks, CV_WARPS * 32, smem, st>>>(a);                                    \
-    break;
+    conv3_kernel<N><<<(unsigned)((V + rows - 1) / rows), CV_WARPS * 32, smem, st>>>(a);                   \
+    break;                                                                                                \
+  }
   switch (c->cout) {
     GM_CONV_CASE(16)
     GM_CONV_CASE(32)
