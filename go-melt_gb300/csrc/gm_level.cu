@@ -118,12 +118,13 @@ enum : int {
   LF_BC3 = 1 << 10,
   LF_PHIN = 1 << 11,
   LF_PHOUT = 1 << 12,
+  LF_CONST = 1 << 13,  // k and rho*c independent of phase and temperature
   LF_GENERIC = 1 << 20
 };
 constexpr int LF_L3 = LF_LASER | LF_SURF | LF_CLAMP | LF_BC3 | LF_PHIN | LF_PHOUT;  // Level-3 step
 constexpr int LF_L3ACC = LF_L3 | LF_ACCUM;                                         // ... with melt time
 constexpr int LF_L2 = LF_BOX | LF_SURF | LF_CLAMP | LF_BC3 | LF_PHIN | LF_PHOUT;   // Level-2 step
-constexpr int LF_L1 = LF_BOX | LF_SURF | LF_CLAMP | LF_INACT | LF_BC1 | LF_PHIN | LF_PHOUT;  // Level-1 step
+constexpr int LF_L1 = LF_BOX | LF_SURF | LF_CLAMP | LF_INACT | LF_BC1 | LF_PHIN;  // Level-1 step (phase kept)
 
 // Pipeline per CTA (one barrier per node plane):
 //   two shared-memory slots of staged node planes (T, k, rho*c, phase bits),
@@ -160,6 +161,7 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
   const bool hPhin = G ? a.ph_in != nullptr : (FL & LF_PHIN) != 0;
   const bool hPhout = G ? a.ph_out != nullptr : (FL & LF_PHOUT) != 0;
   const int bcm = G ? a.bc_mode : ((FL & LF_BC1) ? 1 : ((FL & LF_BC3) ? 3 : 0));
+  constexpr bool kConst = (FL & LF_CONST) != 0;  // element means of k and rho*c are the constants
 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
@@ -207,7 +209,13 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
         uint32_t ph = 0;
         if (pin && sbase[s] >= 0) {
           const int id = sbase[s] + pl * nxy;
-          ph = node_props_sel(P, pfT[s], pfP[s], id < subs, k, c) | ((pfP[s] & PH_S2) << 1);
+          if (kConst) {  // phase bits only
+            const bool s2 = pfT[s] >= P.T_liquidus;
+            const bool s1 = (pfP[s] & PH_S1) || s2 || id < subs;
+            ph = (s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u) | ((pfP[s] & PH_S2) << 1);
+          } else {
+            ph = node_props_sel(P, pfT[s], pfP[s], id < subs, k, c) | ((pfP[s] & PH_S2) << 1);
+          }
           if (hKarr) {
             k = a.k_arr[id];
             c = a.rc_arr[id];
@@ -271,8 +279,10 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
   for (int c = 0; c < 4; ++c) {
     const V4<real> r = sN[0][c00 + (c >> 1) * PX + (c & 1)];
     fl[c] = r.x;
-    ksl += r.y;
-    csl += r.z;
+    if (!kConst) {
+      ksl += r.y;
+      csl += r.z;
+    }
     if (c == 3) phl = real_bits(r.w);
   }
   tl3 = fl[3];
@@ -291,8 +301,10 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
     for (int c = 0; c < 4; ++c) {
       const V4<real> r = sN[PAR ^ 1][c00 + (c >> 1) * PX + (c & 1)];
       tu[c] = r.x;
-      ksu += r.y;
-      csu += r.z;
+      if (!kConst) {
+        ksu += r.y;
+        csu += r.z;
+      }
       if (c == 3) phu = real_bits(r.w);
     }
     store(ke + 2, PAR);
@@ -334,8 +346,8 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
       for (int c = 1; c < 4; ++c) R[c] = fl[c] + fu[c];
 #pragma unroll
       for (int c = 0; c < 4; ++c) R[4 + c] = fu[c] - fl[c];
-      const real kbar = (ksl + ksu) * (real)0.125;
-      me = a.wvol * ((csl + csu) * (real)0.125) * inv_dt;
+      const real kbar = kConst ? P.k_fluid : (ksl + ksu) * (real)0.125;
+      me = kConst ? a.wvol * (P.rho * P.cp_fluid) * inv_dt : a.wvol * ((csl + csu) * (real)0.125) * inv_dt;
 #pragma unroll
       for (int m = 1; m < 8; ++m) R[m] *= a.lam[m] * kbar;
       bfly_inv(R);
@@ -531,8 +543,16 @@ static int auto_zchunk(int tiles_xy, int nz) {
   return best;
 }
 
-static int level_flags(const gm_level_args* g) {
+// k and rho*c the same in every phase and independent of T (the products of
+// computeStateProperties then select one constant).
+static bool props_const(const gm_props* p) {
+  return p && p->k_powder == p->k_bulk_a0 && p->k_fluid == p->k_bulk_a0 && p->k_bulk_a1 == 0.0 &&
+         p->cp_solid_a1 == 0.0 && p->cp_mushy == p->cp_solid_a0 && p->cp_fluid == p->cp_solid_a0;
+}
+
+static int level_flags(const gm_level_args* g, const gm_props* p) {
   int f = 0;
+  if (!g->k_arr && props_const(p)) f |= LF_CONST;
   if (g->laser) f |= LF_LASER;
   if (g->rhs_box) f |= LF_BOX;
   if (g->F_full || g->corr_full) f |= LF_FULL;
@@ -664,27 +684,33 @@ static LevelK<real> make_levelk(const gm_level_args* g, const gm_props* pr) {
 // The feature combination of a call: one of the specialised instantiations,
 // or the generic one.
 static int variant_of(int flags) {
-  return (flags == LF_L3 || flags == LF_L3ACC || flags == LF_L2 || flags == LF_L1) ? flags : LF_GENERIC;
+  const int b = flags & ~LF_CONST;
+  return (b == LF_L3 || b == LF_L3ACC || b == LF_L2 || b == LF_L1) ? flags : LF_GENERIC;
 }
+
+// One case per specialised variant (with and without constant properties).
+#define GM_LEVEL_VARIANTS(X) \
+  X(LF_L3)                   \
+  X(LF_L3ACC)                \
+  X(LF_L2)                   \
+  X(LF_L1)                   \
+  X(LF_L3 | LF_CONST)        \
+  X(LF_L3ACC | LF_CONST)     \
+  X(LF_L2 | LF_CONST)        \
+  X(LF_L1 | LF_CONST)
 
 template <typename real>
 static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st, int tile_x = 0, int zc = 0) {
   const LevelK<real> a = make_levelk<real>(g, pr);
-  const int fl = level_flags(g);
+  const int fl = level_flags(g, pr);
   if (zc <= 0) zc = g->zchunk;
   switch (variant_of(fl)) {
-    case LF_L3:
-      launch_variant<real, LF_L3>(a, zc, st, tile_x, g->dtype, fl);
-      break;
-    case LF_L3ACC:
-      launch_variant<real, LF_L3ACC>(a, zc, st, tile_x, g->dtype, fl);
-      break;
-    case LF_L2:
-      launch_variant<real, LF_L2>(a, zc, st, tile_x, g->dtype, fl);
-      break;
-    case LF_L1:
-      launch_variant<real, LF_L1>(a, zc, st, tile_x, g->dtype, fl);
-      break;
+#define GM_CASE(V)                                            \
+  case V:                                                     \
+    launch_variant<real, V>(a, zc, st, tile_x, g->dtype, fl); \
+    break;
+    GM_LEVEL_VARIANTS(GM_CASE)
+#undef GM_CASE
     default:
       launch_variant<real, LF_GENERIC>(a, zc, st, tile_x, g->dtype, fl);
   }
@@ -708,7 +734,7 @@ template <typename real>
 static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, void* desc, long long desc_bytes,
                            cudaStream_t st, BatchHeader* hdr) {
   std::vector<LevelK<real>> tabs(nb);
-  const int fl = level_flags(&g[0]);
+  const int fl = level_flags(&g[0], &p[0]);
   std::vector<int> first(nb + 1);
   first[0] = 0;
   // one z-chunk for the whole batch: the cost model over all instances'
@@ -722,7 +748,7 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
   const int zc_batch =
       auto_zchunk<real, LT_X, LT_Y, LF_GENERIC>((int)min(tiles, (long long)(1 << 30)), nzmax);
   for (int b = 0; b < nb; ++b) {
-    if (level_flags(&g[b]) != fl) return GM_ERR_ARG;
+    if (level_flags(&g[b], &p[b]) != fl) return GM_ERR_ARG;
     LevelK<real>& a = tabs[b];
     a = make_levelk<real>(&g[b], &p[b]);
     if (a.zchunk <= 0) a.zchunk = zc_batch;
@@ -750,18 +776,12 @@ static int launch_batched(const BatchHeader& h, const void* desc, cudaStream_t s
   const int* first = (const int*)((const char*)desc + batch_first_offset<real>(h.nb));
   const dim3 blk(LT_X, LT_Y);
   switch (h.variant) {
-    case LF_L3:
-      level_step_batched_kernel<real, LT_X, LT_Y, LF_L3><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
-      break;
-    case LF_L3ACC:
-      level_step_batched_kernel<real, LT_X, LT_Y, LF_L3ACC><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
-      break;
-    case LF_L2:
-      level_step_batched_kernel<real, LT_X, LT_Y, LF_L2><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
-      break;
-    case LF_L1:
-      level_step_batched_kernel<real, LT_X, LT_Y, LF_L1><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
-      break;
+#define GM_CASE(V)                                                                              \
+  case V:                                                                                       \
+    level_step_batched_kernel<real, LT_X, LT_Y, V><<<h.blocks, blk, 0, st>>>(tab, first, h.nb); \
+    break;
+    GM_LEVEL_VARIANTS(GM_CASE)
+#undef GM_CASE
     default:
       level_step_batched_kernel<real, LT_X, LT_Y, LF_GENERIC><<<h.blocks, blk, 0, st>>>(tab, first, h.nb);
   }
@@ -884,7 +904,7 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
   if (status != GM_OK) return status;
   {
     std::lock_guard<std::mutex> lock(gm::g_tuned_mutex);
-    gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a) & ~gm::LF_ACCUM, a->nx, a->ny, a->nz}] = best;
+    gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a, p) & ~gm::LF_ACCUM, a->nx, a->ny, a->nz}] = best;
   }
   if (out) {
     out->tile_x = best.tile_x;
