@@ -150,7 +150,8 @@ class gm_couple_args(C.Structure):
 class gm_coarse_source_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("geom", gm_couple_geom), ("npos", C.c_int), ("rows", vp),
                 ("xq", C.POINTER(C.c_double) * 3), ("fine_wq", C.c_double), ("out", vp), ("out_lo", C.c_int * 3),
-                ("out_n", C.c_int * 3), ("scratch", vp), ("scratch_cap", C.c_longlong)]
+                ("out_n", C.c_int * 3), ("scratch", vp), ("scratch_cap", C.c_longlong), ("ngroups", C.c_int),
+                ("out_group_stride", C.c_longlong)]
 
 
 class gm_window(C.Structure):
@@ -174,16 +175,16 @@ class gm_subcycle_plan(C.Structure):
         ("L0_ny", C.c_longlong), ("l0_idx3", _P_INT * 3), ("rows", vp), ("dts", vp), ("T1p", vp), ("T1c", vp),
         ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
-        ("src_scratch", vp), ("src_cap", C.c_longlong), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
+        ("src_scratch", vp), ("src_cap", C.c_longlong), ("src2", vp), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
         ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int)]
 
 
 def subcycle_kernel_count(N2: int, N3: int) -> int:
-    """Kernels gm_subcycle launches: set-up and Level 1 (8), two passes of a
-    Level-2 ring prolongation plus N2 Level-2 steps (coupling 2, source 2,
-    Level-2 solve, Level-3 ring, N3 Level-3 solves, restriction, T'), the
-    T'2/mass/corrector block (7) and the tail (3)."""
-    return 18 + 2 * (1 + N2 * (8 + N3))
+    """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
+    Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
+    steps (coupling 2, Level-2 solve, Level-3 ring, N3 Level-3 solves,
+    restriction, T'), the T'2/mass/corrector block (7) and the tail (3)."""
+    return 20 + 2 * (1 + N2 * (6 + N3))
 
 
 _lib = None

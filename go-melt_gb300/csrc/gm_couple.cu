@@ -62,6 +62,7 @@ struct CoupleK {
   const double* dt;
   real wq;
   real cf[3];  // -2 wq / (H_d h_d): constant factor of the flux term along axis d
+  int kconst;  // k and rho*c independent of phase and temperature: no per-node properties
   real* partials;
   long long nitems;
   int nchunk;
@@ -145,8 +146,8 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
         const int lx = i % S1, ly = (i / S1) % S1, lz = i / S2;
         if (lx <= nbx && ly <= nby && lz <= nbz) {
           const int id = (e0x + lx) + (e0y + ly) * a.fnx + (e0z + lz) * fnxy;
-          real k, c;
-          node_props_sel(a.p, a.T[id], a.ph ? (uint32_t)a.ph[id] : 0u, id < a.substrate, k, c);
+          real k = a.p.k_fluid, c = a.p.rho * a.p.cp_fluid;
+          if (!a.kconst) node_props_sel(a.p, a.T[id], a.ph ? (uint32_t)a.ph[id] : 0u, id < a.substrate, k, c);
           if (a.k_arr) {
             k = a.k_arr[id];
             c = a.rc_arr[id];
@@ -356,24 +357,27 @@ __global__ void coarse_source_tables(int np, const double* rows, int n0, int n1,
   }
 }
 
+// Group g of ng (np rows each) is averaged into out + g * gstride.
 template <typename real>
-__global__ void coarse_source_assemble(int np, const double* rows, int n0, int n1, int n2, int lo0, int lo1, int lo2,
-                                       const real* S, double cpre, real* out, int ob0, int ob1, int ob2, int on0,
-                                       int on1) {
+__global__ void coarse_source_assemble(int np, int ng, long long gstride, const double* rows, int n0, int n1, int n2,
+                                       int lo0, int lo1, int lo2, const real* S, double cpre, real* out, int ob0,
+                                       int ob1, int ob2, int on0, int on1) {
   const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
-  const long long tot = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+  const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nodes * ng;
        t += (long long)gridDim.x * blockDim.x) {
-    const int bx = (int)(t % (n0 + 1)), by = (int)((t / (n0 + 1)) % (n1 + 1)),
-              bz = (int)(t / ((long long)(n0 + 1) * (n1 + 1)));
+    const int g = (int)(t / nodes);
+    const long long u = t - g * nodes;
+    const int bx = (int)(u % (n0 + 1)), by = (int)((u / (n0 + 1)) % (n1 + 1)),
+              bz = (int)(u / ((long long)(n0 + 1) * (n1 + 1)));
     real s = 0;
-    for (int p = 0; p < np; ++p) {
+    for (int p = g * np; p < (g + 1) * np; ++p) {
       const real c = (real)(cpre * rows[p * 7 + 6]);
       const real* Sp = S + (long long)p * per;
       s += c * Sp[bx] * Sp[n0 + 1 + by] * Sp[n0 + 1 + n1 + 1 + bz];
     }
     const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
-    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += s / (real)np;
+    out[g * gstride + gx + (long long)gy * on0 + (long long)gz * on0 * on1] += s / (real)np;
   }
 }
 
@@ -441,6 +445,8 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
   a.partials = (real*)g->partials;
   a.nitems = (long long)a.ax[0].ncb * a.ax[1].ncb * a.ax[2].ncb * a.nchunk;
   a.p = make_props<real>(*pr);
+  a.kconst = !g->k_arr && pr->k_powder == pr->k_bulk_a0 && pr->k_fluid == pr->k_bulk_a0 && pr->k_bulk_a1 == 0.0 &&
+             pr->cp_solid_a1 == 0.0 && pr->cp_mushy == pr->cp_solid_a0 && pr->cp_fluid == pr->cp_solid_a0;
   long long blocks = (a.nitems + 3) / 4;
   if (blocks > 152 * 16) blocks = 152 * 16;
   couple_kernel<real><<<(int)blocks, 128, 0, st>>>(a);
@@ -489,9 +495,11 @@ static int do_source(const gm_coarse_source_args* g, const gm_props* pr, cudaStr
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   const double cpre = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * g->fine_wq;
   const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
-  coarse_source_assemble<real><<<grid1(nodes), 256, 0, st>>>(
-      g->npos, g->rows, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo, (const real*)g->scratch, cpre,
-      (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1]);
+  const int ng = g->ngroups > 1 ? g->ngroups : 1;
+  coarse_source_assemble<real><<<grid1(nodes * ng), 256, 0, st>>>(
+      g->npos / ng, ng, g->out_group_stride, g->rows, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo,
+      (const real*)g->scratch, cpre, (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0],
+      g->out_n[1]);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
@@ -499,6 +507,9 @@ extern "C" int gm_coarse_source(const gm_coarse_source_args* g, const gm_props* 
   if (!g || !p || !geom_ok(&g->geom) || !g->rows || g->npos < 1 || !g->out || !g->scratch) return GM_ERR_ARG;
   if (!g->xq[0] || !g->xq[1] || !g->xq[2]) return GM_ERR_ARG;
   if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
+  if (g->ngroups > 1 && (g->npos % g->ngroups ||
+                         g->out_group_stride < (long long)g->out_n[0] * g->out_n[1] * g->out_n[2]))
+    return GM_ERR_ARG;
   const gm_couple_geom& G = g->geom;
   const long long need = (long long)g->npos * ((G.ax[0].ncb + 1) + (G.ax[1].ncb + 1) + (G.ax[2].ncb + 1));
   if (need > g->scratch_cap) return GM_ERR_TOO_LARGE;

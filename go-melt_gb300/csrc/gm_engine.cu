@@ -129,7 +129,7 @@ void couple_fields(Ctx& c, const gm_couple_geom& g, const gm_window& fine, const
 }
 
 void source(Ctx& c, const gm_couple_geom& g, const double* const xq[3], const double* rows, int npos, void* out,
-            const int lo[3], const int n[3]) {
+            const int lo[3], const int n[3], int ngroups = 1, long long group_stride = 0) {
   const gm_subcycle_plan& p = *c.p;
   gm_coarse_source_args a;
   memset(&a, 0, sizeof(a));
@@ -146,6 +146,8 @@ void source(Ctx& c, const gm_couple_geom& g, const double* const xq[3], const do
   a.out = out;
   a.scratch = p.src_scratch;
   a.scratch_cap = p.src_cap;
+  a.ngroups = ngroups;
+  a.out_group_stride = group_stride;
   GM_TRY(gm_coarse_source(&a, c.pr, c.st));
 }
 
@@ -229,12 +231,11 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
   for (int l2 = 0; l2 < N2; ++l2) {
     void* hist_l2 = at(p.tp3hist, l2 * n3, c.esz);
     const double* dt2 = p.dts + 1 + l2;
-    memzero(c, p.rhs2, nrhs2);
+    copy(c, p.rhs2, at(p.src2, l2 * nrhs2, c.esz), nrhs2 * c.esz);  // the step's source (computed once)
     if (part2)
       couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, hist_l2, Tp3c, dt2);
     else
       couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, nullptr, nullptr, nullptr);
-    source(c, p.c32, p.xq32, p.rows + (long long)l2 * N3 * 7, N3, p.rhs2, p.rhs2_lo, p.rhs2_n);
     void* T2n = p.T2w[l2 % 2];
     uint8_t* ph2n = p.ph2w[l2 % 2];
     level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 3, nullptr,
@@ -272,7 +273,8 @@ bool plan_ok(const gm_subcycle_plan* p) {
   if (!p->L2.Tp || !p->L3.Tp || !p->acc3 || !p->macc3) return false;
   if (!p->T1p || !p->T1c || !p->T2w[0] || !p->T2w[1] || !p->T3w[0] || !p->T3w[1] || !p->tp3w[0] || !p->tp3w[1] ||
       !p->Tp2w || !p->rhs1 || !p->rhs2 || !p->tp3hist || !p->ph2w[0] || !p->ph2w[1] || !p->ph3w[0] || !p->ph3w[1] ||
-      !p->partials || !p->src_scratch || !p->L0 || !p->ring2[0] || !p->ring2[1] || !p->ring3[0] || !p->ring3[1])
+      !p->partials || !p->src_scratch || !p->L0 || !p->ring2[0] || !p->ring2[1] || !p->ring3[0] || !p->ring3[1] ||
+      !p->src2)
     return false;
   if ((p->L2all == nullptr) != (p->L3all == nullptr) || (p->L2all == nullptr) != (p->L3pall == nullptr)) return false;
   return true;
@@ -306,6 +308,11 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   s1.coarse_ph = p->L1.ph;
   s1.substrate = p->L1.substrate;
   GM_TRY(gm_restrict_s1(&s1, c.st));
+
+  // Level-2 sources of all N2 steps (mean over each step's N3 rows), once
+  const long long nrhs2 = (long long)p->rhs2_n[0] * p->rhs2_n[1] * p->rhs2_n[2];
+  memzero(c, p->src2, nrhs2 * p->N2);
+  source(c, p->c32, p->xq32, p->rows, p->N2 * p->N3, p->src2, p->rhs2_lo, p->rhs2_n, p->N2, nrhs2);
 
   // Level-1 right-hand side and predictor
   memzero(c, p->rhs1, nrhs1);

@@ -465,8 +465,15 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
   }
 }
 
+// Resident CTAs per SM: 4 for the FP32 constant-property variants (they fit
+// 64 registers without spills), else 3 (FP32) or 2 (FP64).
+template <typename real, int FL>
+constexpr int level_min_blocks() {
+  return sizeof(real) != 4 ? 2 : ((FL & LF_CONST) ? 4 : 3);
+}
+
 template <typename real, int TX, int BY, int FL>
-__global__ void __launch_bounds__(TX * BY, sizeof(real) == 4 ? 3 : 2) level_step_kernel(const LevelK<real> a) {
+__global__ void __launch_bounds__(TX * BY, level_min_blocks<real, FL>()) level_step_kernel(const LevelK<real> a) {
   level_body<real, TX, BY, FL>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 

@@ -572,9 +572,10 @@ class Engine:
         p.ph3w[0], p.ph3w[1] = pu(self._buf("ph3a", nn3, u8)), pu(self._buf("ph3b", nn3, u8))
         part = self._work["partials"]
         p.partials, p.partials_cap = part.data_ptr(), part.numel()
-        ns = max(N2 * N3 * sum(c31.box_n), N3 * sum(c32.box_n))
+        ns = N2 * N3 * max(sum(c31.box_n), sum(c32.box_n))
         scr = self._buf("srcscratch", ns)
         p.src_scratch, p.src_cap = scr.data_ptr(), scr.numel()
+        p.src2 = self._buf("src2", N2 * int(np.prod(c32.box_n))).data_ptr()
         if out_hist is not None:
             p.L2all, p.L3all, p.L3pall = (t.data_ptr() for t in out_hist)
         p.zchunk = int(getattr(self, "zchunk", 0))

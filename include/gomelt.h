@@ -364,6 +364,11 @@ typedef struct gm_coarse_source_args {
   int out_lo[3], out_n[3];
   void* scratch;
   long long scratch_cap;
+  /* ngroups > 1: the npos rows are ngroups consecutive groups of equal size,
+   * each averaged into its own output box at out + g * out_group_stride
+   * elements (one launch pair for several coarse steps); 0 or 1: one group. */
+  int ngroups;
+  long long out_group_stride;
 } gm_coarse_source_args;
 
 int gm_coarse_source(const gm_coarse_source_args* a, const gm_props* p, void* stream);
@@ -421,6 +426,7 @@ typedef struct gm_subcycle_plan {
   long long partials_cap;
   void* src_scratch;         /* scratch of gm_coarse_source */
   long long src_cap;
+  void* src2;                /* work: the N2 Level-2 source boxes of the call (N2 * rhs2 box values) */
   void* L2all;               /* optional (N2*nn2): Level-2 T after each corrector Level-2 step */
   void* L3all;               /* optional (N2*nn3): Level-3 T */
   void* L3pall;              /* optional (N2*nn3): Level-3 T' */

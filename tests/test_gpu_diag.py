@@ -104,3 +104,37 @@ def test_field_error():
     m, r = dg.field_error(torch.tensor(a, dtype=torch.float32, device="cuda"), torch.tensor(b, device="cuda"))
     rm, rr = D_oracle.field_error(a.astype(np.float32), b)
     assert abs(m - rm) <= 1e-12 * max(rm, 1) and abs(r - rr) <= 1e-9 * rr
+
+
+def test_energy_balance_closes_on_plain_steps():
+    """On the plain multilevel path (single-track workload, constant
+    properties) every Level-2 step's Level-3 window balances its energy far
+    inside the 1 % acceptance threshold of a predicted field."""
+    import createPath
+    import engine
+    import levels
+    import workloads
+    from diagnostics import Diagnostics
+
+    cfg = workloads.config0()
+    P = levels.setup_properties(cfg["properties"])
+    nm = levels.setup_nonmesh(cfg["nonmesh"])
+    rows = np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    e = engine.Engine(cfg, P, 10, 10)
+    e.set_layer(rows[0])
+    dg = Diagnostics()
+    res = []
+    for k in range(3):
+        c = rows[k * 100:(k + 1) * 100]
+        e.move(c[0], vstart)
+        T3s = e.T[3].clone()
+        _, L3all, _ = e.subcycle(c, history=True)
+        L3 = e.geo.L[3]
+        for j in range(10):
+            jr = c[j * 10:(j + 1) * 10]
+            t = dg.energy_terms(e.ps, nodes=L3.nodes, h=L3.spacing(), origin=L3.origin(),
+                                ne_planes=L3.nodes[2] - 1, T0=T3s if j == 0 else L3all[j - 1], T1=L3all[j],
+                                ph=e.ph[3], substrate=e.substrate[3], interval=float(jr[:, 5].sum()), rows=jr)
+            res.append(dg.residual(t, jr, P["laser_eta"]))
+    assert max(res[10:]) < 2e-3, res
