@@ -307,27 +307,38 @@ def run_ours(args):
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        e2e_ms = 0.0
+        # One step deep pipeline through the public API: step i+1 is issued
+        # (its table upload and host rows H2D included) before step i's peak
+        # temperature, copied to pinned memory, is read back and checked.  The
+        # 512 MB L2 flush runs inside the timed region before every step.
         mm_e2e = 0.0
         h2d = 0
+        peak = torch.empty(args.steps, dtype=eng.T[3].dtype, pin_memory=True)
+        done = []
         t0 = time.perf_counter()
         plan = eng.plan_move(chunk(k)[0], vstart)
-        e2e_ms += 1000.0 * (time.perf_counter() - t0)
         for i in range(args.steps):
             flush.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
             c = chunk(k + i)
             eng.move(c[0], vstart, plan)
             eng.subcycle(c)
-            # host half of the next move while this step runs on the device
-            plan = eng.plan_move(chunk(k + i + 1)[0], vstart)
-            tmax = float(eng.T[3].max().item())  # the driver's per-chunk temperature check
-            e2e_ms += 1000.0 * (time.perf_counter() - t0)
+            peak[i:i + 1].copy_(eng.T[3].max().reshape(1), non_blocking=True)  # the per-chunk temperature check
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            done.append(ev)
+            plan = eng.plan_move(chunk(k + i + 1)[0], vstart)  # host half of the next move, device busy
+            if i > 0:
+                done[i - 1].synchronize()
+                tmax = float(peak[i - 1])
+                if not np.isfinite(tmax) or tmax > 1e5:
+                    raise SystemExit(f"non-finite or invalid temperature {tmax}")
             mm_e2e += scan_mm(c)
             h2d += eng.last_table_bytes + 8 * (n23 * 7 + N2 + 1)
-            if not np.isfinite(tmax) or tmax > 1e5:
-                raise SystemExit(f"non-finite or invalid temperature {tmax}")
+        done[-1].synchronize()
+        tmax = float(peak[args.steps - 1])
+        e2e_ms = 1000.0 * (time.perf_counter() - t0)
+        if not np.isfinite(tmax) or tmax > 1e5:
+            raise SystemExit(f"non-finite or invalid temperature {tmax}")
         eng.move(chunk(k + args.steps)[0], vstart, plan)
         k += args.steps + 1
 
@@ -389,7 +400,9 @@ def run_ours(args):
         "dtype": "f32" if dtype == torch.float32 else "f64", "data": "synthetic (generated G-code raster)",
         "config": {"workload": "part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, L3 160x160x40 @5um, "
                                "first layer, N2=N3=10, dt3=1.575us",
-                   "step": "moveEverything + subcycleGOMELT (100 fine steps)", "l2": "flushed between steps",
+                   "step": "moveEverything + subcycleGOMELT (100 fine steps)",
+                   "l2": "flushed between steps (value: untimed; e2e: inside the timed region)",
+                   "e2e": "host rows and tables H2D per step, peak-T D2H per step read one step later",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": mm_e2e / (e2e_ms * 1e-3), "unit": "mm/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": 4 if dtype == torch.float32 else 8},

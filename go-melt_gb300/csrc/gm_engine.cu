@@ -378,6 +378,7 @@ GraphSlot* slot_for(void* stream) {
 }
 
 int subcycle_graph(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
+  if (!stream) return subcycle_issue(p, props, stream);  // the legacy default stream cannot be captured
   GraphSlot* slot = slot_for(stream);
   if (!slot || slot->calls++ == 0) return subcycle_issue(p, props, stream);
   cudaStream_t st = (cudaStream_t)stream;
