@@ -38,6 +38,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "go-melt_gb300"))
 
 L2_FLUSH_BYTES = 512 << 20
+WORKLOAD_NAME = ("part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, L3 160x160x40 @5um, "
+                 "first layer, N2=N3=10, dt3=1.575us")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_FILE = os.path.join(ROOT, "profiles", "level_step_l3_config1.txt")
 
@@ -62,6 +64,9 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
+    ap.add_argument("--unet-only", action="store_true",
+                    help="surrogate kernels alone: forward passes on the part-scale grid and training steps "
+                         "(for profiling)")
     ap.add_argument("--batched", action="store_true",
                     help="batched single-track instances: per-instance vs batched level launches (CUDA graphs)")
     return ap.parse_args()
@@ -205,24 +210,47 @@ def oracle_sample(cfg, rows, nsteps, warm=1):
     return mm / dt, dt, nsteps
 
 
+def _oracle_worker(job):
+    start, nsteps, warm = job
+    cfg, P, nm, rows = workload()
+    v, secs, n = oracle_sample(cfg, rows[start:], nsteps, warm=warm)
+    return v * secs, secs, n
+
+
+def oracle_parallel(nsteps, warm, workers=None):
+    """The oracle sample on every host core: `workers` single-threaded
+    processes (spawned), each stepping its own segment of the toolpath.
+    Returns (mm/s over all workers, wall seconds of the slowest, steps per
+    worker, workers)."""
+    import multiprocessing as mp
+
+    workers = workers or os.cpu_count() or 1
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[k] = "1"
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_oracle_worker, [(w * 500, nsteps, warm) for w in range(workers)])
+    mm = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return mm / wall, wall, nsteps, workers
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    cfg, P, nm, rows = workload()
-    v, secs, n = oracle_sample(cfg, rows, args.steps, warm=max(1, args.warmup))
-    cores = 1
+    v, secs, n, cores = oracle_parallel(args.steps, max(1, args.warmup))
     line = {
         "impl": "reference", "metric": "simulated scan mm per wall-s (plain multilevel explicit step)", "value": v,
         "unit": "mm/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * secs / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (generated G-code raster)",
-        "config": {"workload": "part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, "
-                               "L3 160x160x40 @5um, first layer", "sample": "fine-level steps"},
+        "config": {"workload": WORKLOAD_NAME, "step": "moveEverything + subcycleGOMELT (100 fine steps)",
+                   "sample": "Level-3 fine steps on every host core"},
         "cpu_baseline": {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} Level-3 steps of the NumPy FP64 oracle (props, source, surface flux, "
-                                   f"solve, Dirichlet ring, clamp) along the toolpath; Level-1/2 work and "
-                                   f"coupling terms excluded, so this overstates the CPU rate"},
+                         "sample": f"{cores} processes x {n} Level-3 steps of the NumPy FP64 oracle (props, "
+                                   f"source, surface flux, solve, Dirichlet ring, clamp), each on its own "
+                                   f"toolpath segment; Level-1/2 work and coupling terms excluded, so this "
+                                   f"overstates the CPU rate"},
         "e2e": {"value": v, "unit": "mm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -398,8 +426,7 @@ def run_ours(args):
         "value": mm / (t_ms * 1e-3), "unit": "mm/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if dtype == torch.float32 else "f64", "data": "synthetic (generated G-code raster)",
-        "config": {"workload": "part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, L3 160x160x40 @5um, "
-                               "first layer, N2=N3=10, dt3=1.575us",
+        "config": {"workload": WORKLOAD_NAME,
                    "step": "moveEverything + subcycleGOMELT (100 fine steps)",
                    "l2": "flushed between steps (value: untimed; e2e: inside the timed region)",
                    "e2e": "host rows and tables H2D per step, peak-T D2H per step read one step later",
@@ -424,10 +451,10 @@ def run_ours(args):
                               "L3_peak_K": chk["L3_peak_K"],
                               "what": "same steps from the same start in FP32 and FP64 on this GPU"}
     if not args.no_cpu_baseline and ws == 1:
-        v, secs, n = oracle_sample(cfg, rows, args.cpu_steps)
-        line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": 1, "kind": "port",
-                                "sample": f"{n} Level-3 steps of the NumPy FP64 oracle ({secs:.1f} s); Level-1/2 "
-                                          f"work and coupling terms excluded"}
+        v, secs, n, cores = oracle_parallel(args.cpu_steps, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
+                                "sample": f"{cores} processes x {n} Level-3 steps of the NumPy FP64 oracle "
+                                          f"({secs:.1f} s); Level-1/2 work and coupling terms excluded"}
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
@@ -676,6 +703,47 @@ def run_batched(args):
     print(json.dumps(out), flush=True)
 
 
+def run_unet_only(args):
+    """The surrogate's kernels alone (the case the ncu summary of the
+    convolution uses): --steps forward passes on the 160 x 160 x 40 grid,
+    then --steps training steps of batch 4 on 80 x 80 x 20 grids (random
+    inputs), timed with CUDA events."""
+    import torch
+
+    import surrogate
+
+    dev = torch.device("cuda", 0)
+    net = surrogate.UNet(dev, seed=0)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    out = {"unet_only": True}
+    for name, grid, train in (("inference", (1, 160, 160, 40), False), ("training", (4, 80, 80, 20), True)):
+        V = grid[0] * grid[1] * grid[2] * grid[3]
+        x = torch.zeros(V, 16, dtype=torch.bfloat16)
+        x[:, :6] = torch.randn(V, 6, generator=g).to(torch.bfloat16)
+        x = x.to(dev)
+        tgt = torch.randn(V, generator=g).to(dev) * 0.01
+        msk = torch.ones(V, device=dev)
+
+        def step():
+            net.forward(x, grid)
+            if train:
+                net.backward(tgt, msk, 1.0 / V)
+                net.step(lr=1e-4)
+
+        step()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(args.steps):
+            step()
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / args.steps
+        fl = net.flops(grid) * (3 if train else 1)
+        out[name] = {"grid": list(grid), "ms": ms, "tflops": fl / (ms * 1e-3) / 1e12}
+    print(json.dumps(out), flush=True)
+
+
 def run_kernel_only(args):
     """The dominant kernel alone on the workload's Level-3 window after
     --warmup subcycle calls (the case the ncu summaries under profiles/ use)."""
@@ -707,6 +775,8 @@ def main():
     args = parse_args()
     if args.kernel_only:
         run_kernel_only(args)
+    elif args.unet_only:
+        run_unet_only(args)
     elif args.precision:
         run_precision(args)
     elif args.surrogate:
