@@ -195,18 +195,30 @@ struct WgradK {
 };
 
 constexpr int WG_WARPS = 8;
-constexpr int WG_KV = 32;  // voxels staged per step
+constexpr int WG_KV = 64;  // voxels staged per step
+
+// Four 8x8 BF16 blocks from shared memory, transposed (thread (g, t) receives
+// rows 2t, 2t+1 of column g of each block): the K-strided operands of the
+// weight-gradient GEMM as mma fragments.
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const uint16_t* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
 
 // Warp tiles: 16 output channels (co) x NB8 * 8 input channels (ci); up to
-// four tiles per warp, statically indexed.
+// four tiles per warp, statically indexed.  Voxel tiles of dY and the
+// tap-shifted X are staged with rows padded to a 16-byte multiple, so every
+// fragment comes from one ldmatrix.trans.
 template <int NB8>
 __global__ void __launch_bounds__(WG_WARPS * 32) wgrad_kernel(const WgradK a) {
-  extern __shared__ uint16_t sm[];
+  extern __shared__ __align__(16) uint16_t sm[];
   const int tap = blockIdx.y, split = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int cin = a.cin, cout = a.cout;
-  const int sdy = cout + 2, sx = cin + 2;  // padded row strides (bf16)
+  const int sdy = cout + 8, sx = cin + 8;  // row strides (bf16), multiples of 8
   uint16_t* sDy = sm;
   uint16_t* sX = sm + WG_KV * sdy;
   const long long V = (long long)a.g.B * a.g.X * a.g.Y * a.g.Z;
@@ -218,6 +230,8 @@ __global__ void __launch_bounds__(WG_WARPS * 32) wgrad_kernel(const WgradK a) {
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int n = 0; n < NB8; ++n) acc[i][n][0] = acc[i][n][1] = acc[i][n][2] = acc[i][n][3] = 0.f;
+  // ldmatrix row addresses: lane l supplies row (l & 7) of block (l >> 3)
+  const int lr = lane & 7, lb = lane >> 3;
   for (long long v0 = vb; v0 < ve; v0 += WG_KV) {
     __syncthreads();
     for (int r = warp; r < WG_KV; r += WG_WARPS) {
@@ -236,16 +250,10 @@ __global__ void __launch_bounds__(WG_WARPS * 32) wgrad_kernel(const WgradK a) {
           srcx = reinterpret_cast<const uint32_t*>(
               a.in + (base + x + (long long)a.g.X * (y + (long long)a.g.Y * z)) * a.in_stride + a.in_off);
       }
-      for (int c = lane; c < cout / 2; c += 32) {
-        const uint32_t val = srcd ? srcd[c] : 0u;
-        sDy[r * sdy + 2 * c] = (uint16_t)(val & 0xffffu);
-        sDy[r * sdy + 2 * c + 1] = (uint16_t)(val >> 16);
-      }
-      for (int c = lane; c < cin / 2; c += 32) {
-        const uint32_t val = srcx ? srcx[c] : 0u;
-        sX[r * sx + 2 * c] = (uint16_t)(val & 0xffffu);
-        sX[r * sx + 2 * c + 1] = (uint16_t)(val >> 16);
-      }
+      uint32_t* dd = reinterpret_cast<uint32_t*>(sDy + r * sdy);
+      uint32_t* dxs = reinterpret_cast<uint32_t*>(sX + r * sx);
+      for (int c = lane; c < cout / 2; c += 32) dd[c] = srcd ? srcd[c] : 0u;
+      for (int c = lane; c < cin / 2; c += 32) dxs[c] = srcx ? srcx[c] : 0u;
     }
     __syncthreads();
 #pragma unroll
@@ -255,18 +263,16 @@ __global__ void __launch_bounds__(WG_WARPS * 32) wgrad_kernel(const WgradK a) {
         const int tile = warp + s * WG_WARPS;
         if (tile >= tiles) continue;
         const int m0 = (tile % mt) * 16, n0 = (tile / mt) * (NB8 * 8);
+        // A[co][v] = dY[v][co]: blocks (co 0-7 | 8-15) x (v 0-7 | 8-15) -> a0..a3
         uint32_t af[4];
-        // A[co][v] = dY[v][co]: rows g / g+8, k pairs 2t / 2t+8
-        af[0] = pack_raw(sDy[(kk + 2 * t) * sdy + m0 + g], sDy[(kk + 2 * t + 1) * sdy + m0 + g]);
-        af[1] = pack_raw(sDy[(kk + 2 * t) * sdy + m0 + g + 8], sDy[(kk + 2 * t + 1) * sdy + m0 + g + 8]);
-        af[2] = pack_raw(sDy[(kk + 2 * t + 8) * sdy + m0 + g], sDy[(kk + 2 * t + 9) * sdy + m0 + g]);
-        af[3] = pack_raw(sDy[(kk + 2 * t + 8) * sdy + m0 + g + 8], sDy[(kk + 2 * t + 9) * sdy + m0 + g + 8]);
+        ldsm_x4_t(af, sDy + (kk + lr + 8 * (lb >> 1)) * sdy + m0 + 8 * (lb & 1));
 #pragma unroll
-        for (int n = 0; n < NB8; ++n) {
-          const int ci = n0 + n * 8 + g;
-          const uint32_t b0 = pack_raw(sX[(kk + 2 * t) * sx + ci], sX[(kk + 2 * t + 1) * sx + ci]);
-          const uint32_t b1 = pack_raw(sX[(kk + 2 * t + 8) * sx + ci], sX[(kk + 2 * t + 9) * sx + ci]);
-          mma16816(acc[s][n], af, b0, b1);
+        for (int n = 0; n < NB8; n += 2) {
+          // B[v][ci] = X[v][ci]: blocks (v 0-7 | 8-15) x (ci n | n+1) -> b0, b1 of n and n+1
+          uint32_t bf[4];
+          ldsm_x4_t(bf, sX + (kk + lr + 8 * (lb & 1)) * sx + n0 + 8 * (n + (lb >> 1)));
+          mma16816(acc[s][n], af, bf[0], bf[1]);
+          mma16816(acc[s][n + 1], af, bf[2], bf[3]);
         }
       }
     }
@@ -619,9 +625,12 @@ extern "C" int gm_unet_wgrad(const gm_wgrad_args* c, void* stream) {
   a.nsplit = (int)(need / (27LL * c->cin * c->cout));
   a.chunk = (V + a.nsplit - 1) / a.nsplit;
   a.chunk = (a.chunk + WG_KV - 1) / WG_KV * WG_KV;
-  const size_t smem = (size_t)WG_KV * ((c->cout + 2) + (c->cin + 2)) * 2;
+  const size_t smem = (size_t)WG_KV * ((c->cout + 8) + (c->cin + 8)) * 2;
   cudaStream_t st = (cudaStream_t)stream;
-  if (smem > 48 * 1024) return GM_ERR_ARG;
+  if (smem > 48 * 1024 &&
+      (cudaFuncSetAttribute(wgrad_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+       cudaFuncSetAttribute(wgrad_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess))
+    return GM_ERR_LAUNCH;
   if (nb8 == 4)
     wgrad_kernel<4><<<dim3(a.nsplit, 27), WG_WARPS * 32, smem, st>>>(a);
   else
