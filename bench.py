@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--cpu-steps", type=int, default=8, help="oracle fine steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--l3-shape", default="",
+                    help="--kernel-only: launch shape instead of the autotuned one, 'separable,ROWS,THREAD_ROWS,ZCHUNK' "
+                         "or 'tiles,TILE_X,ZCHUNK'")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the Level-3 level-step kernel --steps times (for profiling)")
     ap.add_argument("--precision", action="store_true",
@@ -174,6 +177,14 @@ def profile_traffic():
 
 
 # ---------------------------------------------------------------------------
+def shape_json(v):
+    """A measured level-step launch shape (kern.TunedShape) for the JSON line."""
+    if v.kernel == 1:
+        return {"kernel": "separable", "cta": [v.tile_x, v.tile_y], "rows_per_thread": v.rows, "zchunk": v.zchunk,
+                "us": round(v.us, 2)}
+    return {"kernel": "element_tiles", "tile": [v.tile_x, v.tile_y], "zchunk": v.zchunk, "us": round(v.us, 2)}
+
+
 # CPU oracle sample (reference arm and cpu_baseline)
 # ---------------------------------------------------------------------------
 def oracle_sample(cfg, rows, nsteps, warm=1):
@@ -439,8 +450,7 @@ def run_ours(args):
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
-        "autotuned": {f"L{lev}": {"tile": [v[0], v[1]], "zchunk": v[2], "us": round(v[3], 2)}
-                      for lev, v in tuned.items()},
+        "autotuned": {f"L{lev}": shape_json(v) for lev, v in tuned.items()},
     }
     if args.fp64_steps > 0:
         del eng
@@ -665,7 +675,7 @@ def run_batched(args):
                    desc.data_ptr(), nbytes, C.byref(info), kern.stream_ptr(stream))
             if lev == 3:
                 tuned = kern.level_autotune(engs[0].ps, reps=5, stream=stream, **kws[0])
-                out["L3_autotuned_shape"] = {"tile": [tuned[0], tuned[1]], "zchunk": tuned[2], "us": tuned[3]}
+                out["L3_autotuned_shape"] = shape_json(tuned)
 
             def single():
                 for e, kw in zip(engs, kws):
@@ -751,6 +761,7 @@ def run_kernel_only(args):
     import torch
 
     import engine
+    import kern
 
     cfg, P, nm, rows = workload()
     N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
@@ -761,14 +772,34 @@ def run_kernel_only(args):
     for k in range(args.warmup):
         eng.move(rows[k * n23], vstart)
         eng.subcycle(rows[k * n23:(k + 1) * n23])
+    if args.l3_shape:  # e.g. "separable,4,2,6" (rows, thread rows, z-chunk) or "tiles,32,14"
+        f = args.l3_shape.split(",")
+        shape = (dict(kernel=1, rows=int(f[1]), tile_y=int(f[2]), zchunk=int(f[3])) if f[0] == "separable"
+                 else dict(kernel=0, tile_x=int(f[1]), zchunk=int(f[2])))
+    else:
+        tuned = eng.autotune(rows[0])  # the launch shapes the bench uses
     last = torch.as_tensor(rows[args.warmup * n23 - 1], device=eng.dev)
     Tout = torch.empty_like(eng.T[3])
     phout = torch.empty_like(eng.ph[3])
     ring = eng._ring(3, eng.T[2], eng.T[2])
-    for _ in range(args.steps):
-        eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
     torch.cuda.synchronize()
-    print(json.dumps({"kernel_only": "level_step_kernel (Level 3)", "launches": args.steps, "nodes": eng.geo.L[3].nn}))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("level3_steps")  # ncu --nvtx --nvtx-include level3_steps/
+    with torch.cuda.stream(eng.stream):
+        e0.record(eng.stream)
+        for _ in range(args.steps):
+            if args.l3_shape:
+                kern.level_step_shape(eng.ps, stream=eng.stream, **shape,
+                                      **eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last,
+                                                         ring=ring, alpha=0.5))
+            else:
+                eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
+        e1.record(eng.stream)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({"kernel_only": "level step (Level 3)", "launches": args.steps, "nodes": eng.geo.L[3].nn,
+                      "us_per_launch_host_issued": 1000 * e0.elapsed_time(e1) / args.steps,
+                      "shape": args.l3_shape or shape_json(tuned[3])}))
 
 
 def main():

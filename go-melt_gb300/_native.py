@@ -98,7 +98,13 @@ class gm_batch_info(C.Structure):
 
 
 class gm_tune_result(C.Structure):
-    _fields_ = [("tile_x", C.c_int), ("tile_y", C.c_int), ("zchunk", C.c_int), ("us", C.c_float)]
+    _fields_ = [("tile_x", C.c_int), ("tile_y", C.c_int), ("zchunk", C.c_int), ("us", C.c_float),
+                ("kernel", C.c_int), ("rows", C.c_int)]
+
+
+class gm_level_shape(C.Structure):
+    _fields_ = [("kernel", C.c_int), ("tile_x", C.c_int), ("tile_y", C.c_int), ("rows", C.c_int),
+                ("zchunk", C.c_int)]
 
 
 class gm_state_props_args(C.Structure):
@@ -242,6 +248,7 @@ SIGNATURES = {
     "gm_level_batched_prepare": [vp, C.c_int, vp, vp, C.c_longlong, C.POINTER(gm_batch_info), vp],
     "gm_level_batched_launch": [vp, C.POINTER(gm_batch_info), vp],
     "gm_level_autotune": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.c_int, C.POINTER(gm_tune_result), vp],
+    "gm_level_step_shape": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.POINTER(gm_level_shape), vp],
     "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],
     "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
     "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],

@@ -62,6 +62,11 @@ struct LevelK {
   double inv_r2, inv_d2;
   double src_c;  // 6*sqrt(3)*eta * rc^2 * dc * wvol  (times P)
   Props<real> p;
+  // separable form (constant k, rho*c), formed on the host in double:
+  real rh[3];            // hx, hy, hz
+  real rir2, rid2;       // 1/r^2, 1/d^2 of the laser
+  real sa1, sb1, sb2;    // k hy hz / (36 hx), k hx hz / (36 hy), k hx hy / (36 hz)
+  real smass;            // lumped mass of 8 elements times dt: hx hy hz rho c
 };
 
 constexpr int ZMAX = 64;
@@ -477,6 +482,312 @@ __global__ void __launch_bounds__(TX * BY, level_min_blocks<real, FL>()) level_s
   level_body<real, TX, BY, FL>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// ---------------------------------------------------------------------------
+// Separable form of the level step for constant k and rho*c.
+//
+// With one conductivity and one heat capacity the element sum of
+// solveMatrixFreeFE is the assembled brick operator, a tensor sum of 1-D
+// operators over the active element box [0,nx-1) x [0,ny-1) x [0,ne_planes):
+//   sum_e K_e T = k [Kx (x) My (x) Mz + Mx (x) Ky (x) Mz + Mx (x) My (x) Kz] T,
+// 1-D stiffness K = (1/h)(-1, 2, -1) and consistent mass M = (h/6)(1, 4, 1)
+// at a node with two elements, one-sided (1/h)(1, -1) and (h/6)(2, 1) at a
+// node with one.  The lumped mass is (rho c / dt)(h^3/8) times the number of
+// elements at the node (8 inside, 4 on the top plane).  Every node of the x/y
+// ring and of the bottom plane is a Dirichlet node in the variants that use
+// this kernel (bc_mode 1 and 3), so only the top plane needs the one-sided z
+// operators.  Same algebra as level_body in a different order of summation.
+//
+// Thread mapping: a warp owns one x-tile of 30 node columns (lanes 1..30;
+// lanes 0 and 31 are the x halo) and a strip of BYT consecutive y rows, and
+// marches its CTA's z-chunk.  T planes p-1, p, p+1 of the strip and its two
+// halo rows sit in a 4-deep register ring (plane p+2 is loaded while plane p
+// is computed); the per-node inputs of plane p+1 (phase, melt time, RHS box)
+// are loaded one plane ahead.  z and y stencils are register arithmetic and
+// the x stencil takes the neighbouring lanes' partial sums by shuffles, so
+// warps never wait on one another.  The Dirichlet nodes (x/y ring, bottom
+// plane) are written by the last z-slice of CTAs, which does no stencil work:
+// the marching warps neither load ring values nor store ring nodes.
+// ---------------------------------------------------------------------------
+constexpr int SEP_TILE = 30;  // output node columns of a warp
+constexpr int SEP_ZMAX = 32;  // planes a CTA marches (one z source factor a lane)
+
+template <typename real, int BYT>
+constexpr int sep_min_blocks() {
+  return (sizeof(real) == 4 && BYT == 2) ? 3 : 2;  // 256-thread CTAs: 85 or 128 registers a thread
+}
+
+template <typename real, int BYT, int FL>
+__global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_kernel(const LevelK<real> a) {
+  constexpr int RY = BYT + 2;  // strip rows with the two y halo rows
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr bool hLaser = (FL & LF_LASER) != 0;
+  constexpr bool hBox = (FL & LF_BOX) != 0;
+  constexpr bool hAcc = (FL & LF_ACCUM) != 0;
+  constexpr bool hSurf = (FL & LF_SURF) != 0;
+  constexpr bool hClamp = (FL & LF_CLAMP) != 0;
+  constexpr bool hInact = (FL & LF_INACT) != 0;
+  constexpr bool hPhout = (FL & LF_PHOUT) != 0;
+  constexpr bool needPh = hPhout || hAcc;
+  constexpr int bcm = (FL & LF_BC1) ? 1 : 3;
+  static_assert((FL & LF_CONST) && !(FL & (LF_GENERIC | LF_KARR | LF_FULL | LF_BC2)), "constant-property variants");
+
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxy = nx * ny;
+  const int lane = threadIdx.x & 31;
+  const int x = blockIdx.x * SEP_TILE - 1 + lane;
+  const int y0 = (blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5)) * BYT;
+  const int ntop = a.ne_planes;
+  const Props<real>& P = a.p;
+  real dt = 0;
+  if (lane == 0) dt = (real)(*a.dt);
+  dt = __shfl_sync(FULL, dt, 0);
+  const int subs = a.substrate > (long long)nxy * nz ? nxy * nz : (int)a.substrate;
+  const bool xin = x >= 0 && x < nx;
+  const bool out_x = lane >= 1 && lane <= SEP_TILE && x < nx;
+  const bool ring_x = x == 0 || x == nx - 1;
+
+  // new phase, output and melt time of node id (old temperature Told, phase byte ph)
+  auto finish = [&](int id, real Tn, real Told, uint32_t ph, real cAcc, real cMacc) {
+    if (hClamp) Tn = fmax(Tn, P.T_amb);
+    a.T_out[id] = Tn;
+    if (needPh) {
+      const bool s2 = Told >= P.T_liquidus;
+      const bool s1 = (ph & PH_S1) || s2 || id < subs;
+      if (hPhout) a.ph_out[id] = (uint8_t)((s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u));
+      if (hAcc) {
+        const bool prev2 = (ph & PH_S2) != 0;
+        const real racc = (s2 && !prev2) ? cAcc : (real)0;
+        a.max_accum[id] = fmax(racc, cMacc);
+        a.accum[id] = (cAcc + dt * (s2 ? (real)1 : (real)0)) - racc;
+      }
+    }
+  };
+
+  if (blockIdx.z == gridDim.z - 1) {
+    // ---- Dirichlet nodes, spread over the threads of this slice: the bottom
+    // plane, then the x/y ring of planes 1..nz-1 (perimeter order y0, y1, x0, x1) ----
+    const int perim = 2 * nx + 2 * (ny - 2);
+    const long long nring = (long long)nxy + (long long)(nz - 1) * perim;
+    const long long nthr = (long long)gridDim.x * gridDim.y * blockDim.x;
+    const long long t0 = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+#pragma unroll 4
+    for (long long k = t0; k < nring; k += nthr) {
+      int rx, ry, rp;
+      if (k < nxy) {
+        rp = 0;
+        rx = (int)k % nx;
+        ry = (int)k / nx;
+      } else {
+        const long long kk = k - nxy;
+        rp = 1 + (int)(kk / perim);
+        const int j = (int)(kk % perim);
+        if (j < nx) {
+          rx = j;
+          ry = 0;
+        } else if (j < 2 * nx) {
+          rx = j - nx;
+          ry = ny - 1;
+        } else if (j < 2 * nx + ny - 2) {
+          rx = 0;
+          ry = 1 + j - 2 * nx;
+        } else {
+          rx = nx - 1;
+          ry = 1 + j - 2 * nx - (ny - 2);
+        }
+      }
+      const int id = rx + ry * nx + rp * nxy;
+      real Tn;
+      if (bcm == 1) {
+        Tn = a.face[4];
+        if (rp > 0) {
+          Tn = (ry == 0) ? a.face[2] : a.face[3];
+          if (rx == 0) Tn = a.face[0];
+          if (rx == nx - 1) Tn = a.face[1];
+        }
+      } else {
+        Tn = a.bc_alpha * a.bc_new[id] + a.bc_beta * a.bc_old[id];
+      }
+      finish(id, Tn, needPh ? a.T_in[id] : (real)0, needPh ? (uint32_t)a.ph_in[id] : 0u,
+             hAcc ? a.accum[id] : (real)0, hAcc ? a.max_accum[id] : (real)0);
+    }
+    return;
+  }
+
+  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  // stencil constants: A = a1 (Zm- + 4 Zm + Zm+), B = b1 Ky(Zm) + b2 My(Zk)
+  const real a1 = a.sa1, b1 = a.sb1, b2 = a.sb2;
+  const real minv = dt / a.smass;  // 1 / (8 elements' lumped mass)
+
+  // laser: x factor times the rows' y factors; lane l keeps the z factor of
+  // plane Z0 + l.  The laser offsets are formed in double by lane 0.
+  real sxy[BYT], szl = 0;
+  if (hLaser) {
+    real rx = 0, ry = 0, rz = 0, srcP = 0;
+    if (lane == 0) {
+      rx = (real)(a.ox - a.laser[0]);
+      ry = (real)(a.oy - a.laser[1]);
+      rz = (real)(a.oz - a.laser[2]);
+      srcP = (real)(a.src_c * a.laser[6]);
+    }
+    rx = __shfl_sync(FULL, rx, 0);
+    ry = __shfl_sync(FULL, ry, 0);
+    rz = __shfl_sync(FULL, rz, 0);
+    srcP = __shfl_sync(FULL, srcP, 0);
+    const real sx = xin ? srcP * src_factor<real>(x, nx, rx, a.rh[0], a.rir2) : (real)0;
+    // lane r < BYT evaluates the y factor of row y0 + r for the whole warp
+    const real syl =
+        (lane < BYT && y0 + lane < ny) ? src_factor<real>(y0 + lane, ny, ry, a.rh[1], a.rir2) : (real)0;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) sxy[r] = sx * __shfl_sync(FULL, syl, r);
+    if (Z0 + lane < Z1) szl = src_factor<real>(Z0 + lane, nz, rz, a.rh[2], a.rid2);
+  }
+
+  int box_w = 0, box_pl = 0;
+  bool box_x = false;
+  if (hBox) {
+    box_w = a.box[1] - a.box[0];
+    box_pl = box_w * (a.box[3] - a.box[2]);
+    box_x = x >= a.box[0] && x < a.box[1];
+  }
+  // rows whose nodes this warp writes (not on the y ring, inside the grid)
+  bool row_out[BYT];
+#pragma unroll
+  for (int r = 0; r < BYT; ++r) row_out[r] = out_x && !ring_x && y0 + r > 0 && y0 + r < ny - 1;
+
+  real Tr[4][RY];
+  const real* Tcol = a.T_in + (x + (y0 - 1) * nx);  // strip row 0 of plane 0 (dereferenced only inside the grid)
+  auto load_plane = [&](real(&dst)[RY], int pl) {
+    const bool ok = xin && pl >= 0 && pl < nz;
+#pragma unroll
+    for (int i = 0; i < RY; ++i) {
+      const int y = y0 - 1 + i;
+      dst[i] = (ok && y >= 0 && y < ny) ? Tcol[i * nx + pl * nxy] : (real)0;
+    }
+  };
+  // per-node inputs of one output plane, loaded one plane ahead
+  uint32_t nph[2][BYT];
+  real nacc[2][BYT], nmac[2][BYT], nrhs[2][BYT];
+  auto prefetch = [&](auto slot_c, int pl) {
+    constexpr int S = decltype(slot_c)::value;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) {
+      const int y = y0 + r;
+      const bool ok = row_out[r] && pl < Z1;
+      const int id = x + y * nx + pl * nxy;
+      nph[S][r] = 0;
+      nacc[S][r] = nmac[S][r] = nrhs[S][r] = 0;
+      if (ok) {
+        if (needPh) nph[S][r] = a.ph_in[id];
+        if (hAcc) {
+          nacc[S][r] = a.accum[id];
+          nmac[S][r] = a.max_accum[id];
+        }
+        if (hBox && box_x && y >= a.box[2] && y < a.box[3] && pl >= a.box[4] && pl < a.box[5])
+          nrhs[S][r] = a.rhs_box[(x - a.box[0]) + (y - a.box[2]) * box_w + (pl - a.box[4]) * box_pl];
+      }
+    }
+  };
+
+  load_plane(Tr[0], Z0 - 1);
+  load_plane(Tr[1], Z0);
+  load_plane(Tr[2], Z0 + 1);
+  prefetch(std::integral_constant<int, 0>(), Z0);
+
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
+
+  auto body = [&](auto par, int p) {
+    constexpr int PAR = decltype(par)::value;
+    constexpr int NB = PAR & 1;  // per-node input slot of plane p
+    real(&Tm)[RY] = Tr[PAR & 3];
+    real(&T0)[RY] = Tr[(PAR + 1) & 3];
+    real(&Tp)[RY] = Tr[(PAR + 2) & 3];
+    real(&Tq)[RY] = Tr[(PAR + 3) & 3];
+    if (p + 2 <= Z1) load_plane(Tq, p + 2);
+    prefetch(std::integral_constant<int, NB ^ 1>(), p + 1);
+
+    const bool top = p == ntop;
+    // ---- top surface (convection / radiation / evaporation on the faces of element plane ntop-1) ----
+    real surf[BYT];
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) surf[r] = 0;
+    if (hSurf && top && ntop >= 1) {
+      const real w2 = a.w2;
+      real c00[BYT + 1], c10[BYT + 1], c01[BYT + 1], c11[BYT + 1];
+#pragma unroll
+      for (int i = 0; i <= BYT; ++i) {  // element (x, y0 - 1 + i): strip rows i, i+1
+        const real t10 = __shfl_down_sync(FULL, T0[i], 1), t11 = __shfl_down_sync(FULL, T0[i + 1], 1);
+        c00[i] = c10[i] = c01[i] = c11[i] = 0;
+        const int ey = y0 - 1 + i;
+        if (x >= 0 && x < nx - 1 && ey >= 0 && ey < ny - 1) {
+          const real t00 = T0[i], t01 = T0[i + 1];
+#pragma unroll
+          for (int qy = 0; qy < 2; ++qy)
+#pragma unroll
+            for (int qx = 0; qx < 2; ++qx) {
+              const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
+              const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
+              const real Tq4 = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
+              const real q = surface_flux(P, Tq4) * w2;
+              c00[i] += px0 * py0 * q;
+              c10[i] += px1 * py0 * q;
+              c01[i] += px0 * py1 * q;
+              c11[i] += px1 * py1 * q;
+            }
+        }
+      }
+      // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
+#pragma unroll
+      for (int r = 0; r < BYT; ++r)
+        surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
+    }
+
+    // ---- z and y stencils in registers, x stencil by shuffles ----
+    real Zm[RY], Zk[RY];
+    if (top) {
+#pragma unroll
+      for (int i = 0; i < RY; ++i) {
+        Zm[i] = Tm[i] + (real)2 * T0[i];
+        Zk[i] = T0[i] - Tm[i];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < RY; ++i) {
+        const real s = Tm[i] + Tp[i];
+        Zm[i] = s + (real)4 * T0[i];
+        Zk[i] = (real)2 * T0[i] - s;
+      }
+    }
+    const real mi = top ? (real)2 * minv : minv;
+    const real sz = hLaser ? __shfl_sync(FULL, szl, p - Z0) : (real)0;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) {
+      const int i = r + 1;
+      const real u = Zm[i - 1] + Zm[i + 1];
+      const real w = Zk[i - 1] + Zk[i + 1];
+      const real A = a1 * (u + (real)4 * Zm[i]);
+      const real B = b1 * ((real)2 * Zm[i] - u) + b2 * (w + (real)4 * Zk[i]);
+      const real Al = __shfl_up_sync(FULL, A, 1), Ar = __shfl_down_sync(FULL, A, 1);
+      const real Bl = __shfl_up_sync(FULL, B, 1), Br = __shfl_down_sync(FULL, B, 1);
+      if (!row_out[r] || p == 0) continue;
+      const real KT = ((real)2 * A - Al - Ar) + (Bl + Br + (real)4 * B);
+      const real Told = T0[i];
+      real Rt = -KT;
+      if (hLaser) Rt += sxy[r] * sz;
+      if (hBox) Rt += nrhs[NB][r];
+      if (hSurf) Rt += surf[r];
+      real Tn = Told + Rt * mi;
+      if (hInact && p > ntop) Tn = P.T_amb;
+      finish(x + (y0 + r) * nx + p * nxy, Tn, Told, nph[NB][r], nacc[NB][r], nmac[NB][r]);
+    }
+  };
+
+  for (int p = Z0; p < Z1; p += 4) {
+    body(std::integral_constant<int, 0>(), p);
+    if (p + 1 < Z1) body(std::integral_constant<int, 1>(), p + 1);
+    if (p + 2 < Z1) body(std::integral_constant<int, 2>(), p + 2);
+    if (p + 3 < Z1) body(std::integral_constant<int, 3>(), p + 3);
+  }
+}
+
 // Many level windows (instances of uneven sizes) in one launch: instance b
 // owns the linear blocks [first[b], first[b+1]) of the grid, laid out
 // (bx, by, bz) with bx fastest over its own tiles; its parameters are read
@@ -589,8 +900,11 @@ struct TuneKey {
     return nz < o.nz;
   }
 };
+// A launch shape: kernel 0 = element tiles (tile_x 32 -> 32 x 8, 16 -> 16 x
+// 16), kernel 1 = separable stencil (wys thread rows of `rows` y rows each);
+// zchunk = node planes per CTA.
 struct TuneVal {
-  int tile_x, zchunk;
+  int kernel, tile_x, wys, rows, zchunk;
 };
 static std::map<TuneKey, TuneVal> g_tuned;
 static std::mutex g_tuned_mutex;
@@ -614,21 +928,87 @@ static void launch_shape(const LevelK<real>& a, int zc_req, cudaStream_t st) {
   level_step_kernel<real, TXv, BYv, FL><<<grid, block, 0, st>>>(b);
 }
 
-// tile_x 0: tuned shape if any, else 32 x 8 with the z-chunk model.
+// Element-tile launch: tile_x 16 -> 16 x 16, else 32 x 8; zc_req <= 0: the
+// z-chunk model.
 template <typename real, int FL>
-static void launch_variant(const LevelK<real>& a, int zc_req, cudaStream_t st, int tile_x = 0, int dtype = 0,
-                           int flags = 0) {
-  if (tile_x == 0 && zc_req <= 0) {
-    TuneVal v;
-    if (tuned_shape(TuneKey{dtype, flags & ~LF_ACCUM, a.nx, a.ny, a.nz}, &v)) {
-      tile_x = v.tile_x;
-      zc_req = v.zchunk;
-    }
-  }
+static void launch_variant(const LevelK<real>& a, int zc_req, cudaStream_t st, int tile_x) {
   if (tile_x == 16)
     launch_shape<real, FL, 16, 16>(a, zc_req, st);
   else
     launch_shape<real, FL, LT_X, LT_Y>(a, zc_req, st);
+}
+
+// The separable kernel serves the constant-property Level-1/2/3 variants
+// when no node lies above the active element planes (or those nodes are
+// reset to T_amb).
+static bool sep_eligible(const gm_level_args* g, int fl) {
+  if (!(fl & LF_CONST)) return false;
+  const int b = fl & ~LF_CONST;
+  if (b != LF_L3 && b != LF_L3ACC && b != LF_L2 && b != LF_L1) return false;
+  return g->ne_planes == g->nz - 1 || (fl & LF_INACT);
+}
+
+// Separable launch: CTAs of `warps` warps (one x-tile, warps x BYT rows),
+// v.zchunk <= SEP_ZMAX planes.
+template <typename real, int FL, int BYT>
+static void launch_sep_t(const LevelK<real>& a, int warps, int zc, cudaStream_t st) {
+  LevelK<real> b = a;
+  b.zchunk = zc;
+  // the last z-slice of CTAs writes the Dirichlet nodes
+  const dim3 grid(cdiv(a.nx, SEP_TILE), cdiv(a.ny, warps * BYT), cdiv(a.nz, zc) + 1);
+  level_sep_kernel<real, BYT, FL><<<grid, 32 * warps, 0, st>>>(b);
+}
+
+template <typename real>
+static int launch_sep(const LevelK<real>& a, int fl, const TuneVal& v, cudaStream_t st) {
+  if ((v.rows != 2 && v.rows != 4) || v.wys < 1 || v.wys > 8 || v.zchunk < 1 || v.zchunk > SEP_ZMAX)
+    return GM_ERR_ARG;
+  switch (fl) {
+#define GM_SEP(V)                                                  \
+  case V | LF_CONST:                                               \
+    if (v.rows == 2)                                               \
+      launch_sep_t<real, V | LF_CONST, 2>(a, v.wys, v.zchunk, st); \
+    else                                                           \
+      launch_sep_t<real, V | LF_CONST, 4>(a, v.wys, v.zchunk, st); \
+    break;
+    GM_SEP(LF_L3)
+    GM_SEP(LF_L3ACC)
+    GM_SEP(LF_L2)
+    GM_SEP(LF_L1)
+#undef GM_SEP
+    default:
+      return GM_ERR_ARG;
+  }
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+// Untuned separable shape: 4 rows a thread (2 in FP64), 4-warp CTAs, and
+// the z-chunk (<= SEP_ZMAX) whose CTA count best fills the SMs: busiest SM's
+// CTAs x (planes + 2 halo planes).
+template <typename real>
+static TuneVal sep_default(const gm_level_args* g) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 152;
+  }
+  TuneVal v{1, SEP_TILE, 4, sizeof(real) == 4 ? 4 : 2, 1};
+  const int res = 4;  // resident 4-warp CTAs per SM at about 128 registers a thread
+  const long long gxy = (long long)cdiv(g->nx, SEP_TILE) * cdiv(g->ny, v.wys * v.rows);
+  double best = -1;
+  for (int zc = 2; zc <= min(g->nz, SEP_ZMAX); ++zc) {
+    const long long ctas = gxy * cdiv(g->nz, zc);
+    const long long waves = (ctas + (long long)sms * res - 1) / ((long long)sms * res);
+    const double cost = (double)waves * (zc + 2);
+    if (best < 0 || cost < best - 1e-9) {
+      best = cost;
+      v.zchunk = zc;
+    }
+  }
+  if (g->nz < 2) v.zchunk = 1;
+  return v;
 }
 
 template <typename real>
@@ -685,6 +1065,16 @@ static LevelK<real> make_levelk(const gm_level_args* g, const gm_props* pr) {
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   a.src_c = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * (hx * hy * hz / 8.0);
   a.zchunk = g->zchunk;
+  a.rh[0] = (real)hx;
+  a.rh[1] = (real)hy;
+  a.rh[2] = (real)hz;
+  a.rir2 = (real)a.inv_r2;
+  a.rid2 = (real)a.inv_d2;
+  const double kc = pr->k_fluid / 1000.0;
+  a.sa1 = (real)(kc * hy * hz / (36.0 * hx));
+  a.sb1 = (real)(kc * hx * hz / (36.0 * hy));
+  a.sb2 = (real)(kc * hx * hy / (36.0 * hz));
+  a.smass = (real)(hx * hy * hz * pr->rho * pr->cp_fluid);
   return a;
 }
 
@@ -706,20 +1096,36 @@ static int variant_of(int flags) {
   X(LF_L2 | LF_CONST)        \
   X(LF_L1 | LF_CONST)
 
+// One level step with shape `sh`; sh.kernel < 0: the tuned shape for this
+// call if gm_level_autotune measured one (and the caller left zchunk at 0),
+// else the separable kernel where eligible, else 32 x 8 element tiles.
 template <typename real>
-static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st, int tile_x = 0, int zc = 0) {
+static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t st,
+                        TuneVal sh = TuneVal{-1, 0, 0, 0, 0}) {
   const LevelK<real> a = make_levelk<real>(g, pr);
   const int fl = level_flags(g, pr);
-  if (zc <= 0) zc = g->zchunk;
+  const bool sep_ok = sep_eligible(g, fl);
+  if (sh.kernel < 0) {
+    TuneVal v;
+    if (g->zchunk <= 0 && tuned_shape(TuneKey{g->dtype, fl & ~LF_ACCUM, g->nx, g->ny, g->nz}, &v)) {
+      sh = v;
+    } else if (sep_ok) {
+      sh = sep_default<real>(g);
+      if (g->zchunk > 0) sh.zchunk = g->zchunk;
+    } else {
+      sh = TuneVal{0, 0, 0, 0, g->zchunk};
+    }
+  }
+  if (sh.kernel == 1) return sep_ok ? launch_sep<real>(a, fl, sh, st) : GM_ERR_ARG;
   switch (variant_of(fl)) {
-#define GM_CASE(V)                                            \
-  case V:                                                     \
-    launch_variant<real, V>(a, zc, st, tile_x, g->dtype, fl); \
+#define GM_CASE(V)                                        \
+  case V:                                                 \
+    launch_variant<real, V>(a, sh.zchunk, st, sh.tile_x); \
     break;
     GM_LEVEL_VARIANTS(GM_CASE)
 #undef GM_CASE
     default:
-      launch_variant<real, LF_GENERIC>(a, zc, st, tile_x, g->dtype, fl);
+      launch_variant<real, LF_GENERIC>(a, sh.zchunk, st, sh.tile_x);
   }
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
@@ -862,6 +1268,19 @@ extern "C" int gm_level_step_batched(const gm_level_args* a, int nb, const gm_pr
   return gm_level_batched_launch(desc, &info, stream);
 }
 
+extern "C" int gm_level_step_shape(const gm_level_args* a, const gm_props* p, const gm_level_shape* shape,
+                                   void* stream) {
+  if (!p || !shape) return GM_ERR_ARG;
+  const int rc = gm::check_level_args(a);
+  if (rc != GM_OK) return rc;
+  if (shape->kernel != 0 && shape->kernel != 1) return GM_ERR_ARG;
+  if (shape->kernel == 0 && shape->tile_x != 32 && shape->tile_x != 16) return GM_ERR_ARG;
+  const gm::TuneVal v{shape->kernel, shape->tile_x, shape->tile_y, shape->rows, shape->zchunk};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a->dtype == GM_F32) return gm::launch_level<float>(a, p, st, v);
+  return gm::launch_level<double>(a, p, st, v);
+}
+
 extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out,
                                  void* stream) {
   if (!p || reps < 1) return GM_ERR_ARG;
@@ -874,36 +1293,44 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
     cudaEventDestroy(e0);
     return GM_ERR_CUDA;
   }
-  gm_level_args b = *a;
-  gm::TuneVal best{0, 0};
+  // candidates: element tiles 32 x 8 and 16 x 16, and (where eligible) the
+  // separable kernel with 2 or 4 rows a thread and 1, 2 or 4 thread rows,
+  // each over the distinct z-chunks of 2..64 planes
+  std::vector<gm::TuneVal> cand;
+  std::vector<int> zcs;
+  for (int nch = gm::cdiv(a->nz, gm::ZMAX), last = -1; nch <= a->nz; ++nch) {
+    const int zc = gm::cdiv(a->nz, nch);
+    if (zc == last || zc < 2) continue;
+    last = zc;
+    zcs.push_back(zc);
+  }
+  for (int tx : {gm::LT_X, 16})
+    for (int zc : zcs) cand.push_back(gm::TuneVal{0, tx, 0, 0, zc});
+  if (gm::sep_eligible(a, gm::level_flags(a, p)))
+    for (int rows : {2, 4})
+      for (int warps : {2, 4, 8})
+        for (int zc : zcs)
+          if (zc <= gm::SEP_ZMAX) cand.push_back(gm::TuneVal{1, gm::SEP_TILE, warps, rows, zc});
+  gm::TuneVal best{0, gm::LT_X, 0, 0, 0};
   float best_us = -1.f;
   int status = GM_OK;
-  const int tiles[2] = {gm::LT_X, 16};
-  for (int ti = 0; ti < 2 && status == GM_OK; ++ti) {
-    int last = -1;
-    for (int nch = gm::cdiv(a->nz, gm::ZMAX); nch <= a->nz && status == GM_OK; ++nch) {
-      const int zc = gm::cdiv(a->nz, nch);
-      if (zc == last || zc < 2) continue;
-      last = zc;
-      b.zchunk = zc;
-      for (int r = -1; r < reps && status == GM_OK; ++r) {  // one untimed launch first
-        if (r == 0) cudaEventRecord(e0, st);
-        status = a->dtype == GM_F32 ? gm::launch_level<float>(&b, p, st, tiles[ti], zc)
-                                    : gm::launch_level<double>(&b, p, st, tiles[ti], zc);
-      }
-      if (status != GM_OK) break;
-      cudaEventRecord(e1, st);
-      if (cudaEventSynchronize(e1) != cudaSuccess) {
-        status = GM_ERR_CUDA;
-        break;
-      }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      const float us = 1000.f * ms / reps;
-      if (best_us < 0 || us < best_us) {
-        best_us = us;
-        best = gm::TuneVal{tiles[ti], zc};
-      }
+  for (const gm::TuneVal& v : cand) {
+    for (int r = -1; r < reps && status == GM_OK; ++r) {  // one untimed launch first
+      if (r == 0) cudaEventRecord(e0, st);
+      status = a->dtype == GM_F32 ? gm::launch_level<float>(a, p, st, v) : gm::launch_level<double>(a, p, st, v);
+    }
+    if (status != GM_OK) break;
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      status = GM_ERR_CUDA;
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const float us = 1000.f * ms / reps;
+    if (best_us < 0 || us < best_us) {
+      best_us = us;
+      best = v;
     }
   }
   cudaEventDestroy(e0);
@@ -914,10 +1341,18 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
     gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a, p) & ~gm::LF_ACCUM, a->nx, a->ny, a->nz}] = best;
   }
   if (out) {
-    out->tile_x = best.tile_x;
-    out->tile_y = best.tile_x == 16 ? 16 : gm::LT_Y;
+    out->kernel = best.kernel;
     out->zchunk = best.zchunk;
     out->us = best_us;
+    if (best.kernel == 1) {
+      out->tile_x = gm::SEP_TILE;
+      out->tile_y = best.wys;
+      out->rows = best.rows;
+    } else {
+      out->tile_x = best.tile_x;
+      out->tile_y = best.tile_x == 16 ? 16 : gm::LT_Y;
+      out->rows = 1;
+    }
   }
   return GM_OK;
 }

@@ -298,11 +298,11 @@ class Engine:
         return move_v
 
     def autotune(self, row, reps=5):
-        """Measure the launch shape (tile, z-chunk) of the Level-3, Level-2 and
-        Level-1 steps as the subcycle issues them (gm_level_autotune); later
-        level steps of the same shapes use the fastest.  Needs the tables of a
-        move; writes only scratch outputs; synchronises the stream.  Returns
-        {level: (tile_x, tile_y, zchunk, us)}."""
+        """Measure the launch shape (kernel, tile, z-chunk) of the Level-3,
+        Level-2 and Level-1 steps as the subcycle issues them
+        (gm_level_autotune); later level steps of the same shapes use the
+        fastest.  Needs the tables of a move; writes only scratch outputs;
+        synchronises the stream.  Returns {level: kern.TunedShape}."""
         g = self.geo
         t = self.tables
         if t is None:

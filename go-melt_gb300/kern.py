@@ -7,6 +7,7 @@ computeFunctions.py and the subcycle engine are built on them.
 from __future__ import annotations
 
 import ctypes as C
+from typing import NamedTuple
 
 import numpy as np
 import torch
@@ -61,13 +62,32 @@ def level_step(props: N.gm_props, *, stream=None, **kw):
     N.call("gm_level_step", C.byref(a), C.byref(props), stream_ptr(stream))
 
 
-def level_autotune(props: N.gm_props, *, reps=5, stream=None, **kw):
-    """gm_level_autotune for the call level_args(**kw) describes; returns
-    (tile_x, tile_y, zchunk, microseconds)."""
+class TunedShape(NamedTuple):
+    """A measured launch shape (gm_tune_result): kernel 0 = element tiles
+    tile_x x tile_y, kernel 1 = separable stencil with tile_y thread rows of
+    `rows` y rows (tile_x threads across x)."""
+    tile_x: int
+    tile_y: int
+    zchunk: int
+    us: float
+    kernel: int
+    rows: int
+
+
+def level_autotune(props: N.gm_props, *, reps=5, stream=None, **kw) -> TunedShape:
+    """gm_level_autotune for the call level_args(**kw) describes."""
     a = level_args(**kw)
     r = N.gm_tune_result()
     N.call("gm_level_autotune", C.byref(a), C.byref(props), int(reps), C.byref(r), stream_ptr(stream), kernels=0)
-    return r.tile_x, r.tile_y, r.zchunk, r.us
+    return TunedShape(r.tile_x, r.tile_y, r.zchunk, r.us, r.kernel, r.rows)
+
+
+def level_step_shape(props: N.gm_props, *, kernel, zchunk, tile_x=32, tile_y=1, rows=4, stream=None, **kw):
+    """gm_level_step_shape: one level step with an explicit launch shape
+    (kernel 0: tile_x 32 or 16; kernel 1: tile_y thread rows of `rows` rows)."""
+    a = level_args(**kw)
+    s = N.gm_level_shape(int(kernel), int(tile_x), int(tile_y), int(rows), int(zchunk))
+    N.call("gm_level_step_shape", C.byref(a), C.byref(props), C.byref(s), stream_ptr(stream))
 
 
 def level_args(*, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_out=None,

@@ -228,17 +228,37 @@ int gm_level_batched_prepare(const gm_level_args* args, int nb, const gm_props* 
                              long long desc_bytes, gm_batch_info* info, void* stream);
 int gm_level_batched_launch(const void* desc, const gm_batch_info* info, void* stream);
 
-/* Autotuner: times gm_level_step for this call over the tile shapes (32 x 8,
- * 16 x 16) and z-chunks (every distinct split of the node planes) with CUDA
- * events, `reps` launches each after one untimed launch, and keeps the
- * fastest for later calls with the same dtype, features and grid that leave
- * zchunk at 0.  The timed launches write T_out / ph_out / melt time as the
- * call would (so pass scratch outputs, or tune a call whose repetition is
- * harmless); synchronises the stream; not for use during stream capture.
+/* Launch shape of a level step.  kernel 0: element tiles, tile_x 32
+ * (32 x 8 element columns a CTA) or 16 (16 x 16).  kernel 1: the separable
+ * stencil for constant-property materials (constant k and rho*c; the
+ * Level-1/2/3 feature sets of gm_subcycle, all nodes at or below the active
+ * element planes unless inactive_amb): a warp owns 30 node columns (tile_x,
+ * fixed) and `rows` (2 or 4) y rows, tile_y (1..8) warps a CTA.
+ * zchunk: node planes a CTA marches (at most 32 for kernel 1). */
+typedef struct gm_level_shape {
+  int kernel, tile_x, tile_y, rows, zchunk;
+} gm_level_shape;
+
+/* gm_level_step with an explicit launch shape (results agree with every
+ * other shape to rounding; GM_ERR_ARG if the separable kernel is asked for a
+ * call it does not serve).  No counterpart in the reference. */
+int gm_level_step_shape(const gm_level_args* a, const gm_props* p, const gm_level_shape* shape, void* stream);
+
+/* Autotuner: times gm_level_step for this call over the element tiles
+ * (32 x 8, 16 x 16) and, where it applies, the separable kernel (2 or 4 rows
+ * a thread, 1, 2 or 4 thread rows), each over the z-chunks (every distinct
+ * split of the node planes), with CUDA events, `reps` launches each after
+ * one untimed launch, and keeps the fastest for later calls with the same
+ * dtype, features and grid that leave zchunk at 0.  The timed launches write
+ * T_out / ph_out / melt time as the call would (so pass scratch outputs, or
+ * tune a call whose repetition is harmless); synchronises the stream; not for
+ * use during stream capture.  Result: the shape (fields as gm_level_shape;
+ * for kernel 0 tile_y is the tile height and rows 1) and its time.
  * No counterpart in the reference. */
 typedef struct gm_tune_result {
   int tile_x, tile_y, zchunk;
   float us;
+  int kernel, rows;
 } gm_tune_result;
 
 int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out, void* stream);

@@ -78,8 +78,8 @@ def test_autotune_keeps_results():
     w = windows(torch.float32, False)[3]
     kern.level_step(ps, **w)
     ref = w["T_out"].clone()
-    tx, ty, zc, us = kern.level_autotune(ps, reps=3, **w)
-    assert (tx, ty) in ((32, 8), (16, 16)) and 2 <= zc <= 41 and us > 0
+    tx, ty, zc, us, kernel, rows = kern.level_autotune(ps, reps=3, **w)
+    assert kernel == 0 and (tx, ty) in ((32, 8), (16, 16)) and 2 <= zc <= 41 and us > 0
     w["T_out"].zero_()
     kern.level_step(ps, **w)  # uses the tuned shape
     torch.cuda.synchronize()
