@@ -322,6 +322,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         clocks.start()
         ev = []
+        torch.cuda.nvtx.range_push("timed_steps")  # ncu --nvtx --nvtx-include timed_steps/
         for i in range(args.steps):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -331,6 +332,7 @@ def run_ours(args):
             e.record(stream)
             ev.append((s, e))
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         launches = N.launch_count() // args.steps
         t_ms = sum(s.elapsed_time(e) for s, e in ev)
         mm = sum(scan_mm(chunk(k + i)) for i in range(args.steps))

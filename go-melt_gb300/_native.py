@@ -48,7 +48,7 @@ class gm_level_args(C.Structure):
         ("rhs_box", vp), ("box", C.c_int * 6), ("laser", vp), ("surface", C.c_int), ("bc_mode", C.c_int),
         ("face", C.c_double * 5), ("inactive_amb", C.c_int), ("bc_new", vp), ("bc_old", vp),
         ("bc_alpha", C.c_double), ("bc_beta", C.c_double), ("bc_map", gm_map3), ("clamp", C.c_int),
-        ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int),
+        ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int), ("pdl", C.c_int),
     ]
 
 
@@ -182,7 +182,8 @@ class gm_subcycle_plan(C.Structure):
         ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("src2", vp), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
-        ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int)]
+        ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int),
+        ("pdl", C.c_int)]
 
 
 def subcycle_kernel_count(N2: int, N3: int) -> int:

@@ -87,6 +87,7 @@ void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tou
   a.accum = acc;
   a.max_accum = macc;
   a.zchunk = p.zchunk;
+  a.pdl = p.pdl;  // dt and the laser row are plan inputs, never written by the subcycle's kernels
   GM_TRY(gm_level_step(&a, c.pr, c.st));
 }
 

@@ -499,10 +499,10 @@ __global__ void __launch_bounds__(TX * BY, level_min_blocks<real, FL>()) level_s
 //
 // Thread mapping: a warp owns one x-tile of 30 node columns (lanes 1..30;
 // lanes 0 and 31 are the x halo) and a strip of BYT consecutive y rows, and
-// marches its CTA's z-chunk.  T planes p-1, p, p+1 of the strip and its two
-// halo rows sit in a 4-deep register ring (plane p+2 is loaded while plane p
-// is computed); the per-node inputs of plane p+1 (phase, melt time, RHS box)
-// are loaded one plane ahead.  z and y stencils are register arithmetic and
+// marches its CTA's z-chunk.  T planes p-1 .. p+3 of the strip and its two
+// halo rows sit in a 6-deep register ring (plane p+3 is loaded while plane p
+// is computed, so a load has two plane iterations to arrive); the per-node
+// inputs (phase, melt time, RHS box) are loaded two planes ahead.  z and y stencils are register arithmetic and
 // the x stencil takes the neighbouring lanes' partial sums by shuffles, so
 // warps never wait on one another.  The Dirichlet nodes (x/y ring, bottom
 // plane) are written by the last z-slice of CTAs, which does no stencil work:
@@ -513,7 +513,46 @@ constexpr int SEP_ZMAX = 32;  // planes a CTA marches (one z source factor a lan
 
 template <typename real, int BYT>
 constexpr int sep_min_blocks() {
-  return (sizeof(real) == 4 && BYT == 2) ? 3 : 2;  // 256-thread CTAs: 85 or 128 registers a thread
+  // 256-thread CTAs: 64, 85 or 128 registers a thread
+  return sizeof(real) != 4 ? 2 : (BYT == 1 ? 4 : (BYT == 2 ? 3 : 2));
+}
+
+// Top-surface flux of the strip's nodes: each lane evaluates the faces of
+// elements (x, y0-1+i), i = 0..BYT, at their 2 x 2 Gauss points and the node
+// sums are gathered from the lane to the left.  Called by every lane of the
+// warp (shuffles); one call per warp and launch, kept out of line so that the
+// unrolled plane loop stays small.
+template <typename real, int BYT>
+__device__ __noinline__ void sep_surface(const Props<real>& P, real w2, int x, int nx, int y0, int ny,
+                                         const real* T0, real* surf) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
+  real c00[BYT + 1], c10[BYT + 1], c01[BYT + 1], c11[BYT + 1];
+#pragma unroll
+  for (int i = 0; i <= BYT; ++i) {  // element (x, y0 - 1 + i): strip rows i, i+1
+    const real t10 = __shfl_down_sync(FULL, T0[i], 1), t11 = __shfl_down_sync(FULL, T0[i + 1], 1);
+    c00[i] = c10[i] = c01[i] = c11[i] = 0;
+    const int ey = y0 - 1 + i;
+    if (x >= 0 && x < nx - 1 && ey >= 0 && ey < ny - 1) {
+      const real t00 = T0[i], t01 = T0[i + 1];
+#pragma unroll
+      for (int qy = 0; qy < 2; ++qy)
+#pragma unroll
+        for (int qx = 0; qx < 2; ++qx) {
+          const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
+          const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
+          const real Tq4 = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
+          const real q = surface_flux(P, Tq4) * w2;
+          c00[i] += px0 * py0 * q;
+          c10[i] += px1 * py0 * q;
+          c01[i] += px0 * py1 * q;
+          c11[i] += px1 * py1 * q;
+        }
+    }
+  }
+  // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
+#pragma unroll
+  for (int r = 0; r < BYT; ++r) surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
 }
 
 template <typename real, int BYT, int FL>
@@ -537,9 +576,24 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   const int y0 = (blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5)) * BYT;
   const int ntop = a.ne_planes;
   const Props<real>& P = a.p;
-  real dt = 0;
-  if (lane == 0) dt = (real)(*a.dt);
-  dt = __shfl_sync(FULL, dt, 0);
+  // Programmatic dependent launch: the next kernel in the stream may start its
+  // CTAs now; they wait (griddepcontrol.wait) for this grid before touching
+  // its fields.  Without a programmatic dependency both are no-ops.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  // double-precision inputs converted once per CTA: dt and the laser's offsets
+  // from the window origin and power factor (rx, ry, rz, srcP)
+  __shared__ real s_in[5];
+  if (threadIdx.x == 0) {
+    s_in[0] = (real)(*a.dt);
+    if (hLaser) {
+      s_in[1] = (real)(a.ox - a.laser[0]);
+      s_in[2] = (real)(a.oy - a.laser[1]);
+      s_in[3] = (real)(a.oz - a.laser[2]);
+      s_in[4] = (real)(a.src_c * a.laser[6]);
+    }
+  }
+  __syncthreads();
+  const real dt = s_in[0];
   const int subs = a.substrate > (long long)nxy * nz ? nxy * nz : (int)a.substrate;
   const bool xin = x >= 0 && x < nx;
   const bool out_x = lane >= 1 && lane <= SEP_TILE && x < nx;
@@ -563,6 +617,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   };
 
   if (blockIdx.z == gridDim.z - 1) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     // ---- Dirichlet nodes, spread over the threads of this slice: the bottom
     // plane, then the x/y ring of planes 1..nz-1 (perimeter order y0, y1, x0, x1) ----
     const int perim = 2 * nx + 2 * (ny - 2);
@@ -618,20 +673,10 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   const real minv = dt / a.smass;  // 1 / (8 elements' lumped mass)
 
   // laser: x factor times the rows' y factors; lane l keeps the z factor of
-  // plane Z0 + l.  The laser offsets are formed in double by lane 0.
+  // plane Z0 + l.
   real sxy[BYT], szl = 0;
   if (hLaser) {
-    real rx = 0, ry = 0, rz = 0, srcP = 0;
-    if (lane == 0) {
-      rx = (real)(a.ox - a.laser[0]);
-      ry = (real)(a.oy - a.laser[1]);
-      rz = (real)(a.oz - a.laser[2]);
-      srcP = (real)(a.src_c * a.laser[6]);
-    }
-    rx = __shfl_sync(FULL, rx, 0);
-    ry = __shfl_sync(FULL, ry, 0);
-    rz = __shfl_sync(FULL, rz, 0);
-    srcP = __shfl_sync(FULL, srcP, 0);
+    const real rx = s_in[1], ry = s_in[2], rz = s_in[3], srcP = s_in[4];
     const real sx = xin ? srcP * src_factor<real>(x, nx, rx, a.rh[0], a.rir2) : (real)0;
     // lane r < BYT evaluates the y factor of row y0 + r for the whole warp
     const real syl =
@@ -640,6 +685,8 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     for (int r = 0; r < BYT; ++r) sxy[r] = sx * __shfl_sync(FULL, syl, r);
     if (Z0 + lane < Z1) szl = src_factor<real>(Z0 + lane, nz, rz, a.rh[2], a.rid2);
   }
+  // every read and write of a field comes after the preceding grid completed
+  asm volatile("griddepcontrol.wait;" ::: "memory");
 
   int box_w = 0, box_pl = 0;
   bool box_x = false;
@@ -653,7 +700,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
 #pragma unroll
   for (int r = 0; r < BYT; ++r) row_out[r] = out_x && !ring_x && y0 + r > 0 && y0 + r < ny - 1;
 
-  real Tr[4][RY];
+  real Tr[6][RY];
   const real* Tcol = a.T_in + (x + (y0 - 1) * nx);  // strip row 0 of plane 0 (dereferenced only inside the grid)
   auto load_plane = [&](real(&dst)[RY], int pl) {
     const bool ok = xin && pl >= 0 && pl < nz;
@@ -663,9 +710,9 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       dst[i] = (ok && y >= 0 && y < ny) ? Tcol[i * nx + pl * nxy] : (real)0;
     }
   };
-  // per-node inputs of one output plane, loaded one plane ahead
-  uint32_t nph[2][BYT];
-  real nacc[2][BYT], nmac[2][BYT], nrhs[2][BYT];
+  // per-node inputs of one output plane, loaded two planes ahead
+  uint32_t nph[3][BYT];
+  real nacc[3][BYT], nmac[3][BYT], nrhs[3][BYT];
   auto prefetch = [&](auto slot_c, int pl) {
     constexpr int S = decltype(slot_c)::value;
 #pragma unroll
@@ -690,55 +737,27 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   load_plane(Tr[0], Z0 - 1);
   load_plane(Tr[1], Z0);
   load_plane(Tr[2], Z0 + 1);
+  load_plane(Tr[3], Z0 + 2);
   prefetch(std::integral_constant<int, 0>(), Z0);
+  prefetch(std::integral_constant<int, 1>(), Z0 + 1);
 
-  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
-
+  // plane q lives in T slot (q - Z0 + 1) % 6 and per-node slot (q - Z0) % 3;
+  // iteration p issues the loads of plane p + 3 and the inputs of plane p + 2
   auto body = [&](auto par, int p) {
     constexpr int PAR = decltype(par)::value;
-    constexpr int NB = PAR & 1;  // per-node input slot of plane p
-    real(&Tm)[RY] = Tr[PAR & 3];
-    real(&T0)[RY] = Tr[(PAR + 1) & 3];
-    real(&Tp)[RY] = Tr[(PAR + 2) & 3];
-    real(&Tq)[RY] = Tr[(PAR + 3) & 3];
-    if (p + 2 <= Z1) load_plane(Tq, p + 2);
-    prefetch(std::integral_constant<int, NB ^ 1>(), p + 1);
+    constexpr int NB = PAR % 3;  // per-node input slot of plane p
+    real(&Tm)[RY] = Tr[PAR % 6];
+    real(&T0)[RY] = Tr[(PAR + 1) % 6];
+    real(&Tp)[RY] = Tr[(PAR + 2) % 6];
+    if (p + 3 <= Z1) load_plane(Tr[(PAR + 4) % 6], p + 3);
+    prefetch(std::integral_constant<int, (PAR + 2) % 3>(), p + 2);
 
     const bool top = p == ntop;
     // ---- top surface (convection / radiation / evaporation on the faces of element plane ntop-1) ----
     real surf[BYT];
 #pragma unroll
     for (int r = 0; r < BYT; ++r) surf[r] = 0;
-    if (hSurf && top && ntop >= 1) {
-      const real w2 = a.w2;
-      real c00[BYT + 1], c10[BYT + 1], c01[BYT + 1], c11[BYT + 1];
-#pragma unroll
-      for (int i = 0; i <= BYT; ++i) {  // element (x, y0 - 1 + i): strip rows i, i+1
-        const real t10 = __shfl_down_sync(FULL, T0[i], 1), t11 = __shfl_down_sync(FULL, T0[i + 1], 1);
-        c00[i] = c10[i] = c01[i] = c11[i] = 0;
-        const int ey = y0 - 1 + i;
-        if (x >= 0 && x < nx - 1 && ey >= 0 && ey < ny - 1) {
-          const real t00 = T0[i], t01 = T0[i + 1];
-#pragma unroll
-          for (int qy = 0; qy < 2; ++qy)
-#pragma unroll
-            for (int qx = 0; qx < 2; ++qx) {
-              const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
-              const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
-              const real Tq4 = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
-              const real q = surface_flux(P, Tq4) * w2;
-              c00[i] += px0 * py0 * q;
-              c10[i] += px1 * py0 * q;
-              c01[i] += px0 * py1 * q;
-              c11[i] += px1 * py1 * q;
-            }
-        }
-      }
-      // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
-#pragma unroll
-      for (int r = 0; r < BYT; ++r)
-        surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
-    }
+    if (hSurf && top && ntop >= 1) sep_surface<real, BYT>(P, a.w2, x, nx, y0, ny, T0, surf);
 
     // ---- z and y stencils in registers, x stencil by shuffles ----
     real Zm[RY], Zk[RY];
@@ -765,10 +784,11 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       const real w = Zk[i - 1] + Zk[i + 1];
       const real A = a1 * (u + (real)4 * Zm[i]);
       const real B = b1 * ((real)2 * Zm[i] - u) + b2 * (w + (real)4 * Zk[i]);
-      const real Al = __shfl_up_sync(FULL, A, 1), Ar = __shfl_down_sync(FULL, A, 1);
-      const real Bl = __shfl_up_sync(FULL, B, 1), Br = __shfl_down_sync(FULL, B, 1);
+      // x stencil: (2A - A(x-1) - A(x+1)) + (B(x-1) + 4B + B(x+1)) = 2A + 4B + D(x-1) + D(x+1), D = B - A
+      const real D = B - A;
+      const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
       if (!row_out[r] || p == 0) continue;
-      const real KT = ((real)2 * A - Al - Ar) + (Bl + Br + (real)4 * B);
+      const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
       const real Told = T0[i];
       real Rt = -KT;
       if (hLaser) Rt += sxy[r] * sz;
@@ -780,11 +800,13 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     }
   };
 
-  for (int p = Z0; p < Z1; p += 4) {
+  for (int p = Z0; p < Z1; p += 6) {
     body(std::integral_constant<int, 0>(), p);
     if (p + 1 < Z1) body(std::integral_constant<int, 1>(), p + 1);
     if (p + 2 < Z1) body(std::integral_constant<int, 2>(), p + 2);
     if (p + 3 < Z1) body(std::integral_constant<int, 3>(), p + 3);
+    if (p + 4 < Z1) body(std::integral_constant<int, 4>(), p + 4);
+    if (p + 5 < Z1) body(std::integral_constant<int, 5>(), p + 5);
   }
 }
 
@@ -951,25 +973,38 @@ static bool sep_eligible(const gm_level_args* g, int fl) {
 // Separable launch: CTAs of `warps` warps (one x-tile, warps x BYT rows),
 // v.zchunk <= SEP_ZMAX planes.
 template <typename real, int FL, int BYT>
-static void launch_sep_t(const LevelK<real>& a, int warps, int zc, cudaStream_t st) {
+static void launch_sep_t(const LevelK<real>& a, int warps, int zc, bool pdl, cudaStream_t st) {
   LevelK<real> b = a;
   b.zchunk = zc;
   // the last z-slice of CTAs writes the Dirichlet nodes
   const dim3 grid(cdiv(a.nx, SEP_TILE), cdiv(a.ny, warps * BYT), cdiv(a.nz, zc) + 1);
-  level_sep_kernel<real, BYT, FL><<<grid, 32 * warps, 0, st>>>(b);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(32 * warps);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, level_sep_kernel<real, BYT, FL>, b);
 }
 
 template <typename real>
-static int launch_sep(const LevelK<real>& a, int fl, const TuneVal& v, cudaStream_t st) {
-  if ((v.rows != 2 && v.rows != 4) || v.wys < 1 || v.wys > 8 || v.zchunk < 1 || v.zchunk > SEP_ZMAX)
+static int launch_sep(const LevelK<real>& a, int fl, const TuneVal& v, bool pdl, cudaStream_t st) {
+  if ((v.rows != 1 && v.rows != 2 && v.rows != 4) || v.wys < 1 || v.wys > 8 || v.zchunk < 1 ||
+      v.zchunk > SEP_ZMAX)
     return GM_ERR_ARG;
   switch (fl) {
 #define GM_SEP(V)                                                  \
   case V | LF_CONST:                                               \
-    if (v.rows == 2)                                               \
-      launch_sep_t<real, V | LF_CONST, 2>(a, v.wys, v.zchunk, st); \
+    if (v.rows == 1)                                               \
+      launch_sep_t<real, V | LF_CONST, 1>(a, v.wys, v.zchunk, pdl, st); \
+    else if (v.rows == 2)                                          \
+      launch_sep_t<real, V | LF_CONST, 2>(a, v.wys, v.zchunk, pdl, st); \
     else                                                           \
-      launch_sep_t<real, V | LF_CONST, 4>(a, v.wys, v.zchunk, st); \
+      launch_sep_t<real, V | LF_CONST, 4>(a, v.wys, v.zchunk, pdl, st); \
     break;
     GM_SEP(LF_L3)
     GM_SEP(LF_L3ACC)
@@ -1116,7 +1151,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
       sh = TuneVal{0, 0, 0, 0, g->zchunk};
     }
   }
-  if (sh.kernel == 1) return sep_ok ? launch_sep<real>(a, fl, sh, st) : GM_ERR_ARG;
+  if (sh.kernel == 1) return sep_ok ? launch_sep<real>(a, fl, sh, g->pdl != 0, st) : GM_ERR_ARG;
   switch (variant_of(fl)) {
 #define GM_CASE(V)                                        \
   case V:                                                 \
@@ -1307,7 +1342,7 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
   for (int tx : {gm::LT_X, 16})
     for (int zc : zcs) cand.push_back(gm::TuneVal{0, tx, 0, 0, zc});
   if (gm::sep_eligible(a, gm::level_flags(a, p)))
-    for (int rows : {2, 4})
+    for (int rows : {1, 2, 4})
       for (int warps : {2, 4, 8})
         for (int zc : zcs)
           if (zc <= gm::SEP_ZMAX) cand.push_back(gm::TuneVal{1, gm::SEP_TILE, warps, rows, zc});

@@ -147,6 +147,7 @@ class Engine:
         self.s2_prev_lo = None  # Level-0 start of the window last written (S2 snapshot)
         self._pending = None  # MovePlan made by plan_move and not yet applied
         self.use_graph = False  # run gm_subcycle as one CUDA graph per call
+        self.use_pdl = True  # level steps as programmatic dependent launches
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
         self.tmp = None
@@ -582,6 +583,7 @@ class Engine:
         p.ring2[0], p.ring2[1] = self._buf("ring2a", nn2).data_ptr(), self._buf("ring2b", nn2).data_ptr()
         p.ring3[0], p.ring3[1] = self._buf("ring3a", nn3).data_ptr(), self._buf("ring3b", nn3).data_ptr()
         p.graph = 1 if self.use_graph else 0
+        p.pdl = 1 if self.use_pdl else 0
         return p
 
     # ------------------------------------------------------------------

@@ -97,6 +97,10 @@ typedef struct gm_level_args {
   void* accum;                 /* optional melt-time accumulators (Level 3) */
   void* max_accum;
   int zchunk;                  /* node planes per CTA (0: automatic) */
+  int pdl;                     /* 1: the separable kernel may launch as a programmatic dependent of
+                                  the preceding kernel in the stream (its CTAs start early and wait
+                                  for that kernel before touching any field); dt and laser must not
+                                  be written by that kernel.  0: ordinary stream order. */
 } gm_level_args;
 
 int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream);
@@ -233,7 +237,7 @@ int gm_level_batched_launch(const void* desc, const gm_batch_info* info, void* s
  * stencil for constant-property materials (constant k and rho*c; the
  * Level-1/2/3 feature sets of gm_subcycle, all nodes at or below the active
  * element planes unless inactive_amb): a warp owns 30 node columns (tile_x,
- * fixed) and `rows` (2 or 4) y rows, tile_y (1..8) warps a CTA.
+ * fixed) and `rows` (1, 2 or 4) y rows, tile_y (1..8) warps a CTA.
  * zchunk: node planes a CTA marches (at most 32 for kernel 1). */
 typedef struct gm_level_shape {
   int kernel, tile_x, tile_y, rows, zchunk;
@@ -245,8 +249,8 @@ typedef struct gm_level_shape {
 int gm_level_step_shape(const gm_level_args* a, const gm_props* p, const gm_level_shape* shape, void* stream);
 
 /* Autotuner: times gm_level_step for this call over the element tiles
- * (32 x 8, 16 x 16) and, where it applies, the separable kernel (2 or 4 rows
- * a thread, 1, 2 or 4 thread rows), each over the z-chunks (every distinct
+ * (32 x 8, 16 x 16) and, where it applies, the separable kernel (1, 2 or 4
+ * rows a thread, 2, 4 or 8 warps a CTA), each over the z-chunks (every distinct
  * split of the node planes), with CUDA events, `reps` launches each after
  * one untimed launch, and keeps the fastest for later calls with the same
  * dtype, features and grid that leave zchunk at 0.  The timed launches write
@@ -456,6 +460,8 @@ typedef struct gm_subcycle_plan {
   int graph;                 /* 1: capture the call's launches and run them as one CUDA graph, updated in
                                 place from call to call on the same stream (the first call on a stream
                                 issues directly) */
+  int pdl;                   /* 1: level steps launch as programmatic dependents of the kernel before
+                                them (their CTAs start while it drains) */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
