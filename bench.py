@@ -41,7 +41,7 @@ L2_FLUSH_BYTES = 512 << 20
 WORKLOAD_NAME = ("part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, L3 160x160x40 @5um, "
                  "first layer, N2=N3=10, dt3=1.575us")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-PROFILE_FILE = os.path.join(ROOT, "profiles", "level_step_l3_config1.txt")
+PROFILE_FILE = os.path.join(ROOT, "profiles", "level_sep_l3_part_scale.txt")
 
 
 def parse_args():
@@ -67,6 +67,9 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the library's untuned launch shapes (for ncu launch lists: timings under ncu would "
+                         "steer the autotuner)")
     ap.add_argument("--unet-only", action="store_true",
                     help="surrogate kernels alone: forward passes on the part-scale grid and training steps "
                          "(for profiling)")
@@ -177,6 +180,13 @@ def profile_traffic():
 
 
 # ---------------------------------------------------------------------------
+def l3_kernel_name(v):
+    """The Level-3 level-step kernel the bench runs (constant-property workload)."""
+    if v is None or v.kernel == 1:
+        return "level_sep_kernel (Level 3, separable stencil)"
+    return "level_step_kernel (Level 3, element tiles)"
+
+
 def shape_json(v):
     """A measured level-step launch shape (kern.TunedShape) for the JSON line."""
     if v.kernel == 1:
@@ -276,6 +286,7 @@ def run_ours(args):
 
     import _native as N
     import engine
+    import kern
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -300,7 +311,7 @@ def run_ours(args):
         eng = engine.Engine(cfg, P, N2, N3, dtype=dtype, device=dev, stream=stream)
         eng.set_layer(rows[0])
         eng.move(rows[0], vstart)
-        tuned = eng.autotune(rows[0])  # launch shapes of the level steps, measured (set-up, untimed)
+        tuned = {} if args.no_autotune else eng.autotune(rows[0])  # launch shapes, measured (set-up, untimed)
         eng.use_graph = not args.no_graph  # each subcycle call as one CUDA graph
 
         def chunk(k):
@@ -392,12 +403,14 @@ def run_ours(args):
         phout = torch.empty_like(eng.ph[3])
         last = torch.as_tensor(chunk(k - 1)[-1], device=dev)
         # Launched back to back from a CUDA graph, so that the host's per-call
-        # argument marshalling does not gap the launches.
+        # argument marshalling does not gap the launches, and as programmatic
+        # dependents of one another as the subcycle launches them.
         ring = eng._ring(3, eng.T[2], eng.T[2])
         reps = 20
+        l3kw = eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
 
         def l3():
-            eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
+            kern.level_step(eng.ps, stream=stream, pdl=1, **l3kw)
 
         for _ in range(5):
             l3()
@@ -448,7 +461,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 4 if dtype == torch.float32 else 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "level_step_kernel (Level 3)", "kernel_ms": k_ms,
+                     "traffic": traffic, "kernel": l3_kernel_name(tuned.get(3)), "kernel_ms": k_ms,
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,

@@ -189,9 +189,10 @@ class gm_subcycle_plan(C.Structure):
 def subcycle_kernel_count(N2: int, N3: int) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
-    steps (coupling 2, Level-2 solve, Level-3 ring, N3 Level-3 solves,
-    restriction, T'), the T'2/mass/corrector block (7) and the tail (3)."""
-    return 20 + 2 * (1 + N2 * (6 + N3))
+    steps (source copy, coupling 2, Level-2 solve, Level-3 ring, N3 Level-3
+    solves, restriction, T'), the T'2/mass/corrector block (7) and the tail
+    (3)."""
+    return 20 + 2 * (1 + N2 * (7 + N3))
 
 
 _lib = None

@@ -9,6 +9,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <utility>
 #include "gomelt.h"
 
 namespace gm {
@@ -239,5 +241,45 @@ inline Map3<real> make_map3(const gm_map3& m) {
 }
 
 __host__ __device__ inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// Programmatic dependent launch.  A kernel that starts with pdl_begin() lets
+// the next kernel in the stream launch its CTAs early and then waits until
+// the kernel before it has completed (its writes visible) before it touches
+// any field.  Without a programmatic dependency both instructions are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Whether launches through launch_k on this thread carry the programmatic
+// dependency (set by gm_subcycle for the launches of one call).
+inline bool& pdl_mode() {
+  static thread_local bool on = false;
+  return on;
+}
+
+struct PdlScope {
+  bool prev;
+  explicit PdlScope(bool on) : prev(pdl_mode()) { pdl_mode() = on; }
+  ~PdlScope() { pdl_mode() = prev; }
+};
+
+// Kernel launch on `st`, as a programmatic dependent when pdl_mode() is set
+// (only for kernels that begin with pdl_begin()).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                            Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_mode() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace gm

@@ -117,6 +117,7 @@ __device__ __forceinline__ void contract2(const real phA[2][2], const real phB[2
 // All per-element products are sum-factorised along the axes.
 template <typename real>
 __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
+  pdl_begin();
   constexpr int S1 = SB + 1, S2 = S1 * S1;
   __shared__ V4<real> sR[4][SBN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -289,6 +290,7 @@ template <typename real>
 __global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, int lo0, int lo1, int lo2,
                                      const real* partials, real* out, int ob0, int ob1, int ob2, int on0, int on1,
                                      real scale) {
+  pdl_begin();
   const long long tot = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
   const bool per_warp = nchunk > 1;
   const int lane = threadIdx.x & 31;
@@ -323,6 +325,7 @@ __global__ void coarse_source_tables(int np, const double* rows, int n0, int n1,
                                      const real* cw2, const int* flo0, const int* flo1, const int* flo2,
                                      const int* fhi0, const int* fhi1, const int* fhi2, double rsq, double dsq,
                                      real* S) {
+  pdl_begin();
   const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
   const long long tot = (long long)np * per;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
@@ -362,6 +365,7 @@ template <typename real>
 __global__ void coarse_source_assemble(int np, int ng, long long gstride, const double* rows, int n0, int n1, int n2,
                                        int lo0, int lo1, int lo2, const real* S, double cpre, real* out, int ob0,
                                        int ob1, int ob2, int on0, int on1) {
+  pdl_begin();
   const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
   const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nodes * ng;
@@ -449,11 +453,11 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
              pr->cp_solid_a1 == 0.0 && pr->cp_mushy == pr->cp_solid_a0 && pr->cp_fluid == pr->cp_solid_a0;
   long long blocks = (a.nitems + 3) / 4;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  couple_kernel<real><<<(int)blocks, 128, 0, st>>>(a);
+  launch_k(couple_kernel<real>, dim3((int)blocks), dim3(128), 0, st, a);
   if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
   const int ncbx = a.ax[0].ncb, ncby = a.ax[1].ncb, ncbz = a.ax[2].ncb;
   const long long nodes = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
-  couple_gather_kernel<real><<<grid1(a.nchunk > 1 ? nodes * 32 : nodes), 256, 0, st>>>(
+  launch_k(couple_gather_kernel<real>, dim3(grid1(a.nchunk > 1 ? nodes * 32 : nodes)), dim3(256), 0, st,
       ncbx, ncby, ncbz, a.nchunk, g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, a.partials,
       (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1], (real)g->scale);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
@@ -487,7 +491,7 @@ static int do_source(const gm_coarse_source_args* g, const gm_props* pr, cudaStr
   const int n0 = G.ax[0].ncb, n1 = G.ax[1].ncb, n2 = G.ax[2].ncb;
   const long long tabs = (long long)g->npos * ((n0 + 1) + (n1 + 1) + (n2 + 1));
   const double r = pr->laser_radius, d = pr->laser_depth;
-  coarse_source_tables<real><<<grid1(tabs), 128, 0, st>>>(
+  launch_k(coarse_source_tables<real>, dim3(grid1(tabs)), dim3(128), 0, st,
       g->npos, g->rows, n0, n1, n2, g->xq[0], g->xq[1], g->xq[2], (const real*)G.ax[0].cw,
       (const real*)G.ax[1].cw, (const real*)G.ax[2].cw, G.ax[0].flo, G.ax[1].flo, G.ax[2].flo, G.ax[0].fhi,
       G.ax[1].fhi, G.ax[2].fhi, r * r, d * d, (real*)g->scratch);
@@ -496,7 +500,7 @@ static int do_source(const gm_coarse_source_args* g, const gm_props* pr, cudaStr
   const double cpre = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * g->fine_wq;
   const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
   const int ng = g->ngroups > 1 ? g->ngroups : 1;
-  coarse_source_assemble<real><<<grid1(nodes * ng), 256, 0, st>>>(
+  launch_k(coarse_source_assemble<real>, dim3(grid1(nodes * ng)), dim3(256), 0, st,
       g->npos / ng, ng, g->out_group_stride, g->rows, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo,
       (const real*)g->scratch, cpre, (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0],
       g->out_n[1]);

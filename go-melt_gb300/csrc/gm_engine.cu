@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include "gm_common.cuh"
 #include "gomelt.h"
 
 namespace {
@@ -188,6 +189,25 @@ void memzero(Ctx& c, void* ptr, long long elems) {
   if (cudaMemsetAsync(ptr, 0, elems * c.esz, (cudaStream_t)c.st) != cudaSuccess) c.rc = GM_ERR_CUDA;
 }
 
+// Word copy as a kernel, so that it joins the chain of programmatic dependent
+// launches (a memcpy node would break it).
+__global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, long long n) {
+  gm::pdl_begin();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+void copy_k(Ctx& c, void* dst, const void* src, long long bytes) {
+  if (c.rc != GM_OK || dst == src) return;
+  const long long n = bytes / 4;  // element sizes are 4 or 8 bytes
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  if (gm::launch_k(copy_words_kernel, dim3((unsigned)blocks), dim3(256), 0, (cudaStream_t)c.st, (const uint32_t*)src,
+                   (uint32_t*)dst, n) != cudaSuccess)
+    c.rc = GM_ERR_LAUNCH;
+}
+
 void copy(Ctx& c, void* dst, const void* src, long long bytes) {
   if (c.rc != GM_OK || dst == src) return;
   if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)c.st) != cudaSuccess)
@@ -232,7 +252,7 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
   for (int l2 = 0; l2 < N2; ++l2) {
     void* hist_l2 = at(p.tp3hist, l2 * n3, c.esz);
     const double* dt2 = p.dts + 1 + l2;
-    copy(c, p.rhs2, at(p.src2, l2 * nrhs2, c.esz), nrhs2 * c.esz);  // the step's source (computed once)
+    copy_k(c, p.rhs2, at(p.src2, l2 * nrhs2, c.esz), nrhs2 * c.esz);  // the step's source (computed once)
     if (part2)
       couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, hist_l2, Tp3c, dt2);
     else
@@ -286,6 +306,8 @@ bool plan_ok(const gm_subcycle_plan* p) {
 namespace {
 
 int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
+  // every kernel of the call launches as a programmatic dependent of the one before it
+  const gm::PdlScope pdl(p->pdl != 0);
   Ctx c;
   c.p = p;
   c.pr = props;

@@ -522,10 +522,18 @@ constexpr int sep_min_blocks() {
 // sums are gathered from the lane to the left.  Called by every lane of the
 // warp (shuffles); one call per warp and launch, kept out of line so that the
 // unrolled plane loop stays small.
+template <typename real, int N>
+struct RegCol {  // a strip column passed by value (stays in registers across the call)
+  real v[N];
+};
+
 template <typename real, int BYT>
-__device__ __noinline__ void sep_surface(const Props<real>& P, real w2, int x, int nx, int y0, int ny,
-                                         const real* T0, real* surf) {
+__device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real w2, int x, int nx, int y0, int ny,
+                                                      const RegCol<real, BYT + 2> T0c) {
   constexpr unsigned FULL = 0xffffffffu;
+  const real* T0 = T0c.v;
+  RegCol<real, BYT> out;
+  real* surf = out.v;
   const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
   real c00[BYT + 1], c10[BYT + 1], c01[BYT + 1], c11[BYT + 1];
 #pragma unroll
@@ -553,6 +561,7 @@ __device__ __noinline__ void sep_surface(const Props<real>& P, real w2, int x, i
   // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
 #pragma unroll
   for (int r = 0; r < BYT; ++r) surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
+  return out;
 }
 
 template <typename real, int BYT, int FL>
@@ -757,7 +766,14 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     real surf[BYT];
 #pragma unroll
     for (int r = 0; r < BYT; ++r) surf[r] = 0;
-    if (hSurf && top && ntop >= 1) sep_surface<real, BYT>(P, a.w2, x, nx, y0, ny, T0, surf);
+    if (hSurf && top && ntop >= 1) {
+      RegCol<real, RY> col;
+#pragma unroll
+      for (int i = 0; i < RY; ++i) col.v[i] = T0[i];
+      const RegCol<real, BYT> sf = sep_surface<real, BYT>(P, a.w2, x, nx, y0, ny, col);
+#pragma unroll
+      for (int r = 0; r < BYT; ++r) surf[r] = sf.v[r];
+    }
 
     // ---- z and y stencils in registers, x stencil by shuffles ----
     real Zm[RY], Zk[RY];
@@ -1017,9 +1033,9 @@ static int launch_sep(const LevelK<real>& a, int fl, const TuneVal& v, bool pdl,
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
-// Untuned separable shape: 4 rows a thread (2 in FP64), 4-warp CTAs, and
-// the z-chunk (<= SEP_ZMAX) whose CTA count best fills the SMs: busiest SM's
-// CTAs x (planes + 2 halo planes).
+// Untuned separable shape: 2 rows a thread, 4-warp CTAs (the best family on
+// the 161 x 161 x 41 Level-3 window), and the z-chunk (<= SEP_ZMAX) whose CTA
+// count best fills the SMs: busiest SM's CTAs x (planes + 2 halo planes).
 template <typename real>
 static TuneVal sep_default(const gm_level_args* g) {
   static int sms = 0;
@@ -1029,8 +1045,8 @@ static TuneVal sep_default(const gm_level_args* g) {
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     sms = n > 0 ? n : 152;
   }
-  TuneVal v{1, SEP_TILE, 4, sizeof(real) == 4 ? 4 : 2, 1};
-  const int res = 4;  // resident 4-warp CTAs per SM at about 128 registers a thread
+  TuneVal v{1, SEP_TILE, 4, 2, 1};
+  const int res = sizeof(real) == 4 ? 6 : 3;  // resident 4-warp CTAs per SM (about 80 / 128+ registers a thread)
   const long long gxy = (long long)cdiv(g->nx, SEP_TILE) * cdiv(g->ny, v.wys * v.rows);
   double best = -1;
   for (int zc = 2; zc <= min(g->nz, SEP_ZMAX); ++zc) {

@@ -27,6 +27,7 @@ struct InterpK {
 // (:2427-2459).
 template <typename real>
 __global__ void interp_kernel(const InterpK<real> a) {
+  pdl_begin();
   const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
        t += (long long)gridDim.x * blockDim.x) {
@@ -78,6 +79,7 @@ __global__ void w_matrix_kernel(const real* Nc, const int* node, const real* T, 
 template <typename real>
 __global__ void restrict_kernel(int n0, int n1, int n2, const Map3<real> m, const int* cx, const int* cy, const int* cz,
                                 int cnx, int cny, const real* fine, real* coarse) {
+  pdl_begin();
   const long long tot = (long long)n0 * n1 * n2;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
        t += (long long)gridDim.x * blockDim.x) {
@@ -95,6 +97,7 @@ template <typename real>
 __global__ void restrict_s1_kernel(int n0, int n1, int n2, const Map3<real> m, const int* cx, const int* cy,
                                    const int* cz, int cnx, int cny, const uint8_t* fine_ph, int fnx, int fny,
                                    uint8_t* coarse_ph, long long substrate) {
+  pdl_begin();
   const long long tot = (long long)n0 * n1 * n2;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
        t += (long long)gridDim.x * blockDim.x) {
@@ -176,7 +179,7 @@ static int do_interp(const gm_interp_args* g, cudaStream_t st) {
   a.out_term = (real*)g->out_term;
   a.which_term = g->which_term;
   const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
-  interp_kernel<real><<<grid_for(tot), 256, 0, st>>>(a);
+  launch_k(interp_kernel<real>, dim3(grid_for(tot)), dim3(256), 0, st, a);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
@@ -239,13 +242,13 @@ extern "C" int gm_restrict(const gm_restrict_args* g, void* stream) {
   const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
   if (tot == 0) return GM_OK;
   if (g->dtype == GM_F32)
-    restrict_kernel<float><<<grid_for(tot), 256, 0, st>>>(g->n[0], g->n[1], g->n[2], make_map3<float>(g->map),
-                                                           g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
-                                                           (const float*)g->fine, (float*)g->coarse);
+    launch_k(restrict_kernel<float>, dim3(grid_for(tot)), dim3(256), 0, st, g->n[0], g->n[1], g->n[2],
+             make_map3<float>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny, (const float*)g->fine,
+             (float*)g->coarse);
   else if (g->dtype == GM_F64)
-    restrict_kernel<double><<<grid_for(tot), 256, 0, st>>>(g->n[0], g->n[1], g->n[2], make_map3<double>(g->map),
-                                                            g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
-                                                            (const double*)g->fine, (double*)g->coarse);
+    launch_k(restrict_kernel<double>, dim3(grid_for(tot)), dim3(256), 0, st, g->n[0], g->n[1], g->n[2],
+             make_map3<double>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny, (const double*)g->fine,
+             (double*)g->coarse);
   else
     return GM_ERR_ARG;
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
@@ -259,11 +262,11 @@ extern "C" int gm_restrict_s1(const gm_restrict_s1_args* g, void* stream) {
   if (tot == 0 && g->substrate <= 0) return GM_OK;
   const long long work = tot > g->substrate ? tot : g->substrate;
   if (g->dtype == GM_F32)
-    restrict_s1_kernel<float><<<grid_for(work), 256, 0, st>>>(
+    launch_k(restrict_s1_kernel<float>, dim3(grid_for(work)), dim3(256), 0, st,
         g->n[0], g->n[1], g->n[2], make_map3<float>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
         g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
   else if (g->dtype == GM_F64)
-    restrict_s1_kernel<double><<<grid_for(work), 256, 0, st>>>(
+    launch_k(restrict_s1_kernel<double>, dim3(grid_for(work)), dim3(256), 0, st,
         g->n[0], g->n[1], g->n[2], make_map3<double>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny,
         g->fine_ph, g->map.src_nx, g->map.src_ny, g->coarse_ph, g->substrate);
   else
@@ -321,6 +324,7 @@ extern "C" int gm_clamp_min(int dtype, void* T, long long n, double lo, void* st
 template <typename real>
 __global__ void ring_kernel(int nx, int ny, int nz, const Map3<real> m, const real* srcA, const real* srcB,
                             real* outA, real* outB) {
+  pdl_begin();
   const long long nb = (long long)nx * ny;                // bottom plane
   const long long nxf = 2LL * ny * (nz - 1);              // x faces above the bottom
   const long long nyf = 2LL * (nx > 2 ? nx - 2 : 0) * (nz - 1);  // y faces, x interior
@@ -367,13 +371,13 @@ extern "C" int gm_ring_prolong(const gm_ring_args* g, void* stream) {
   const long long tot = nx * ny + 2 * ny * (nz - 1) + 2 * (nx - 2) * (nz - 1);
   cudaStream_t st = (cudaStream_t)stream;
   if (g->dtype == GM_F32)
-    ring_kernel<float><<<grid_for(tot), 256, 0, st>>>(g->nodes[0], g->nodes[1], g->nodes[2], make_map3<float>(g->map),
-                                                      (const float*)g->srcA, (const float*)g->srcB, (float*)g->outA,
-                                                      (float*)g->outB);
+    launch_k(ring_kernel<float>, dim3(grid_for(tot)), dim3(256), 0, st, g->nodes[0], g->nodes[1], g->nodes[2],
+             make_map3<float>(g->map), (const float*)g->srcA, (const float*)g->srcB, (float*)g->outA,
+             (float*)g->outB);
   else if (g->dtype == GM_F64)
-    ring_kernel<double><<<grid_for(tot), 256, 0, st>>>(g->nodes[0], g->nodes[1], g->nodes[2],
-                                                       make_map3<double>(g->map), (const double*)g->srcA,
-                                                       (const double*)g->srcB, (double*)g->outA, (double*)g->outB);
+    launch_k(ring_kernel<double>, dim3(grid_for(tot)), dim3(256), 0, st, g->nodes[0], g->nodes[1], g->nodes[2],
+             make_map3<double>(g->map), (const double*)g->srcA, (const double*)g->srcB, (double*)g->outA,
+             (double*)g->outB);
   else
     return GM_ERR_ARG;
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
