@@ -150,7 +150,7 @@ class gm_couple_args(C.Structure):
                 ("fine_h", C.c_double * 3), ("T", vp), ("ph", C.POINTER(C.c_uint8)), ("substrate", C.c_longlong),
                 ("k_arr", vp), ("rc_arr", vp), ("Tp", vp), ("dTa", vp), ("dTb", vp), ("dt", vp), ("out", vp),
                 ("out_lo", C.c_int * 3), ("out_n", C.c_int * 3), ("scale", C.c_double), ("partials", vp),
-                ("partials_cap", C.c_longlong)]
+                ("partials_cap", C.c_longlong), ("method", C.c_int)]
 
 
 class gm_coarse_source_args(C.Structure):

@@ -409,6 +409,169 @@ static void fill_axes(const gm_couple_geom* g, CoupleAxis<real> ax[3], int* nchu
   }
 }
 
+// ---------------------------------------------------------------------------
+// Separable coupling for constant k and rho*c.  The element sums above are
+// then tensor products of 1-D maps from fine nodes to coarse nodes of the box:
+//   V = k [cf0 (Dx Iy Iz) + cf1 (Ix Dy Iz) + cf2 (Ix Iy Dz)] T'
+//       - (wq/dt) rho c (Ix Iy Iz)(dTa - dTb)
+// with, per axis, D[N, i] = sum over fine elements e of the coarse element
+// N-A (A in {0,1}) of sgn(A) (delta(i = e+1) - delta(i = e)) (the coarse
+// gradient sign times the fine difference; the factor 2 of the two Gauss
+// sides is in cf) and I[N, i] = sum_e sum_s cw[e,s,A] psi_s(i - e) (the
+// coarse weights of the two Gauss sides times the fine linear shape
+// functions).  The contraction runs one axis per kernel: fine box -> (coarse
+// x, fine y, fine z) -> (coarse x, coarse y, fine z) -> coarse nodes.
+// ---------------------------------------------------------------------------
+template <typename real>
+struct SepAxis {
+  const real* cw;  // [(e*2+s)*2 + A]
+  const int* flo;  // fine element range of each coarse element of the box
+  const int* fhi;
+  int ncb;
+};
+
+// weights of fine nodes e and e+1 in the Gauss-side sum of coarse node A
+template <typename real>
+__device__ __forceinline__ void side_weights(const real* cw, int e, int A, real& a0, real& a1) {
+  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;
+  const real w0 = cw[(e * 2 + 0) * 2 + A], w1 = cw[(e * 2 + 1) * 2 + A];
+  a0 = w0 * PQ + w1 * MQ;
+  a1 = w0 * MQ + w1 * PQ;
+}
+
+// x: U0 = Dx T', U1 = Ix T', U2 = Ix (dTa - dTb) on (coarse x, fine y, fine z)
+template <typename real>
+__global__ void couple_sep_x(SepAxis<real> ax, SepAxis<real> ay, SepAxis<real> az, int fnx, long long fnxy,
+                             const real* Tp, const real* dTa, const real* dTb, int NBy, int NBz, real* U,
+                             long long cs) {
+  pdl_begin();
+  const int ncx = ax.ncb;
+  const long long n = (long long)(ncx + 1) * NBy * NBz;
+  const int fy0 = ay.flo[0], fz0 = az.flo[0];
+  const int nfy = ay.fhi[ay.ncb - 1] - fy0 + 1, nfz = az.fhi[az.ncb - 1] - fz0 + 1;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int Nx = (int)(t % (ncx + 1));
+    const long long r = t / (ncx + 1);
+    const int jy = (int)(r % NBy), jz = (int)(r / NBy);
+    if (jy >= nfy || jz >= nfz) continue;
+    const long long base = (long long)(fy0 + jy) * fnx + (fz0 + jz) * fnxy;
+    real uD = 0, uI = 0, uM = 0;
+#pragma unroll
+    for (int A = 1; A >= 0; --A) {
+      const int c = Nx - A;
+      if (c < 0 || c >= ncx) continue;
+      const real sg = A ? (real)1 : (real)-1;
+      for (int e = ax.flo[c]; e < ax.fhi[c]; ++e) {
+        real a0, a1;
+        side_weights(ax.cw, e, A, a0, a1);
+        if (Tp) {
+          const real t0 = Tp[base + e], t1 = Tp[base + e + 1];
+          uD += sg * (t1 - t0);
+          uI += a0 * t0 + a1 * t1;
+        }
+        if (dTa) {
+          const real d0 = dTa[base + e] - dTb[base + e], d1 = dTa[base + e + 1] - dTb[base + e + 1];
+          uM += a0 * d0 + a1 * d1;
+        }
+      }
+    }
+    U[t] = uD;
+    U[cs + t] = uI;
+    U[2 * cs + t] = uM;
+  }
+}
+
+// y: W0 = Iy U0, W1 = Dy U1, W2 = Iy U1, W3 = Iy U2 on (coarse x, coarse y, fine z)
+template <typename real>
+__global__ void couple_sep_y(int ncx, SepAxis<real> ay, SepAxis<real> az, int NBy, int NBz, const real* U,
+                             long long cs, bool flux, bool mass, real* W, long long ws) {
+  pdl_begin();
+  const int ncy = ay.ncb;
+  const long long n = (long long)(ncx + 1) * (ncy + 1) * NBz;
+  const int fy0 = ay.flo[0], fz0 = az.flo[0];
+  const int nfz = az.fhi[az.ncb - 1] - fz0 + 1;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int Nx = (int)(t % (ncx + 1));
+    const long long r = t / (ncx + 1);
+    const int Ny = (int)(r % (ncy + 1)), jz = (int)(r / (ncy + 1));
+    if (jz >= nfz) continue;
+    real w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+#pragma unroll
+    for (int A = 1; A >= 0; --A) {
+      const int c = Ny - A;
+      if (c < 0 || c >= ncy) continue;
+      const real sg = A ? (real)1 : (real)-1;
+      for (int e = ay.flo[c]; e < ay.fhi[c]; ++e) {
+        real a0, a1;
+        side_weights(ay.cw, e, A, a0, a1);
+        const long long i0 = ((long long)jz * NBy + (e - fy0)) * (ncx + 1) + Nx, i1 = i0 + (ncx + 1);
+        if (flux) {
+          const real d0 = U[i0], d1 = U[i1], u0 = U[cs + i0], u1 = U[cs + i1];
+          w0 += a0 * d0 + a1 * d1;
+          w1 += sg * (u1 - u0);
+          w2 += a0 * u0 + a1 * u1;
+        }
+        if (mass) w3 += a0 * U[2 * cs + i0] + a1 * U[2 * cs + i1];
+      }
+    }
+    W[t] = w0;
+    W[ws + t] = w1;
+    W[2 * ws + t] = w2;
+    W[3 * ws + t] = w3;
+  }
+}
+
+// z: the coarse nodes; out[box node] += scale * V
+template <typename real>
+__global__ void couple_sep_z(int ncx, int ncy, SepAxis<real> az, int lo0, int lo1, int lo2, const real* W,
+                             long long ws, bool flux, bool mass, real kcf0, real kcf1, real kcf2, const double* dt,
+                             real mwq, real* out, int ob0, int ob1, int ob2, int on0, int on1, real scale) {
+  pdl_begin();
+  const int ncz = az.ncb;
+  const long long n = (long long)(ncx + 1) * (ncy + 1) * (ncz + 1);
+  const int fz0 = az.flo[0];
+  const real mf = mass ? mwq / (real)(*dt) : (real)0;  // (wq/dt) rho c
+  const long long pl = (long long)(ncx + 1) * (ncy + 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int Nx = (int)(t % (ncx + 1)), Ny = (int)((t / (ncx + 1)) % (ncy + 1)), Nz = (int)(t / pl);
+    real v = 0;
+#pragma unroll
+    for (int A = 1; A >= 0; --A) {
+      const int c = Nz - A;
+      if (c < 0 || c >= ncz) continue;
+      const real sg = A ? (real)1 : (real)-1;
+      for (int e = az.flo[c]; e < az.fhi[c]; ++e) {
+        real a0, a1;
+        side_weights(az.cw, e, A, a0, a1);
+        const long long i0 = (long long)(e - fz0) * pl + (long long)Ny * (ncx + 1) + Nx, i1 = i0 + pl;
+        if (flux)
+          v += kcf0 * (a0 * W[i0] + a1 * W[i1]) + kcf1 * (a0 * W[ws + i0] + a1 * W[ws + i1]) +
+               kcf2 * sg * (W[2 * ws + i1] - W[2 * ws + i0]);
+        if (mass) v -= mf * (a0 * W[3 * ws + i0] + a1 * W[3 * ws + i1]);
+      }
+    }
+    const int gx = lo0 + Nx - ob0, gy = lo1 + Ny - ob1, gz = lo2 + Nz - ob2;
+    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * v;
+  }
+}
+
+// Scratch of the separable path: U (3 channels over coarse x, fine y, fine z)
+// and W (4 channels over coarse x, coarse y, fine z), fine extents bounded by
+// ncb * rmax + 1 per axis.
+static void sep_extents(const gm_couple_geom* g, long long* cs, long long* ws, int* NBy, int* NBz) {
+  *NBy = g->ax[1].ncb * g->ax[1].rmax + 1;
+  *NBz = g->ax[2].ncb * g->ax[2].rmax + 1;
+  *cs = (long long)(g->ax[0].ncb + 1) * *NBy * *NBz;
+  *ws = (long long)(g->ax[0].ncb + 1) * (g->ax[1].ncb + 1) * *NBz;
+}
+
+static long long sep_scratch(const gm_couple_geom* g) {
+  long long cs, ws;
+  int NBy, NBz;
+  sep_extents(g, &cs, &ws, &NBy, &NBz);
+  return 3 * cs + 4 * ws;
+}
+
 static bool geom_ok(const gm_couple_geom* g) {
   for (int d = 0; d < 3; ++d) {
     const gm_couple_axis& a = g->ax[d];
@@ -421,11 +584,52 @@ static bool geom_ok(const gm_couple_geom* g) {
 
 using namespace gm;
 
-extern "C" long long gm_couple_partials_size(const gm_couple_geom* g) {
-  if (!g || !geom_ok(g)) return -1;
+static long long element_scratch(const gm_couple_geom* g) {
   long long items = 1;
   for (int d = 0; d < 3; ++d) items *= (long long)g->ax[d].ncb * cdiv(g->ax[d].rmax, SB);
   return items * 8;
+}
+
+extern "C" long long gm_couple_partials_size(const gm_couple_geom* g) {
+  if (!g || !geom_ok(g)) return -1;
+  const long long a = element_scratch(g), b = sep_scratch(g);
+  return a > b ? a : b;
+}
+
+template <typename real>
+static int do_couple_sep(const gm_couple_args* g, const gm_props* pr, cudaStream_t st) {
+  SepAxis<real> ax[3];
+  for (int d = 0; d < 3; ++d) {
+    ax[d].cw = (const real*)g->geom.ax[d].cw;
+    ax[d].flo = g->geom.ax[d].flo;
+    ax[d].fhi = g->geom.ax[d].fhi;
+    ax[d].ncb = g->geom.ax[d].ncb;
+  }
+  long long cs, ws;
+  int NBy, NBz;
+  sep_extents(&g->geom, &cs, &ws, &NBy, &NBz);
+  real* U = (real*)g->partials;
+  real* W = U + 3 * cs;
+  const bool flux = g->Tp != nullptr, mass = g->dTa != nullptr;
+  const long long fnxy = (long long)g->fine_nodes[0] * g->fine_nodes[1];
+  if (launch_k(couple_sep_x<real>, dim3(grid1(cs)), dim3(256), 0, st, ax[0], ax[1], ax[2], g->fine_nodes[0], fnxy,
+               (const real*)g->Tp, (const real*)g->dTa, (const real*)g->dTb, NBy, NBz, U, cs) != cudaSuccess)
+    return GM_ERR_LAUNCH;
+  if (launch_k(couple_sep_y<real>, dim3(grid1(ws)), dim3(256), 0, st, ax[0].ncb, ax[1], ax[2], NBy, NBz,
+               (const real*)U, cs, flux, mass, W, ws) != cudaSuccess)
+    return GM_ERR_LAUNCH;
+  const double wq = g->fine_h[0] * g->fine_h[1] * g->fine_h[2] / 8.0;
+  const double kc = pr->k_fluid / 1000.0;
+  double kcf[3];
+  for (int d = 0; d < 3; ++d) kcf[d] = kc * (-2.0 * wq / (g->geom.ax[d].H * g->fine_h[d]));
+  const long long nodes = (long long)(ax[0].ncb + 1) * (ax[1].ncb + 1) * (ax[2].ncb + 1);
+  if (launch_k(couple_sep_z<real>, dim3(grid1(nodes)), dim3(256), 0, st, ax[0].ncb, ax[1].ncb, ax[2],
+               g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, (const real*)W, ws, flux, mass,
+               (real)kcf[0], (real)kcf[1], (real)kcf[2], g->dt, (real)(wq * pr->rho * pr->cp_fluid),
+               (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1],
+               (real)g->scale) != cudaSuccess)
+    return GM_ERR_LAUNCH;
+  return GM_OK;
 }
 
 template <typename real>
@@ -477,9 +681,16 @@ extern "C" int gm_couple(const gm_couple_args* g, const gm_props* p, void* strea
   if ((g->k_arr == nullptr) != (g->rc_arr == nullptr)) return GM_ERR_ARG;
   if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
   if ((long long)g->fine_nodes[0] * g->fine_nodes[1] * g->fine_nodes[2] >= (1LL << 31)) return GM_ERR_TOO_LARGE;
-  const long long need = gm_couple_partials_size(&g->geom);
-  if (need < 0 || need > g->partials_cap) return GM_ERR_TOO_LARGE;
+  if (g->method < 0 || g->method > 2) return GM_ERR_ARG;
+  const bool kconst = !g->k_arr && p->k_powder == p->k_bulk_a0 && p->k_fluid == p->k_bulk_a0 &&
+                      p->k_bulk_a1 == 0.0 && p->cp_solid_a1 == 0.0 && p->cp_mushy == p->cp_solid_a0 &&
+                      p->cp_fluid == p->cp_solid_a0;
+  if (g->method == 2 && !kconst) return GM_ERR_ARG;
+  const bool sep = g->method == 2 || (g->method == 0 && kconst && sep_scratch(&g->geom) <= g->partials_cap);
+  const long long need = sep ? sep_scratch(&g->geom) : element_scratch(&g->geom);
+  if (need > g->partials_cap) return GM_ERR_TOO_LARGE;
   cudaStream_t st = (cudaStream_t)stream;
+  if (sep) return g->dtype == GM_F32 ? do_couple_sep<float>(g, p, st) : do_couple_sep<double>(g, p, st);
   if (g->dtype == GM_F32) return do_couple<float>(g, p, st);
   if (g->dtype == GM_F64) return do_couple<double>(g, p, st);
   return GM_ERR_ARG;

@@ -608,7 +608,10 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   const bool out_x = lane >= 1 && lane <= SEP_TILE && x < nx;
   const bool ring_x = x == 0 || x == nx - 1;
 
-  // new phase, output and melt time of node id (old temperature Told, phase byte ph)
+  // New phase, output and melt time of node id (old temperature Told, phase
+  // byte ph).  The melt-time update (acc + dt S2 - reset acc, max(reset acc,
+  // macc)) leaves a node that is not liquid unchanged (macc >= 0), so the
+  // accumulators are read (cAcc, cMacc) and written at liquid nodes only.
   auto finish = [&](int id, real Tn, real Told, uint32_t ph, real cAcc, real cMacc) {
     if (hClamp) Tn = fmax(Tn, P.T_amb);
     a.T_out[id] = Tn;
@@ -616,11 +619,11 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       const bool s2 = Told >= P.T_liquidus;
       const bool s1 = (ph & PH_S1) || s2 || id < subs;
       if (hPhout) a.ph_out[id] = (uint8_t)((s1 ? PH_S1 : 0u) | (s2 ? PH_S2 : 0u));
-      if (hAcc) {
+      if (hAcc && s2) {
         const bool prev2 = (ph & PH_S2) != 0;
-        const real racc = (s2 && !prev2) ? cAcc : (real)0;
+        const real racc = prev2 ? (real)0 : cAcc;
         a.max_accum[id] = fmax(racc, cMacc);
-        a.accum[id] = (cAcc + dt * (s2 ? (real)1 : (real)0)) - racc;
+        a.accum[id] = (cAcc + dt) - racc;
       }
     }
   };
@@ -670,8 +673,10 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       } else {
         Tn = a.bc_alpha * a.bc_new[id] + a.bc_beta * a.bc_old[id];
       }
-      finish(id, Tn, needPh ? a.T_in[id] : (real)0, needPh ? (uint32_t)a.ph_in[id] : 0u,
-             hAcc ? a.accum[id] : (real)0, hAcc ? a.max_accum[id] : (real)0);
+      const real Told = needPh ? a.T_in[id] : (real)0;
+      const bool liq = hAcc && Told >= P.T_liquidus;
+      finish(id, Tn, Told, needPh ? (uint32_t)a.ph_in[id] : 0u, liq ? a.accum[id] : (real)0,
+             liq ? a.max_accum[id] : (real)0);
     }
     return;
   }
@@ -721,7 +726,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   };
   // per-node inputs of one output plane, loaded two planes ahead
   uint32_t nph[3][BYT];
-  real nacc[3][BYT], nmac[3][BYT], nrhs[3][BYT];
+  real nrhs[3][BYT];
   auto prefetch = [&](auto slot_c, int pl) {
     constexpr int S = decltype(slot_c)::value;
 #pragma unroll
@@ -730,16 +735,34 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       const bool ok = row_out[r] && pl < Z1;
       const int id = x + y * nx + pl * nxy;
       nph[S][r] = 0;
-      nacc[S][r] = nmac[S][r] = nrhs[S][r] = 0;
+      nrhs[S][r] = 0;
       if (ok) {
         if (needPh) nph[S][r] = a.ph_in[id];
-        if (hAcc) {
-          nacc[S][r] = a.accum[id];
-          nmac[S][r] = a.max_accum[id];
-        }
         if (hBox && box_x && y >= a.box[2] && y < a.box[3] && pl >= a.box[4] && pl < a.box[5])
           nrhs[S][r] = a.rhs_box[(x - a.box[0]) + (y - a.box[2]) * box_w + (pl - a.box[4]) * box_pl];
       }
+    }
+  };
+  // melt-time accumulators of the liquid nodes of plane pl (T at the step
+  // start in Tc), loaded one plane ahead; warps without liquid nodes skip it
+  real nacc[2][BYT], nmac[2][BYT];
+  auto prefetch_acc = [&](auto slot_c, int pl, const RegCol<real, BYT> Tc) {
+    constexpr int S = decltype(slot_c)::value;
+    bool liq[BYT], any = false;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) {
+      liq[r] = row_out[r] && pl < Z1 && Tc.v[r] >= P.T_liquidus;
+      any = any || liq[r];
+      nacc[S][r] = nmac[S][r] = 0;
+    }
+    if (__any_sync(FULL, any)) {
+#pragma unroll
+      for (int r = 0; r < BYT; ++r)
+        if (liq[r]) {
+          const int id = x + (y0 + r) * nx + pl * nxy;
+          nacc[S][r] = a.accum[id];
+          nmac[S][r] = a.max_accum[id];
+        }
     }
   };
 
@@ -749,6 +772,14 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
   load_plane(Tr[3], Z0 + 2);
   prefetch(std::integral_constant<int, 0>(), Z0);
   prefetch(std::integral_constant<int, 1>(), Z0 + 1);
+  // the output rows of a strip column (strip rows 1..BYT)
+  auto rows_of = [&](const real* c) {
+    RegCol<real, BYT> o;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) o.v[r] = c[r + 1];
+    return o;
+  };
+  if (hAcc) prefetch_acc(std::integral_constant<int, 0>(), Z0, rows_of(Tr[1]));
 
   // plane q lives in T slot (q - Z0 + 1) % 6 and per-node slot (q - Z0) % 3;
   // iteration p issues the loads of plane p + 3 and the inputs of plane p + 2
@@ -760,6 +791,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     real(&Tp)[RY] = Tr[(PAR + 2) % 6];
     if (p + 3 <= Z1) load_plane(Tr[(PAR + 4) % 6], p + 3);
     prefetch(std::integral_constant<int, (PAR + 2) % 3>(), p + 2);
+    if (hAcc) prefetch_acc(std::integral_constant<int, (PAR + 1) & 1>(), p + 1, rows_of(Tp));
 
     const bool top = p == ntop;
     // ---- top surface (convection / radiation / evaporation on the faces of element plane ntop-1) ----
@@ -812,7 +844,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
       if (hSurf) Rt += surf[r];
       real Tn = Told + Rt * mi;
       if (hInact && p > ntop) Tn = P.T_amb;
-      finish(x + (y0 + r) * nx + p * nxy, Tn, Told, nph[NB][r], nacc[NB][r], nmac[NB][r]);
+      finish(x + (y0 + r) * nx + p * nxy, Tn, Told, nph[NB][r], nacc[PAR & 1][r], nmac[PAR & 1][r]);
     }
   };
 

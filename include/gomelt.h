@@ -94,7 +94,10 @@ typedef struct gm_level_args {
   double bc_alpha, bc_beta;
   gm_map3 bc_map;              /* coarse -> this level's nodes */
   int clamp;                   /* 1: T = max(T, T_amb) */
-  void* accum;                 /* optional melt-time accumulators (Level 3) */
+  void* accum;                 /* optional melt-time accumulators (Level 3): accum += dt at liquid nodes,
+                                  reset when a node turns liquid, max_accum = running maximum of the
+                                  reset values.  A node that is not liquid keeps its values (max_accum
+                                  must be >= 0, as it starts at 0), so kernels may skip it. */
   void* max_accum;
   int zchunk;                  /* node planes per CTA (0: automatic) */
   int pdl;                     /* 1: the separable kernel may launch as a programmatic dependent of
@@ -316,7 +319,8 @@ typedef struct gm_couple_geom {
   gm_couple_axis ax[3];
 } gm_couple_geom;
 
-/* Number of scratch elements (dtype) gm_couple needs for `partials`. */
+/* Number of scratch elements (dtype) gm_couple needs for `partials` (enough
+ * for either method). */
 long long gm_couple_partials_size(const gm_couple_geom* g);
 
 /* Fine -> coarse subgrid terms, added into `out` (a dtype array over the
@@ -349,6 +353,8 @@ typedef struct gm_couple_args {
   double scale;
   void* partials;
   long long partials_cap;
+  int method;  /* 0: separable contraction when k and rho*c are constant and the scratch holds it, else
+                  the element reduction; 1: element reduction; 2: separable (constant properties only) */
 } gm_couple_args;
 
 int gm_couple(const gm_couple_args* a, const gm_props* p, void* stream);
