@@ -439,46 +439,108 @@ __device__ __forceinline__ void side_weights(const real* cw, int e, int A, real&
   a1 = w0 * MQ + w1 * PQ;
 }
 
-// x: U0 = Dx T', U1 = Ix T', U2 = Ix (dTa - dTb) on (coarse x, fine y, fine z)
+// x: U0 = Dx T', U1 = Ix T', U2 = Ix (dTa - dTb) on (coarse x, fine y, fine z).
+// One warp per fine row (jy, jz): the row's T' and dTa - dTb are read once,
+// coalesced, into the warp's shared-memory slice; the node weights of the
+// box's fine elements (a0, a1 for A = 0, 1) are staged once per CTA; lane N
+// then sums coarse node N over its fine elements.  Consecutive lanes read
+// elements rmax apart; shared indices are padded (i + i/32) so that rmax = 4
+// (the 5 um / 20 um ratio) reads hit 32 distinct banks.
+__host__ __device__ inline int cpad(int i) { return i + (i >> 5); }
+
 template <typename real>
 __global__ void couple_sep_x(SepAxis<real> ax, SepAxis<real> ay, SepAxis<real> az, int fnx, long long fnxy,
-                             const real* Tp, const real* dTa, const real* dTb, int NBy, int NBz, real* U,
+                             const real* Tp, const real* dTa, const real* dTb, int NBy, int NBz, int nfxb, real* U,
                              long long cs) {
   pdl_begin();
+  extern __shared__ __align__(16) unsigned char couple_smem[];
+  const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int P = cpad(nfxb) + 1;  // padded length of one per-node or per-element array
+  real* sW = reinterpret_cast<real*>(couple_smem);  // [4][P]: a0(A=0), a1(A=0), a0(A=1), a1(A=1)
+  real* sF = sW + 4 * P + (long long)warp * 2 * P;   // [2][P]: T', dTa - dTb of the row
   const int ncx = ax.ncb;
-  const long long n = (long long)(ncx + 1) * NBy * NBz;
+  const int fx0 = ax.flo[0], nfx = ax.fhi[ncx - 1] - fx0 + 1;  // fine nodes of the box along x (<= nfxb)
   const int fy0 = ay.flo[0], fz0 = az.flo[0];
   const int nfy = ay.fhi[ay.ncb - 1] - fy0 + 1, nfz = az.fhi[az.ncb - 1] - fz0 + 1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int Nx = (int)(t % (ncx + 1));
-    const long long r = t / (ncx + 1);
-    const int jy = (int)(r % NBy), jz = (int)(r / NBy);
-    if (jy >= nfy || jz >= nfz) continue;
-    const long long base = (long long)(fy0 + jy) * fnx + (fz0 + jz) * fnxy;
-    real uD = 0, uI = 0, uM = 0;
+  for (int le = threadIdx.x; le < nfx - 1; le += blockDim.x) {
 #pragma unroll
-    for (int A = 1; A >= 0; --A) {
-      const int c = Nx - A;
-      if (c < 0 || c >= ncx) continue;
-      const real sg = A ? (real)1 : (real)-1;
-      for (int e = ax.flo[c]; e < ax.fhi[c]; ++e) {
-        real a0, a1;
-        side_weights(ax.cw, e, A, a0, a1);
-        if (Tp) {
-          const real t0 = Tp[base + e], t1 = Tp[base + e + 1];
+    for (int A = 0; A < 2; ++A) {
+      real a0, a1;
+      side_weights(ax.cw, fx0 + le, A, a0, a1);
+      sW[(2 * A) * P + cpad(le)] = a0;
+      sW[(2 * A + 1) * P + cpad(le)] = a1;
+    }
+  }
+  __syncthreads();
+  const long long nrows = (long long)NBy * NBz;
+  for (long long row = (long long)blockIdx.x * warps + warp; row < nrows; row += (long long)gridDim.x * warps) {
+    const int jy = (int)(row % NBy), jz = (int)(row / NBy);
+    if (jy >= nfy || jz >= nfz) continue;  // the same for the whole warp
+    const long long base = fx0 + (long long)(fy0 + jy) * fnx + (fz0 + jz) * fnxy;
+    for (int i = lane; i < nfx; i += 32) {
+      sF[cpad(i)] = Tp ? Tp[base + i] : (real)0;
+      sF[P + cpad(i)] = dTa ? dTa[base + i] - dTb[base + i] : (real)0;
+    }
+    __syncwarp();
+    for (int Nx = lane; Nx <= ncx; Nx += 32) {
+      real uD = 0, uI = 0, uM = 0;
+#pragma unroll
+      for (int A = 1; A >= 0; --A) {
+        const int c = Nx - A;
+        if (c < 0 || c >= ncx) continue;
+        const real sg = A ? (real)1 : (real)-1;
+        const real* w0 = sW + (2 * A) * P;
+        const real* w1 = sW + (2 * A + 1) * P;
+        const int e1 = ax.fhi[c] - fx0;
+        for (int le = ax.flo[c] - fx0; le < e1; ++le) {
+          const int q0 = cpad(le), q1 = cpad(le + 1);
+          const real a0 = w0[q0], a1 = w1[q0];
+          const real t0 = sF[q0], t1 = sF[q1];
           uD += sg * (t1 - t0);
           uI += a0 * t0 + a1 * t1;
-        }
-        if (dTa) {
-          const real d0 = dTa[base + e] - dTb[base + e], d1 = dTa[base + e + 1] - dTb[base + e + 1];
-          uM += a0 * d0 + a1 * d1;
+          uM += a0 * sF[P + q0] + a1 * sF[P + q1];
         }
       }
+      const long long t = row * (ncx + 1) + Nx;
+      U[t] = uD;
+      U[cs + t] = uI;
+      U[2 * cs + t] = uM;
     }
-    U[t] = uD;
-    U[cs + t] = uI;
-    U[2 * cs + t] = uM;
+    __syncwarp();
   }
+}
+
+// The y and z contractions give each output CSUB lanes: lane j of the group
+// takes the j-th, (j+CSUB)-th, ... fine element of the node's list (the
+// elements of coarse element N-1 with A = 1, then those of N with A = 0), and
+// the group's partial sums are added by a fixed shuffle tree (deterministic).
+constexpr int CSUB = 4;
+
+template <typename real>
+__device__ __forceinline__ real csub_sum(real v) {
+#pragma unroll
+  for (int o = CSUB / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// element k of coarse node N's list: sets (e, A); false past the end
+template <typename real>
+__device__ __forceinline__ bool node_elem(const SepAxis<real>& ax, int N, int k, int& e, int& A) {
+  if (N >= 1) {
+    const int n1 = ax.fhi[N - 1] - ax.flo[N - 1];
+    if (k < n1) {
+      e = ax.flo[N - 1] + k;
+      A = 1;
+      return true;
+    }
+    k -= n1;
+  }
+  if (N < ax.ncb && k < ax.fhi[N] - ax.flo[N]) {
+    e = ax.flo[N] + k;
+    A = 0;
+    return true;
+  }
+  return false;
 }
 
 // y: W0 = Iy U0, W1 = Dy U1, W2 = Iy U1, W3 = Iy U2 on (coarse x, coarse y, fine z)
@@ -490,20 +552,23 @@ __global__ void couple_sep_y(int ncx, SepAxis<real> ay, SepAxis<real> az, int NB
   const long long n = (long long)(ncx + 1) * (ncy + 1) * NBz;
   const int fy0 = ay.flo[0], fz0 = az.flo[0];
   const int nfz = az.fhi[az.ncb - 1] - fz0 + 1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+  const int sub = threadIdx.x % CSUB;
+  // the loop runs the same number of times in every lane group of a warp
+  const long long stride = (long long)gridDim.x * (blockDim.x / CSUB);
+  const long long t_first = blockIdx.x * (long long)(blockDim.x / CSUB) + threadIdx.x / CSUB;
+  const long long n_up = (n + 31) / 32 * 32;
+  for (long long t = t_first; t < n_up; t += stride) {
+    real w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+    const bool live = t < n;
     const int Nx = (int)(t % (ncx + 1));
     const long long r = t / (ncx + 1);
     const int Ny = (int)(r % (ncy + 1)), jz = (int)(r / (ncy + 1));
-    if (jz >= nfz) continue;
-    real w0 = 0, w1 = 0, w2 = 0, w3 = 0;
-#pragma unroll
-    for (int A = 1; A >= 0; --A) {
-      const int c = Ny - A;
-      if (c < 0 || c >= ncy) continue;
-      const real sg = A ? (real)1 : (real)-1;
-      for (int e = ay.flo[c]; e < ay.fhi[c]; ++e) {
+    if (live && jz < nfz) {
+      int e, A;
+      for (int k = sub; node_elem(ay, Ny, k, e, A); k += CSUB) {
         real a0, a1;
         side_weights(ay.cw, e, A, a0, a1);
+        const real sg = A ? (real)1 : (real)-1;
         const long long i0 = ((long long)jz * NBy + (e - fy0)) * (ncx + 1) + Nx, i1 = i0 + (ncx + 1);
         if (flux) {
           const real d0 = U[i0], d1 = U[i1], u0 = U[cs + i0], u1 = U[cs + i1];
@@ -514,10 +579,16 @@ __global__ void couple_sep_y(int ncx, SepAxis<real> ay, SepAxis<real> az, int NB
         if (mass) w3 += a0 * U[2 * cs + i0] + a1 * U[2 * cs + i1];
       }
     }
-    W[t] = w0;
-    W[ws + t] = w1;
-    W[2 * ws + t] = w2;
-    W[3 * ws + t] = w3;
+    w0 = csub_sum(w0);
+    w1 = csub_sum(w1);
+    w2 = csub_sum(w2);
+    w3 = csub_sum(w3);
+    if (live && sub == 0) {
+      W[t] = w0;
+      W[ws + t] = w1;
+      W[2 * ws + t] = w2;
+      W[3 * ws + t] = w3;
+    }
   }
 }
 
@@ -532,17 +603,20 @@ __global__ void couple_sep_z(int ncx, int ncy, SepAxis<real> az, int lo0, int lo
   const int fz0 = az.flo[0];
   const real mf = mass ? mwq / (real)(*dt) : (real)0;  // (wq/dt) rho c
   const long long pl = (long long)(ncx + 1) * (ncy + 1);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int Nx = (int)(t % (ncx + 1)), Ny = (int)((t / (ncx + 1)) % (ncy + 1)), Nz = (int)(t / pl);
+  const int sub = threadIdx.x % CSUB;
+  const long long stride = (long long)gridDim.x * (blockDim.x / CSUB);
+  const long long t_first = blockIdx.x * (long long)(blockDim.x / CSUB) + threadIdx.x / CSUB;
+  const long long n_up = (n + 31) / 32 * 32;
+  for (long long t = t_first; t < n_up; t += stride) {
     real v = 0;
-#pragma unroll
-    for (int A = 1; A >= 0; --A) {
-      const int c = Nz - A;
-      if (c < 0 || c >= ncz) continue;
-      const real sg = A ? (real)1 : (real)-1;
-      for (int e = az.flo[c]; e < az.fhi[c]; ++e) {
+    const bool live = t < n;
+    const int Nx = (int)(t % (ncx + 1)), Ny = (int)((t / (ncx + 1)) % (ncy + 1)), Nz = (int)(t / pl);
+    if (live) {
+      int e, A;
+      for (int k = sub; node_elem(az, Nz, k, e, A); k += CSUB) {
         real a0, a1;
         side_weights(az.cw, e, A, a0, a1);
+        const real sg = A ? (real)1 : (real)-1;
         const long long i0 = (long long)(e - fz0) * pl + (long long)Ny * (ncx + 1) + Nx, i1 = i0 + pl;
         if (flux)
           v += kcf0 * (a0 * W[i0] + a1 * W[i1]) + kcf1 * (a0 * W[ws + i0] + a1 * W[ws + i1]) +
@@ -550,14 +624,32 @@ __global__ void couple_sep_z(int ncx, int ncy, SepAxis<real> az, int lo0, int lo
         if (mass) v -= mf * (a0 * W[3 * ws + i0] + a1 * W[3 * ws + i1]);
       }
     }
-    const int gx = lo0 + Nx - ob0, gy = lo1 + Ny - ob1, gz = lo2 + Nz - ob2;
-    out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * v;
+    v = csub_sum(v);
+    if (live && sub == 0) {
+      const int gx = lo0 + Nx - ob0, gy = lo1 + Ny - ob1, gz = lo2 + Nz - ob2;
+      out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * v;
+    }
   }
 }
 
 // Scratch of the separable path: U (3 channels over coarse x, fine y, fine z)
 // and W (4 channels over coarse x, coarse y, fine z), fine extents bounded by
 // ncb * rmax + 1 per axis.
+// x-kernel CTA shape: warps a CTA and dynamic shared memory (bytes), 0 warps
+// when one fine row does not fit.
+static void sep_x_shape(const gm_couple_geom* g, size_t esz, int* warps, size_t* smem) {
+  const long long nfxb = (long long)g->ax[0].ncb * g->ax[0].rmax + 1;
+  const long long P = cpad((int)nfxb) + 1;
+  const long long fixed = 4 * P * (long long)esz, per = 2 * P * (long long)esz;
+  *warps = 0;
+  for (int w = 8; w >= 1; w >>= 1)
+    if (fixed + w * per <= 48 * 1024) {
+      *warps = w;
+      break;
+    }
+  *smem = (size_t)(fixed + *warps * per);
+}
+
 static void sep_extents(const gm_couple_geom* g, long long* cs, long long* ws, int* NBy, int* NBz) {
   *NBy = g->ax[1].ncb * g->ax[1].rmax + 1;
   *NBz = g->ax[2].ncb * g->ax[2].rmax + 1;
@@ -612,10 +704,17 @@ static int do_couple_sep(const gm_couple_args* g, const gm_props* pr, cudaStream
   real* W = U + 3 * cs;
   const bool flux = g->Tp != nullptr, mass = g->dTa != nullptr;
   const long long fnxy = (long long)g->fine_nodes[0] * g->fine_nodes[1];
-  if (launch_k(couple_sep_x<real>, dim3(grid1(cs)), dim3(256), 0, st, ax[0], ax[1], ax[2], g->fine_nodes[0], fnxy,
-               (const real*)g->Tp, (const real*)g->dTa, (const real*)g->dTb, NBy, NBz, U, cs) != cudaSuccess)
+  int xw;
+  size_t xsm;
+  sep_x_shape(&g->geom, sizeof(real), &xw, &xsm);
+  if (xw < 1) return GM_ERR_TOO_LARGE;
+  const int nfxb = g->geom.ax[0].ncb * g->geom.ax[0].rmax + 1;
+  const long long rows = (long long)NBy * NBz;
+  if (launch_k(couple_sep_x<real>, dim3(grid1(rows, xw)), dim3(32 * xw), xsm, st, ax[0], ax[1], ax[2],
+               g->fine_nodes[0], fnxy, (const real*)g->Tp, (const real*)g->dTa, (const real*)g->dTb, NBy, NBz, nfxb,
+               U, cs) != cudaSuccess)
     return GM_ERR_LAUNCH;
-  if (launch_k(couple_sep_y<real>, dim3(grid1(ws)), dim3(256), 0, st, ax[0].ncb, ax[1], ax[2], NBy, NBz,
+  if (launch_k(couple_sep_y<real>, dim3(grid1(ws * CSUB)), dim3(256), 0, st, ax[0].ncb, ax[1], ax[2], NBy, NBz,
                (const real*)U, cs, flux, mass, W, ws) != cudaSuccess)
     return GM_ERR_LAUNCH;
   const double wq = g->fine_h[0] * g->fine_h[1] * g->fine_h[2] / 8.0;
@@ -623,7 +722,7 @@ static int do_couple_sep(const gm_couple_args* g, const gm_props* pr, cudaStream
   double kcf[3];
   for (int d = 0; d < 3; ++d) kcf[d] = kc * (-2.0 * wq / (g->geom.ax[d].H * g->fine_h[d]));
   const long long nodes = (long long)(ax[0].ncb + 1) * (ax[1].ncb + 1) * (ax[2].ncb + 1);
-  if (launch_k(couple_sep_z<real>, dim3(grid1(nodes)), dim3(256), 0, st, ax[0].ncb, ax[1].ncb, ax[2],
+  if (launch_k(couple_sep_z<real>, dim3(grid1(nodes * CSUB)), dim3(256), 0, st, ax[0].ncb, ax[1].ncb, ax[2],
                g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, (const real*)W, ws, flux, mass,
                (real)kcf[0], (real)kcf[1], (real)kcf[2], g->dt, (real)(wq * pr->rho * pr->cp_fluid),
                (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1],
@@ -686,7 +785,12 @@ extern "C" int gm_couple(const gm_couple_args* g, const gm_props* p, void* strea
                       p->k_bulk_a1 == 0.0 && p->cp_solid_a1 == 0.0 && p->cp_mushy == p->cp_solid_a0 &&
                       p->cp_fluid == p->cp_solid_a0;
   if (g->method == 2 && !kconst) return GM_ERR_ARG;
-  const bool sep = g->method == 2 || (g->method == 0 && kconst && sep_scratch(&g->geom) <= g->partials_cap);
+  int xw;
+  size_t xsm;
+  sep_x_shape(&g->geom, g->dtype == GM_F64 ? 8 : 4, &xw, &xsm);
+  if (g->method == 2 && xw < 1) return GM_ERR_TOO_LARGE;
+  const bool sep =
+      g->method == 2 || (g->method == 0 && kconst && xw >= 1 && sep_scratch(&g->geom) <= g->partials_cap);
   const long long need = sep ? sep_scratch(&g->geom) : element_scratch(&g->geom);
   if (need > g->partials_cap) return GM_ERR_TOO_LARGE;
   cudaStream_t st = (cudaStream_t)stream;

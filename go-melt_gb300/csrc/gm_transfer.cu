@@ -25,18 +25,59 @@ struct InterpK {
 // interpolatePoints / interpolate_w_matrix (computeFunctions.py:1110-1210),
 // the T' of getNewTprime (:2097) and the field remap of moveEverything
 // (:2427-2459).
+// Launch: x threads over i, grid (ceil(n0 / blockDim.x), ceil(n1 / IROWS),
+// n2): no index is divided, and a thread keeps its x weights over IROWS rows.
+// The eight trilinear weights and their validity rule are those of
+// map3_weights.
+constexpr int IROWS = 8;
 template <typename real>
 __global__ void interp_kernel(const InterpK<real> a) {
   pdl_begin();
-  const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % a.n[0]);
-    const int j = (int)((t / a.n[0]) % a.n[1]);
-    const int k = (int)(t / ((long long)a.n[0] * a.n[1]));
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
+  if (i >= a.n[0]) return;
+  int ex[3], ez[3];
+  real x0[3], x1[3], z0[3], z1[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    if (q >= a.nterms) break;
+    const Map3<real>& m = a.map[q];
+    ex[q] = m.ax[0].e[i];
+    x0[q] = m.ax[0].w[2 * i];
+    x1[q] = m.ax[0].w[2 * i + 1];
+    ez[q] = m.ax[2].e[k];
+    z0[q] = m.ax[2].w[2 * k];
+    z1[q] = m.ax[2].w[2 * k + 1];
+  }
+  const int j1 = min(a.n[1], (int)(blockIdx.y + 1) * IROWS);
+  for (int j = blockIdx.y * IROWS; j < j1; ++j) {
+    const long long t = i + (long long)a.n[0] * (j + (long long)a.n[1] * k);
     real acc = a.base ? a.base[t] : (real)0;
-    for (int q = 0; q < a.nterms; ++q) {
-      const real v = map3_apply(a.map[q], i, j, k, a.src[q]);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (q >= a.nterms) break;
+      const Map3<real>& m = a.map[q];
+      const int ey = m.ax[1].e[j];
+      const real y0 = m.ax[1].w[2 * j], y1 = m.ax[1].w[2 * j + 1];
+      real w8[8];
+      w8[0] = x0[q] * y0 * z0[q];
+      w8[1] = x1[q] * y0 * z0[q];
+      w8[2] = x1[q] * y1 * z0[q];
+      w8[3] = x0[q] * y1 * z0[q];
+      w8[4] = x0[q] * y0 * z1[q];
+      w8[5] = x1[q] * y0 * z1[q];
+      w8[6] = x1[q] * y1 * z1[q];
+      w8[7] = x0[q] * y1 * z1[q];
+      bool ok = true;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) ok = ok && (w8[r] >= (real)-1e-2) && (w8[r] <= (real)(1 + 1e-2));
+#pragma unroll
+      for (int r = 0; r < 8; ++r) w8[r] = ok ? fmin(fmax(w8[r], (real)0), (real)1) : (real)0;
+      const int sx = 1, sy = m.src_nx, sz = m.src_nx * m.src_ny;
+      const int b = ex[q] + ey * sy + ez[q] * sz;
+      const real* u = a.src[q];
+      const real v = w8[0] * u[b] + w8[1] * u[b + sx] + w8[2] * u[b + sx + sy] + w8[3] * u[b + sy] +
+                     w8[4] * u[b + sz] + w8[5] * u[b + sx + sz] + w8[6] * u[b + sx + sy + sz] +
+                     w8[7] * u[b + sy + sz];
       if (a.out_term && q == a.which_term) a.out_term[t] = v;
       acc = acc + a.coef[q] * v;
     }
@@ -178,8 +219,8 @@ static int do_interp(const gm_interp_args* g, cudaStream_t st) {
   a.out = (real*)g->out;
   a.out_term = (real*)g->out_term;
   a.which_term = g->which_term;
-  const long long tot = (long long)a.n[0] * a.n[1] * a.n[2];
-  launch_k(interp_kernel<real>, dim3(grid_for(tot)), dim3(256), 0, st, a);
+  const int bx = a.n[0] <= 256 ? 32 * cdiv(a.n[0], 32) : 256;
+  launch_k(interp_kernel<real>, dim3(cdiv(a.n[0], bx), cdiv(a.n[1], IROWS), a.n[2]), dim3(bx), 0, st, a);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
@@ -196,7 +237,7 @@ static bool map_ok(const gm_map3& m, const int n[3]) {
 extern "C" int gm_interp(const gm_interp_args* g, void* stream) {
   if (!g || !g->out || g->nterms < 1 || g->nterms > 3) return GM_ERR_ARG;
   for (int d = 0; d < 3; ++d)
-    if (g->n[d] < 1) return GM_ERR_ARG;
+    if (g->n[d] < 1 || g->n[d] > 65535) return GM_ERR_ARG;  // rows and planes index the launch grid
   for (int q = 0; q < g->nterms; ++q)
     if (!g->src[q] || !map_ok(g->map[q], g->n) || g->src[q] == g->out) return GM_ERR_ARG;
   if (g->out_term && (g->which_term < 0 || g->which_term >= g->nterms)) return GM_ERR_ARG;
