@@ -677,7 +677,11 @@ def run_batched(args):
                 ring = e._ring(3, e.T[2], e.T[2])
                 kw = e.level_kwargs(3, e.T[3], T_out, row[5:6], e.ph[3], ph_out, laser=row, ring=ring, alpha=0.5)
             else:
-                kw = e.level_kwargs(1, e.T[1], T_out, row[5:6] * 100, e.ph[1], ph_out)
+                # the subcycle's Level-1 step: RHS on the coupling box, phase kept
+                cg = e.tables["c21"]
+                box = [v for d in range(3) for v in (cg.box_lo[d], cg.box_lo[d] + cg.box_n[d])]
+                rhs = torch.zeros(int(np.prod(cg.box_n)), dtype=e.T[1].dtype, device=e.T[1].device)
+                kw = e.level_kwargs(1, e.T[1], T_out, row[5:6] * 100, e.ph[1], None, rhs=rhs, box=box)
             kws.append(kw)
         nodes = sum(int(np.prod(kw["nodes"])) for kw in kws)
         args_arr = (N.gm_level_args * len(kws))(*[kern.level_args(**kw) for kw in kws])

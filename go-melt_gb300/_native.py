@@ -94,7 +94,8 @@ class gm_surr_args(C.Structure):
 
 
 class gm_batch_info(C.Structure):
-    _fields_ = [("nb", C.c_int), ("dtype", C.c_int), ("variant", C.c_int), ("blocks", C.c_int)]
+    _fields_ = [("nb", C.c_int), ("dtype", C.c_int), ("variant", C.c_int), ("blocks", C.c_int),
+                ("kernel", C.c_int), ("rows", C.c_int), ("warps", C.c_int)]
 
 
 class gm_tune_result(C.Structure):

@@ -564,8 +564,11 @@ __device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real 
   return out;
 }
 
+// One CTA of the separable step: x-tile bx, strip group by, z-chunk bz of a
+// (gx, gy, ring_z + 1) grid; z-chunk ring_z is the Dirichlet slice.
 template <typename real, int BYT, int FL>
-__global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_kernel(const LevelK<real> a) {
+__device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, int bz, int gx, int gy,
+                                         int ring_z) {
   constexpr int RY = BYT + 2;  // strip rows with the two y halo rows
   constexpr unsigned FULL = 0xffffffffu;
   constexpr bool hLaser = (FL & LF_LASER) != 0;
@@ -581,8 +584,8 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
 
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxy = nx * ny;
   const int lane = threadIdx.x & 31;
-  const int x = blockIdx.x * SEP_TILE - 1 + lane;
-  const int y0 = (blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5)) * BYT;
+  const int x = bx * SEP_TILE - 1 + lane;
+  const int y0 = (by * (blockDim.x >> 5) + (threadIdx.x >> 5)) * BYT;
   const int ntop = a.ne_planes;
   const Props<real>& P = a.p;
   // Programmatic dependent launch: the next kernel in the stream may start its
@@ -628,14 +631,14 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     }
   };
 
-  if (blockIdx.z == gridDim.z - 1) {
+  if (bz == ring_z) {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // ---- Dirichlet nodes, spread over the threads of this slice: the bottom
     // plane, then the x/y ring of planes 1..nz-1 (perimeter order y0, y1, x0, x1) ----
     const int perim = 2 * nx + 2 * (ny - 2);
     const long long nring = (long long)nxy + (long long)(nz - 1) * perim;
-    const long long nthr = (long long)gridDim.x * gridDim.y * blockDim.x;
-    const long long t0 = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long nthr = (long long)gx * gy * blockDim.x;
+    const long long t0 = ((long long)by * gx + bx) * blockDim.x + threadIdx.x;
 #pragma unroll 4
     for (long long k = t0; k < nring; k += nthr) {
       int rx, ry, rp;
@@ -681,7 +684,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     return;
   }
 
-  const int Z0 = blockIdx.z * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  const int Z0 = bz * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
   // stencil constants: A = a1 (Zm- + 4 Zm + Zm+), B = b1 Ky(Zm) + b2 My(Zk)
   const real a1 = a.sa1, b1 = a.sb1, b2 = a.sb2;
   const real minv = dt / a.smass;  // 1 / (8 elements' lumped mass)
@@ -856,6 +859,44 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
     if (p + 4 < Z1) body(std::integral_constant<int, 4>(), p + 4);
     if (p + 5 < Z1) body(std::integral_constant<int, 5>(), p + 5);
   }
+}
+
+template <typename real, int BYT, int FL>
+__global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_kernel(const LevelK<real> a) {
+  sep_body<real, BYT, FL>(a, blockIdx.x, blockIdx.y, blockIdx.z, gridDim.x, gridDim.y, gridDim.z - 1);
+}
+
+// Many windows in one launch: instance b owns the linear CTAs
+// [first[b], first[b+1]) of the grid, laid out (bx, by, bz) with bx fastest
+// over its own (gx, gy, z-chunks + Dirichlet slice) grid; its parameters are
+// read from tab[b] into shared memory once per CTA.
+template <typename real, int BYT, int FL>
+__global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>())
+    level_sep_batched_kernel(const LevelK<real>* __restrict__ tab, const int* __restrict__ first, int nb) {
+  __shared__ LevelK<real> sa;
+  __shared__ int sb[6];
+  if (threadIdx.x == 0) {
+    const int blk = blockIdx.x;
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {  // last instance with first[b] <= blk
+      const int mid = (lo + hi + 1) >> 1;
+      if (first[mid] <= blk)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    sa = tab[lo];
+    const int local = blk - first[lo];
+    const int gx = cdiv(sa.nx, SEP_TILE), gy = cdiv(sa.ny, (int)(blockDim.x >> 5) * BYT);
+    sb[0] = local % gx;
+    sb[1] = (local / gx) % gy;
+    sb[2] = local / (gx * gy);
+    sb[3] = gx;
+    sb[4] = gy;
+    sb[5] = cdiv(sa.nz, sa.zchunk);  // the Dirichlet slice
+  }
+  __syncthreads();
+  sep_body<real, BYT, FL>(sa, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
 }
 
 // Many level windows (instances of uneven sizes) in one launch: instance b
@@ -1213,13 +1254,16 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
-// Batched launches (32 x 8 tiles).  The descriptor buffer holds a small
-// header {nb, dtype, variant, total blocks}, the per-instance LevelK array
+// Batched launches: the separable kernel (2 rows x 4 warps) when every
+// instance is a constant-property call it serves, else 32 x 8 element tiles.
+// The descriptor buffer holds a small header {nb, dtype, variant, total
+// blocks, kernel, rows, warps}, the per-instance LevelK array
 // and the block prefix first[nb + 1]; a launch reads only device memory, so
 // it can be captured in a CUDA graph and replayed.
 struct BatchHeader {
-  int nb, dtype, variant, blocks;
+  int nb, dtype, variant, blocks, kernel, rows, warps;
 };
+constexpr int SEP_BATCH_ROWS = 2, SEP_BATCH_WARPS = 4;  // separable batch shape
 static size_t batch_tab_offset() { return 256; }
 template <typename real>
 static size_t batch_first_offset(int nb) {
@@ -1233,6 +1277,55 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
   const int fl = level_flags(&g[0], &p[0]);
   std::vector<int> first(nb + 1);
   first[0] = 0;
+  bool sep = true;
+  for (int b = 0; b < nb; ++b) sep = sep && level_flags(&g[b], &p[b]) == fl && sep_eligible(&g[b], fl);
+  if (sep) {
+    // separable: one z-chunk for the batch from the wave model over all
+    // instances' x/y tiles (6 resident 4-warp CTAs per SM in FP32, 3 in FP64)
+    static int sms = 0;
+    if (sms == 0) {
+      int dev = 0, n = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+      sms = n > 0 ? n : 152;
+    }
+    const int res = sizeof(real) == 4 ? 6 : 3;
+    int nzmax = 2;
+    for (int b = 0; b < nb; ++b) nzmax = max(nzmax, g[b].nz);
+    int zc_batch = 2;
+    double best = -1;
+    for (int zc = 2; zc <= min(nzmax, SEP_ZMAX); ++zc) {
+      long long ctas = 0;
+      for (int b = 0; b < nb; ++b)
+        ctas += (long long)cdiv(g[b].nx, SEP_TILE) * cdiv(g[b].ny, SEP_BATCH_WARPS * SEP_BATCH_ROWS) *
+                (cdiv(g[b].nz, zc) + 1);
+      const long long waves = (ctas + (long long)sms * res - 1) / ((long long)sms * res);
+      const double cost = (double)waves * (zc + 2);
+      if (best < 0 || cost < best - 1e-9) {
+        best = cost;
+        zc_batch = zc;
+      }
+    }
+    for (int b = 0; b < nb; ++b) {
+      LevelK<real>& a = tabs[b];
+      a = make_levelk<real>(&g[b], &p[b]);
+      a.zchunk = (g[b].zchunk > 0 && g[b].zchunk <= SEP_ZMAX) ? g[b].zchunk : zc_batch;
+      const long long blocks = (long long)cdiv(a.nx, SEP_TILE) *
+                               cdiv(a.ny, SEP_BATCH_WARPS * SEP_BATCH_ROWS) * (cdiv(a.nz, a.zchunk) + 1);
+      if (first[b] + blocks >= (1LL << 31)) return GM_ERR_TOO_LARGE;
+      first[b + 1] = first[b] + (int)blocks;
+    }
+    const size_t off = batch_first_offset<real>(nb);
+    if ((long long)(off + sizeof(int) * (nb + 1)) > desc_bytes) return GM_ERR_TOO_LARGE;
+    *hdr = BatchHeader{nb, g[0].dtype, fl, first[nb], 1, SEP_BATCH_ROWS, SEP_BATCH_WARPS};
+    if (cudaMemcpyAsync(desc, hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync((char*)desc + batch_tab_offset(), tabs.data(), sizeof(LevelK<real>) * nb,
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync((char*)desc + off, first.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+      return GM_ERR_CUDA;
+    return GM_OK;
+  }
   // one z-chunk for the whole batch: the cost model over all instances'
   // tiles together (a lone small window would be split much finer)
   long long tiles = 0;
@@ -1255,7 +1348,7 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
   }
   const size_t off = batch_first_offset<real>(nb);
   if ((long long)(off + sizeof(int) * (nb + 1)) > desc_bytes) return GM_ERR_TOO_LARGE;
-  *hdr = BatchHeader{nb, g[0].dtype, variant_of(fl), first[nb]};
+  *hdr = BatchHeader{nb, g[0].dtype, variant_of(fl), first[nb], 0, 0, 0};
   // pageable sources: each copy returns once the host data has been consumed
   if (cudaMemcpyAsync(desc, hdr, sizeof(BatchHeader), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync((char*)desc + batch_tab_offset(), tabs.data(), sizeof(LevelK<real>) * nb,
@@ -1270,6 +1363,24 @@ template <typename real>
 static int launch_batched(const BatchHeader& h, const void* desc, cudaStream_t st) {
   const LevelK<real>* tab = (const LevelK<real>*)((const char*)desc + batch_tab_offset());
   const int* first = (const int*)((const char*)desc + batch_first_offset<real>(h.nb));
+  if (h.kernel == 1) {
+    if (h.rows != SEP_BATCH_ROWS || h.warps != SEP_BATCH_WARPS) return GM_ERR_ARG;
+    const dim3 sblk(32 * SEP_BATCH_WARPS);
+    switch (h.variant) {
+#define GM_SEPB(V)                                                                                    \
+  case V | LF_CONST:                                                                                  \
+    level_sep_batched_kernel<real, SEP_BATCH_ROWS, V | LF_CONST><<<h.blocks, sblk, 0, st>>>(tab, first, h.nb); \
+    break;
+      GM_SEPB(LF_L3)
+      GM_SEPB(LF_L3ACC)
+      GM_SEPB(LF_L2)
+      GM_SEPB(LF_L1)
+#undef GM_SEPB
+      default:
+        return GM_ERR_ARG;
+    }
+    return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+  }
   const dim3 blk(LT_X, LT_Y);
   switch (h.variant) {
 #define GM_CASE(V)                                                                              \
@@ -1331,12 +1442,15 @@ extern "C" int gm_level_batched_prepare(const gm_level_args* a, int nb, const gm
   info->dtype = h.dtype;
   info->variant = h.variant;
   info->blocks = h.blocks;
+  info->kernel = h.kernel;
+  info->rows = h.rows;
+  info->warps = h.warps;
   return GM_OK;
 }
 
 extern "C" int gm_level_batched_launch(const void* desc, const gm_batch_info* info, void* stream) {
   if (!desc || !info || info->nb < 1 || info->blocks < 1) return GM_ERR_ARG;
-  const gm::BatchHeader h{info->nb, info->dtype, info->variant, info->blocks};
+  const gm::BatchHeader h{info->nb, info->dtype, info->variant, info->blocks, info->kernel, info->rows, info->warps};
   cudaStream_t st = (cudaStream_t)stream;
   if (h.dtype == GM_F32) return gm::launch_batched<float>(h, desc, st);
   if (h.dtype == GM_F64) return gm::launch_batched<double>(h, desc, st);

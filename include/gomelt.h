@@ -229,6 +229,7 @@ int gm_level_step_batched(const gm_level_args* args, int nb, const gm_props* pro
  * desc is unchanged).  info receives what the launch needs. */
 typedef struct gm_batch_info {
   int nb, dtype, variant, blocks;
+  int kernel, rows, warps;  /* 1: separable kernel (constant-property batches), rows x warps a CTA */
 } gm_batch_info;
 
 int gm_level_batched_prepare(const gm_level_args* args, int nb, const gm_props* props, void* desc,

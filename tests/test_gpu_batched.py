@@ -69,6 +69,37 @@ def test_batched_equals_single(dtype, accum):
             assert torch.equal(a["accum"], b["accum"]) and torch.equal(a["max_accum"], b["max_accum"])
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("accum", [False, True])
+def test_batched_separable_equals_single(dtype, accum):
+    """Constant-property windows take the separable kernel in both forms."""
+    import _native as N
+    import kern
+    from test_gpu_separable import CONST_PROPS
+
+    P = O.SetupProperties(CONST_PROPS)
+    ps = N.props_struct(P)
+    single = windows(dtype, accum, seed=3)
+    batch = windows(dtype, accum, seed=3)
+    for w in single:
+        kern.level_step_shape(ps, kernel=1, rows=2, tile_y=4, zchunk=5, **w)
+    args = (N.gm_level_args * len(batch))(*[kern.level_args(**w) for w in batch])
+    props = (N.gm_props * len(batch))(*[ps] * len(batch))
+    nbytes = int(N.lib().gm_level_batched_desc_size(len(batch), kern.dtype_code(batch[0]["T_in"])))
+    desc = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    info = N.gm_batch_info()
+    N.call("gm_level_batched_prepare", C.cast(args, C.c_void_p), len(batch), C.cast(props, C.c_void_p),
+           desc.data_ptr(), nbytes, C.byref(info), kern.stream_ptr())
+    assert info.kernel == 1 and info.rows == 2 and info.warps == 4
+    N.call("gm_level_batched_launch", desc.data_ptr(), C.byref(info), kern.stream_ptr())
+    torch.cuda.synchronize()
+    for a, b in zip(single, batch):
+        assert torch.equal(a["T_out"], b["T_out"])
+        assert torch.equal(a["ph_out"], b["ph_out"])
+        if accum:
+            assert torch.equal(a["accum"], b["accum"]) and torch.equal(a["max_accum"], b["max_accum"])
+
+
 def test_autotune_keeps_results():
     import _native as N
     import kern
