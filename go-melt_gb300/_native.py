@@ -48,7 +48,7 @@ class gm_level_args(C.Structure):
         ("rhs_box", vp), ("box", C.c_int * 6), ("laser", vp), ("surface", C.c_int), ("bc_mode", C.c_int),
         ("face", C.c_double * 5), ("inactive_amb", C.c_int), ("bc_new", vp), ("bc_old", vp),
         ("bc_alpha", C.c_double), ("bc_beta", C.c_double), ("bc_map", gm_map3), ("clamp", C.c_int),
-        ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int), ("pdl", C.c_int),
+        ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int), ("pdl", C.c_int), ("src_tab", vp),
     ]
 
 
@@ -184,16 +184,27 @@ class gm_subcycle_plan(C.Structure):
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("src2", vp), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
         ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int),
-        ("pdl", C.c_int)]
+        ("pdl", C.c_int), ("src3tab", vp)]
 
 
-def subcycle_kernel_count(N2: int, N3: int) -> int:
+def subcycle_kernel_count(N2: int, N3: int, separable: bool = False) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
     steps (source copy, coupling 2, Level-2 solve, Level-3 ring, N3 Level-3
     solves, restriction, T'), the T'2/mass/corrector block (7) and the tail
-    (3)."""
-    return 20 + 2 * (1 + N2 * (7 + N3))
+    (3).  For a constant-property material (separable kernels) each of the
+    4 + 2 N2 coupling calls is one kernel more and the Level-3 laser factors
+    are tabulated once (one kernel)."""
+    n = 20 + 2 * (1 + N2 * (7 + N3))
+    return n + (4 + 2 * N2 + 1 if separable else 0)
+
+
+def props_constant(s) -> bool:
+    """k and rho*cp of a gm_props independent of phase and temperature (the
+    condition under which the library takes its separable level-step and
+    coupling kernels)."""
+    return (s.k_powder == s.k_bulk_a0 and s.k_fluid == s.k_bulk_a0 and s.k_bulk_a1 == 0.0 and
+            s.cp_solid_a1 == 0.0 and s.cp_mushy == s.cp_solid_a0 and s.cp_fluid == s.cp_solid_a0)
 
 
 _lib = None
@@ -252,6 +263,8 @@ SIGNATURES = {
     "gm_level_batched_launch": [vp, C.POINTER(gm_batch_info), vp],
     "gm_level_autotune": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.c_int, C.POINTER(gm_tune_result), vp],
     "gm_level_step_shape": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.POINTER(gm_level_shape), vp],
+    "gm_fine_source_tables": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), vp,
+                              C.c_int, C.POINTER(gm_props), vp, vp],
     "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],
     "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
     "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],

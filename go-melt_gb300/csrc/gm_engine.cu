@@ -45,7 +45,7 @@ inline long long nn(const gm_window& w) { return (long long)w.nodes[0] * w.nodes
 void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tout, const double* dt,
            const uint8_t* phin, uint8_t* phout, const void* rhs, const int lo[3], const int n[3],
            const double* laser, int bc_mode, const gm_map3* map, const void* bnew, const void* bold, double alpha,
-           void* acc, void* macc) {
+           void* acc, void* macc, const void* src_tab = nullptr) {
   const gm_subcycle_plan& p = *c.p;
   gm_level_args a;
   memset(&a, 0, sizeof(a));
@@ -88,7 +88,8 @@ void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tou
   a.accum = acc;
   a.max_accum = macc;
   a.zchunk = p.zchunk;
-  a.pdl = p.pdl;  // dt and the laser row are plan inputs, never written by the subcycle's kernels
+  a.pdl = p.pdl;  // dt, the laser row and its factor table are never written by the kernels before it
+  a.src_tab = src_tab;
   GM_TRY(gm_level_step(&a, c.pr, c.st));
 }
 
@@ -267,8 +268,10 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
       void* Tn = p.T3w[i % 2];
       uint8_t* phn = p.ph3w[i % 2];
       const double* row = p.rows + (long long)i * 7;
+      const long long L3n = (long long)p.L3.nodes[0] + p.L3.nodes[1] + p.L3.nodes[2];
       level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 3, nullptr,
-            p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr);
+            p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr,
+            p.src3tab ? at(p.src3tab, i * L3n, c.esz) : nullptr);
       T3c = Tn;
       ph3c = phn;
     }
@@ -306,8 +309,6 @@ bool plan_ok(const gm_subcycle_plan* p) {
 namespace {
 
 int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
-  // every kernel of the call launches as a programmatic dependent of the one before it
-  const gm::PdlScope pdl(p->pdl != 0);
   Ctx c;
   c.p = p;
   c.pr = props;
@@ -315,6 +316,15 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   c.esz = p->dtype == GM_F32 ? 4 : 8;
   const long long n1 = nn(p->L1), n2 = nn(p->L2), n3 = nn(p->L3);
   const long long nrhs1 = (long long)p->rhs1_n[0] * p->rhs1_n[1] * p->rhs1_n[2];
+
+  // The Level-3 laser factors of the call, tabulated by an ordinarily
+  // launched kernel that triggers no early launch: every kernel after it
+  // starts once it has completed, so their prologues may read the table.
+  if (p->src3tab)
+    GM_TRY(gm_fine_source_tables(p->dtype, p->L3.nodes, p->L3.origin, p->L3.h, p->rows, p->N2 * p->N3, props,
+                                 p->src3tab, stream));
+  // every later kernel of the call launches as a programmatic dependent of the one before it
+  const gm::PdlScope pdl(p->pdl != 0);
 
   // Level-1 S1 from Level 2 at the overlap, substrate forced
   gm_restrict_s1_args s1;

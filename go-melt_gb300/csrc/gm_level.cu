@@ -67,6 +67,7 @@ struct LevelK {
   real rir2, rid2;       // 1/r^2, 1/d^2 of the laser
   real sa1, sb1, sb2;    // k hy hz / (36 hx), k hx hz / (36 hy), k hx hy / (36 hz)
   real smass;            // lumped mass of 8 elements times dt: hx hy hz rho c
+  const real* src_tab;   // optional laser factors of this step: [nx] x (times the power), [ny] y, [nz] z
 };
 
 constexpr int ZMAX = 64;
@@ -597,7 +598,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
   __shared__ real s_in[5];
   if (threadIdx.x == 0) {
     s_in[0] = (real)(*a.dt);
-    if (hLaser) {
+    if (hLaser && !a.src_tab) {
       s_in[1] = (real)(a.ox - a.laser[0]);
       s_in[2] = (real)(a.oy - a.laser[1]);
       s_in[3] = (real)(a.oz - a.laser[2]);
@@ -692,7 +693,14 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
   // laser: x factor times the rows' y factors; lane l keeps the z factor of
   // plane Z0 + l.
   real sxy[BYT], szl = 0;
-  if (hLaser) {
+  if (hLaser && a.src_tab) {  // the step's factors, tabulated before the subcycle (fine_source_tables)
+    const real* tb = a.src_tab;
+    const real sx = xin ? tb[x] : (real)0;
+    const real syl = (lane < BYT && y0 + lane < ny) ? tb[nx + y0 + lane] : (real)0;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) sxy[r] = sx * __shfl_sync(FULL, syl, r);
+    if (Z0 + lane < Z1) szl = tb[nx + ny + Z0 + lane];
+  } else if (hLaser) {
     const real rx = s_in[1], ry = s_in[2], rz = s_in[3], srcP = s_in[4];
     const real sx = xin ? srcP * src_factor<real>(x, nx, rx, a.rh[0], a.rir2) : (real)0;
     // lane r < BYT evaluates the y factor of row y0 + r for the whole warp
@@ -1199,6 +1207,7 @@ static LevelK<real> make_levelk(const gm_level_args* g, const gm_props* pr) {
   a.sb1 = (real)(kc * hx * hz / (36.0 * hy));
   a.sb2 = (real)(kc * hx * hy / (36.0 * hz));
   a.smass = (real)(hx * hy * hz * pr->rho * pr->cp_fluid);
+  a.src_tab = (const real*)g->src_tab;
   return a;
 }
 
@@ -1588,6 +1597,31 @@ __global__ void fine_source_kernel(int nx, int ny, int nz, double ox, double oy,
   }
 }
 
+// Laser factors of many fine steps on one window, as the separable level
+// step uses them (the same expressions, so the step's results do not change):
+// row i of tab = [nx] P c Sx[ix], [ny] Sy[iy], [nz] Sz[iz] for laser row i.
+template <typename real>
+__global__ void fine_source_tables_kernel(int nx, int ny, int nz, double ox, double oy, double oz, real hx, real hy,
+                                          real hz, const double* rows, int nrows, real ir2, real id2, double src_c,
+                                          real* tab) {
+  const int L = nx + ny + nz;
+  const long long n = (long long)nrows * L;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / L), j = (int)(t - (long long)i * L);
+    const double* laser = rows + 7LL * i;
+    real v;
+    if (j < nx) {
+      const real rx = (real)(ox - laser[0]), srcP = (real)(src_c * laser[6]);
+      v = srcP * src_factor<real>(j, nx, rx, hx, ir2);
+    } else if (j < nx + ny) {
+      v = src_factor<real>(j - nx, ny, (real)(oy - laser[1]), hy, ir2);
+    } else {
+      v = src_factor<real>(j - nx - ny, nz, (real)(oz - laser[2]), hz, id2);
+    }
+    tab[t] = v;
+  }
+}
+
 // computeConvRadBC (:2207-2301): flux of the top faces of element plane
 // ne_planes-1 into the nodes of plane ne_planes; one thread per node gathers
 // its (up to four) faces.
@@ -1662,6 +1696,29 @@ extern "C" int gm_fine_source(int dtype, const int nodes[3], const double origin
     gm::fine_source_kernel<double><<<gm::lgrid(n), 256, 0, st>>>(nodes[0], nodes[1], nodes[2], origin[0], origin[1],
                                                                   origin[2], h[0], h[1], h[2], laser, r * r, d * d,
                                                                   src_c, (double*)F);
+  else
+    return GM_ERR_ARG;
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_fine_source_tables(int dtype, const int nodes[3], const double origin[3], const double h[3],
+                                     const double* rows, int nrows, const gm_props* p, void* tab, void* stream) {
+  if (!nodes || !origin || !h || !rows || !p || !tab || nrows < 1 || nodes[0] < 2 || nodes[1] < 2 || nodes[2] < 2)
+    return GM_ERR_ARG;
+  const double r = p->laser_radius, d = p->laser_depth;
+  const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
+  const double src_c = 6.0 * sqrt(3.0) * p->laser_eta * rc * rc * dc * (h[0] * h[1] * h[2] / 8.0);
+  const double ir2 = 1.0 / (r * r), id2 = 1.0 / (d * d);
+  const long long n = (long long)nrows * (nodes[0] + nodes[1] + nodes[2]);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == GM_F32)
+    gm::fine_source_tables_kernel<float><<<gm::lgrid(n), 256, 0, st>>>(
+        nodes[0], nodes[1], nodes[2], origin[0], origin[1], origin[2], (float)h[0], (float)h[1], (float)h[2], rows,
+        nrows, (float)ir2, (float)id2, src_c, (float*)tab);
+  else if (dtype == GM_F64)
+    gm::fine_source_tables_kernel<double><<<gm::lgrid(n), 256, 0, st>>>(
+        nodes[0], nodes[1], nodes[2], origin[0], origin[1], origin[2], h[0], h[1], h[2], rows, nrows, ir2, id2, src_c,
+        (double*)tab);
   else
     return GM_ERR_ARG;
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;

@@ -513,7 +513,7 @@ class Engine:
                         torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev))
         p = self._plan(rows, dtd, out_hist)
         N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
-               kernels=N.subcycle_kernel_count(N2, N3))
+               kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps)))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         return out_hist
 
@@ -584,6 +584,8 @@ class Engine:
         p.ring3[0], p.ring3[1] = self._buf("ring3a", nn3).data_ptr(), self._buf("ring3b", nn3).data_ptr()
         p.graph = 1 if self.use_graph else 0
         p.pdl = 1 if self.use_pdl else 0
+        if N.props_constant(self.ps):  # the separable Level-3 step reads tabulated laser factors
+            p.src3tab = self._buf("src3tab", N2 * N3 * int(sum(L3.nodes))).data_ptr()
         return p
 
     # ------------------------------------------------------------------

@@ -104,6 +104,9 @@ typedef struct gm_level_args {
                                   the preceding kernel in the stream (its CTAs start early and wait
                                   for that kernel before touching any field); dt and laser must not
                                   be written by that kernel.  0: ordinary stream order. */
+  const void* src_tab;         /* optional: this step's laser factors from gm_fine_source_tables (one
+                                  row); the separable kernel reads them instead of evaluating the
+                                  Gaussians (with pdl, not written by the preceding kernels either) */
 } gm_level_args;
 
 int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream);
@@ -129,6 +132,14 @@ int gm_state_properties(const gm_state_props_args* a, const gm_props* p, void* s
  * (computeSourcesL3, :2960-3012).  laser: device row (x,y,z,...,P at [6]). */
 int gm_fine_source(int dtype, const int nodes[3], const double origin[3], const double h[3], const double* laser,
                    const gm_props* p, void* F, void* stream);
+
+/* Laser source factors of `nrows` fine steps on one window, tabulated once:
+ * row i of `tab` (dtype, nrows x (nx + ny + nz)) holds the x factors times
+ * the power factor, then the y and the z factors of laser row i (rows: 7
+ * doubles each), as gm_level_step evaluates them (computeSourcesL3,
+ * :2960-3012, separable form).  No counterpart in the reference. */
+int gm_fine_source_tables(int dtype, const int nodes[3], const double origin[3], const double h[3],
+                          const double* rows, int nrows, const gm_props* p, void* tab, void* stream);
 
 /* Convection + radiation + evaporation flux of the top faces of element plane
  * ne_planes-1, added into F at node plane ne_planes (computeConvRadBC,
@@ -469,6 +480,8 @@ typedef struct gm_subcycle_plan {
                                 issues directly) */
   int pdl;                   /* 1: level steps launch as programmatic dependents of the kernel before
                                 them (their CTAs start while it drains) */
+  void* src3tab;             /* optional work (N2*N3 * (nx+ny+nz) of Level 3): the Level-3 laser factors
+                                of the call, tabulated at its start */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */

@@ -210,3 +210,29 @@ def test_separable_rejects_other_calls():
                               ph_out=torch.empty(n, dtype=torch.uint8, device="cuda"), surface=1, clamp=1,
                               bc_mode=3, bc_new=T, bc_old=T, bc_alpha=1.0,
                               laser=dev([0.5, 0.5, 0, 1, 1, 1e-5, 100.0], torch.float64))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_tabulated_laser_factors_bit_identical(dtype):
+    """The Level-3 step with the laser factors from gm_fine_source_tables
+    equals the step that evaluates them itself, bit for bit."""
+    import ctypes as C
+
+    import _native as N
+    import kern
+
+    ps, nn, kw, _, _, _ = level3_case(CFG, 5, dtype, False)
+    rows = torch.tensor([[1.01, 0.99, 0.0, 1, 1, 1.5e-6, 250.0], [1.013, 0.997, 0.0, 1, 1, 1.5e-6, 250.0]],
+                        dtype=torch.float64, device="cuda")
+    nodes = (C.c_int * 3)(*kw["nodes"])
+    origin = (C.c_double * 3)(*kw["origin"])
+    h = (C.c_double * 3)(*kw["h"])
+    L = sum(kw["nodes"])
+    tab = torch.empty(2 * L, dtype=dtype, device="cuda")
+    N.call("gm_fine_source_tables", kern.dtype_code(tab), nodes, origin, h, rows.data_ptr(), 2, C.byref(ps),
+           tab.data_ptr(), kern.stream_ptr())
+    kw["laser"] = rows[1]
+    a = run(ps, (1, 2, 4, 5), nn, dtype, ph_out=torch.empty(nn, dtype=torch.uint8, device="cuda"), **kw)
+    kw["src_tab"] = tab[L:]
+    b = run(ps, (1, 2, 4, 5), nn, dtype, ph_out=torch.empty(nn, dtype=torch.uint8, device="cuda"), **kw)
+    np.testing.assert_array_equal(a, b)
