@@ -319,19 +319,24 @@ __global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, i
 
 // Per-position 1-D source factors on the coarse node box:
 // S[p][t] = sum_{fine e, side s assigned to coarse node t} phi_A(e,s) exp(-3 (x_q - v_p)^2 / r^2)
+// One warp per table entry (row p, axis entry r): the lanes take the terms
+// (coarse element r-1 or r, fine element, Gauss side) of the entry and the
+// warp adds them in a fixed order.  The x entries carry the row's power
+// factor cpre * P, so the assembly multiplies three table values.
 template <typename real>
 __global__ void coarse_source_tables(int np, const double* rows, int n0, int n1, int n2, const double* xq0,
                                      const double* xq1, const double* xq2, const real* cw0, const real* cw1,
                                      const real* cw2, const int* flo0, const int* flo1, const int* flo2,
                                      const int* fhi0, const int* fhi1, const int* fhi2, double rsq, double dsq,
-                                     real* S) {
+                                     double cpre, real* S) {
   pdl_begin();
   const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
+  const int lane = threadIdx.x & 31;
   const long long tot = (long long)np * per;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-       t += (long long)gridDim.x * blockDim.x) {
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long t = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); t < tot; t += nw) {
     const int p = (int)(t / per);
-    int r = (int)(t % per);
+    int r = (int)(t - (long long)p * per);
     int d, ncb;
     const double* xq;
     const real* cw;
@@ -345,43 +350,55 @@ __global__ void coarse_source_tables(int np, const double* rows, int n0, int n1,
       r -= n0 + 1 + n1 + 1; d = 2; ncb = n2; xq = xq2; cw = cw2; flo = flo2; fhi = fhi2; s2 = dsq;
     }
     const double v = rows[p * 7 + d];
-    const double inv2 = 1.0 / s2;
+    const real inv2 = (real)(1.0 / s2);
+    // terms of coarse element r-1 (A = 1) then r (A = 0), two Gauss sides each
+    const int na = (r >= 1 && r - 1 < ncb) ? 2 * (fhi[r - 1] - flo[r - 1]) : 0;
+    const int nb = (r < ncb) ? 2 * (fhi[r] - flo[r]) : 0;
     real acc = 0;
-    for (int c = r - 1; c <= r; ++c) {
-      if (c < 0 || c >= ncb) continue;
-      const int A = r - c;
-      for (int e = flo[c]; e < fhi[c]; ++e)
-        for (int s = 0; s < 2; ++s) {
-          const double dx = xq[e * 2 + s] - v;  // offset in double, exponential in the kernel's precision
-          acc += cw[(e * 2 + s) * 2 + A] * exp((real)(-3.0 * dx * dx * inv2));
-        }
+    for (int k = lane; k < na + nb; k += 32) {
+      const int A = k < na ? 1 : 0;
+      const int kk = k < na ? k : k - na;
+      const int e = (A ? flo[r - 1] : flo[r]) + (kk >> 1), sd = kk & 1;
+      const real dx = (real)(xq[e * 2 + sd] - v);  // offset in double, the rest in the kernel's precision
+      acc += cw[(e * 2 + sd) * 2 + A] * exp((real)-3 * dx * dx * inv2);
     }
-    S[t] = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) S[t] = d == 0 ? (real)(cpre * rows[p * 7 + 6]) * acc : acc;
   }
 }
 
-// Group g of ng (np rows each) is averaged into out + g * gstride.
-template <typename real>
-__global__ void coarse_source_assemble(int np, int ng, long long gstride, const double* rows, int n0, int n1, int n2,
-                                       int lo0, int lo1, int lo2, const real* S, double cpre, real* out, int ob0,
-                                       int ob1, int ob2, int on0, int on1) {
+// Coarse node (bx, by, bz) of group g: mean over the group's np rows of
+// Sx[bx] Sy[by] Sz[bz].  AG lanes per output split the rows and add their
+// partial sums by a fixed shuffle tree (deterministic).
+template <typename real, int AG>
+__global__ void coarse_source_assemble(int np, int ng, long long gstride, int n0, int n1, int n2, int lo0, int lo1,
+                                       int lo2, const real* S, real* out, int ob0, int ob1, int ob2, int on0,
+                                       int on1) {
   pdl_begin();
   const int per = (n0 + 1) + (n1 + 1) + (n2 + 1);
-  const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nodes * ng;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(t / nodes);
-    const long long u = t - g * nodes;
-    const int bx = (int)(u % (n0 + 1)), by = (int)((u / (n0 + 1)) % (n1 + 1)),
-              bz = (int)(u / ((long long)(n0 + 1) * (n1 + 1)));
+  const int nodes = (n0 + 1) * (n1 + 1) * (n2 + 1);
+  const int sub = threadIdx.x % AG;
+  const long long total = (long long)nodes * ng;
+  const long long tot_up = (total + 31) / 32 * 32;
+  const long long stride = (long long)gridDim.x * (blockDim.x / AG);
+  for (long long t = blockIdx.x * (long long)(blockDim.x / AG) + threadIdx.x / AG; t < tot_up; t += stride) {
+    const bool live = t < total;
+    const int g = live ? (int)(t / nodes) : 0;
+    const int u = live ? (int)(t - (long long)g * nodes) : 0;
+    const int bx = u % (n0 + 1), by = (u / (n0 + 1)) % (n1 + 1), bz = u / ((n0 + 1) * (n1 + 1));
     real s = 0;
-    for (int p = g * np; p < (g + 1) * np; ++p) {
-      const real c = (real)(cpre * rows[p * 7 + 6]);
-      const real* Sp = S + (long long)p * per;
-      s += c * Sp[bx] * Sp[n0 + 1 + by] * Sp[n0 + 1 + n1 + 1 + bz];
+    if (live)
+      for (int p = g * np + sub; p < (g + 1) * np; p += AG) {
+        const real* Sp = S + (long long)p * per;
+        s += Sp[bx] * Sp[n0 + 1 + by] * Sp[n0 + 1 + n1 + 1 + bz];
+      }
+#pragma unroll
+    for (int o = AG / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (live && sub == 0) {
+      const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
+      out[g * gstride + gx + (long long)gy * on0 + (long long)gz * on0 * on1] += s / (real)np;
     }
-    const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
-    out[g * gstride + gx + (long long)gy * on0 + (long long)gz * on0 * on1] += s / (real)np;
   }
 }
 
@@ -806,19 +823,24 @@ static int do_source(const gm_coarse_source_args* g, const gm_props* pr, cudaStr
   const int n0 = G.ax[0].ncb, n1 = G.ax[1].ncb, n2 = G.ax[2].ncb;
   const long long tabs = (long long)g->npos * ((n0 + 1) + (n1 + 1) + (n2 + 1));
   const double r = pr->laser_radius, d = pr->laser_depth;
-  launch_k(coarse_source_tables<real>, dim3(grid1(tabs)), dim3(128), 0, st,
-      g->npos, g->rows, n0, n1, n2, g->xq[0], g->xq[1], g->xq[2], (const real*)G.ax[0].cw,
-      (const real*)G.ax[1].cw, (const real*)G.ax[2].cw, G.ax[0].flo, G.ax[1].flo, G.ax[2].flo, G.ax[0].fhi,
-      G.ax[1].fhi, G.ax[2].fhi, r * r, d * d, (real*)g->scratch);
-  if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
   const double rc = 1.0 / (r * sqrt(M_PI)), dc = 1.0 / (d * sqrt(M_PI));
   const double cpre = 6.0 * sqrt(3.0) * pr->laser_eta * rc * rc * dc * g->fine_wq;
+  launch_k(coarse_source_tables<real>, dim3(grid1(tabs * 32)), dim3(256), 0, st,
+      g->npos, g->rows, n0, n1, n2, g->xq[0], g->xq[1], g->xq[2], (const real*)G.ax[0].cw,
+      (const real*)G.ax[1].cw, (const real*)G.ax[2].cw, G.ax[0].flo, G.ax[1].flo, G.ax[2].flo, G.ax[0].fhi,
+      G.ax[1].fhi, G.ax[2].fhi, r * r, d * d, cpre, (real*)g->scratch);
+  if (cudaGetLastError() != cudaSuccess) return GM_ERR_LAUNCH;
   const long long nodes = (long long)(n0 + 1) * (n1 + 1) * (n2 + 1);
   const int ng = g->ngroups > 1 ? g->ngroups : 1;
-  launch_k(coarse_source_assemble<real>, dim3(grid1(nodes * ng)), dim3(256), 0, st,
-      g->npos / ng, ng, g->out_group_stride, g->rows, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo,
-      (const real*)g->scratch, cpre, (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0],
-      g->out_n[1]);
+  const int np = g->npos / ng;
+  if (np >= 16)
+    launch_k(coarse_source_assemble<real, 32>, dim3(grid1(nodes * ng * 32)), dim3(256), 0, st, np, ng,
+             g->out_group_stride, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo, (const real*)g->scratch,
+             (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1]);
+  else
+    launch_k(coarse_source_assemble<real, 4>, dim3(grid1(nodes * ng * 4)), dim3(256), 0, st, np, ng,
+             g->out_group_stride, n0, n1, n2, G.ax[0].cb_lo, G.ax[1].cb_lo, G.ax[2].cb_lo, (const real*)g->scratch,
+             (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1]);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
