@@ -151,7 +151,7 @@ class gm_couple_args(C.Structure):
                 ("fine_h", C.c_double * 3), ("T", vp), ("ph", C.POINTER(C.c_uint8)), ("substrate", C.c_longlong),
                 ("k_arr", vp), ("rc_arr", vp), ("Tp", vp), ("dTa", vp), ("dTb", vp), ("dt", vp), ("out", vp),
                 ("out_lo", C.c_int * 3), ("out_n", C.c_int * 3), ("scale", C.c_double), ("partials", vp),
-                ("partials_cap", C.c_longlong), ("method", C.c_int)]
+                ("partials_cap", C.c_longlong), ("method", C.c_int), ("base", vp)]
 
 
 class gm_coarse_source_args(C.Structure):
@@ -190,12 +190,12 @@ class gm_subcycle_plan(C.Structure):
 def subcycle_kernel_count(N2: int, N3: int, separable: bool = False) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
-    steps (source copy, coupling 2, Level-2 solve, Level-3 ring, N3 Level-3
-    solves, restriction, T'), the T'2/mass/corrector block (7) and the tail
+    steps (coupling 2 onto the step's source, Level-2 solve, Level-3 ring, N3
+    Level-3 solves, restriction, T'), the T'2/mass/corrector block (7) and the tail
     (3).  For a constant-property material (separable kernels) each of the
     4 + 2 N2 coupling calls is one kernel more and the Level-3 laser factors
     are tabulated once (one kernel)."""
-    n = 20 + 2 * (1 + N2 * (7 + N3))
+    n = 20 + 2 * (1 + N2 * (6 + N3))
     return n + (4 + 2 * N2 + 1 if separable else 0)
 
 

@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(128) couple_kernel(const CoupleK<real> a) {
 template <typename real>
 __global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, int lo0, int lo1, int lo2,
                                      const real* partials, real* out, int ob0, int ob1, int ob2, int on0, int on1,
-                                     real scale) {
+                                     real scale, const real* base) {
   pdl_begin();
   const long long tot = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
   const bool per_warp = nchunk > 1;
@@ -312,7 +312,8 @@ __global__ void couple_gather_kernel(int ncbx, int ncby, int ncbz, int nchunk, i
     if (per_warp) s = warp_sum(s);
     if (!per_warp || lane == 0) {
       const int gx = lo0 + bx - ob0, gy = lo1 + by - ob1, gz = lo2 + bz - ob2;
-      out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * s;
+      const long long o = gx + (long long)gy * on0 + (long long)gz * on0 * on1;
+      out[o] = (base ? base[o] : out[o]) + scale * s;
     }
   }
 }
@@ -613,7 +614,8 @@ __global__ void couple_sep_y(int ncx, SepAxis<real> ay, SepAxis<real> az, int NB
 template <typename real>
 __global__ void couple_sep_z(int ncx, int ncy, SepAxis<real> az, int lo0, int lo1, int lo2, const real* W,
                              long long ws, bool flux, bool mass, real kcf0, real kcf1, real kcf2, const double* dt,
-                             real mwq, real* out, int ob0, int ob1, int ob2, int on0, int on1, real scale) {
+                             real mwq, real* out, int ob0, int ob1, int ob2, int on0, int on1, real scale,
+                             const real* base) {
   pdl_begin();
   const int ncz = az.ncb;
   const long long n = (long long)(ncx + 1) * (ncy + 1) * (ncz + 1);
@@ -644,7 +646,8 @@ __global__ void couple_sep_z(int ncx, int ncy, SepAxis<real> az, int lo0, int lo
     v = csub_sum(v);
     if (live && sub == 0) {
       const int gx = lo0 + Nx - ob0, gy = lo1 + Ny - ob1, gz = lo2 + Nz - ob2;
-      out[gx + (long long)gy * on0 + (long long)gz * on0 * on1] += scale * v;
+      const long long o = gx + (long long)gy * on0 + (long long)gz * on0 * on1;
+      out[o] = (base ? base[o] : out[o]) + scale * v;
     }
   }
 }
@@ -743,7 +746,7 @@ static int do_couple_sep(const gm_couple_args* g, const gm_props* pr, cudaStream
                g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, (const real*)W, ws, flux, mass,
                (real)kcf[0], (real)kcf[1], (real)kcf[2], g->dt, (real)(wq * pr->rho * pr->cp_fluid),
                (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1],
-               (real)g->scale) != cudaSuccess)
+               (real)g->scale, (const real*)g->base) != cudaSuccess)
     return GM_ERR_LAUNCH;
   return GM_OK;
 }
@@ -779,7 +782,8 @@ static int do_couple(const gm_couple_args* g, const gm_props* pr, cudaStream_t s
   const long long nodes = (long long)(ncbx + 1) * (ncby + 1) * (ncbz + 1);
   launch_k(couple_gather_kernel<real>, dim3(grid1(a.nchunk > 1 ? nodes * 32 : nodes)), dim3(256), 0, st,
       ncbx, ncby, ncbz, a.nchunk, g->geom.ax[0].cb_lo, g->geom.ax[1].cb_lo, g->geom.ax[2].cb_lo, a.partials,
-      (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1], (real)g->scale);
+      (real*)g->out, g->out_lo[0], g->out_lo[1], g->out_lo[2], g->out_n[0], g->out_n[1], (real)g->scale,
+      (const real*)g->base);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
@@ -796,6 +800,11 @@ extern "C" int gm_couple(const gm_couple_args* g, const gm_props* p, void* strea
   if ((g->dTa == nullptr) != (g->dTb == nullptr) || (g->dTa && !g->dt)) return GM_ERR_ARG;
   if ((g->k_arr == nullptr) != (g->rc_arr == nullptr)) return GM_ERR_ARG;
   if (!box_inside(&g->geom, g->out_lo, g->out_n)) return GM_ERR_ARG;
+  if (g->base) {  // out = base + terms: every node of the output box must be a coupling node
+    for (int d = 0; d < 3; ++d)
+      if (g->out_lo[d] != g->geom.ax[d].cb_lo || g->out_n[d] != g->geom.ax[d].ncb + 1) return GM_ERR_ARG;
+    if (g->base == g->out) return GM_ERR_ARG;
+  }
   if ((long long)g->fine_nodes[0] * g->fine_nodes[1] * g->fine_nodes[2] >= (1LL << 31)) return GM_ERR_TOO_LARGE;
   if (g->method < 0 || g->method > 2) return GM_ERR_ARG;
   const bool kconst = !g->k_arr && p->k_powder == p->k_bulk_a0 && p->k_fluid == p->k_bulk_a0 &&

@@ -94,7 +94,7 @@ void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tou
 }
 
 void couple(Ctx& c, const gm_couple_geom& g, const gm_window& fine, void* out, const int lo[3], const int n[3],
-            const void* Tp, const void* dTa, const void* dTb, const double* dt) {
+            const void* Tp, const void* dTa, const void* dTb, const double* dt, const void* base = nullptr) {
   const gm_subcycle_plan& p = *c.p;
   gm_couple_args a;
   memset(&a, 0, sizeof(a));
@@ -117,6 +117,7 @@ void couple(Ctx& c, const gm_couple_geom& g, const gm_window& fine, void* out, c
   a.scale = 1.0;
   a.partials = p.partials;
   a.partials_cap = p.partials_cap;
+  a.base = base;
   GM_TRY(gm_couple(&a, c.pr, c.st));
 }
 
@@ -124,11 +125,11 @@ void couple(Ctx& c, const gm_couple_geom& g, const gm_window& fine, void* out, c
 // carried fields instead, so this variant takes them explicitly.
 void couple_fields(Ctx& c, const gm_couple_geom& g, const gm_window& fine, const void* T, const uint8_t* ph,
                    void* out, const int lo[3], const int n[3], const void* Tp, const void* dTa, const void* dTb,
-                   const double* dt) {
+                   const double* dt, const void* base = nullptr) {
   gm_window w = fine;
   w.T = (void*)T;
   w.ph = (uint8_t*)ph;
-  couple(c, g, w, out, lo, n, Tp, dTa, dTb, dt);
+  couple(c, g, w, out, lo, n, Tp, dTa, dTb, dt, base);
 }
 
 void source(Ctx& c, const gm_couple_geom& g, const double* const xq[3], const double* rows, int npos, void* out,
@@ -190,25 +191,6 @@ void memzero(Ctx& c, void* ptr, long long elems) {
   if (cudaMemsetAsync(ptr, 0, elems * c.esz, (cudaStream_t)c.st) != cudaSuccess) c.rc = GM_ERR_CUDA;
 }
 
-// Word copy as a kernel, so that it joins the chain of programmatic dependent
-// launches (a memcpy node would break it).
-__global__ void copy_words_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, long long n) {
-  gm::pdl_begin();
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    dst[i] = src[i];
-}
-
-void copy_k(Ctx& c, void* dst, const void* src, long long bytes) {
-  if (c.rc != GM_OK || dst == src) return;
-  const long long n = bytes / 4;  // element sizes are 4 or 8 bytes
-  long long blocks = (n + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  if (blocks < 1) blocks = 1;
-  if (gm::launch_k(copy_words_kernel, dim3((unsigned)blocks), dim3(256), 0, (cudaStream_t)c.st, (const uint32_t*)src,
-                   (uint32_t*)dst, n) != cudaSuccess)
-    c.rc = GM_ERR_LAUNCH;
-}
-
 void copy(Ctx& c, void* dst, const void* src, long long bytes) {
   if (c.rc != GM_OK || dst == src) return;
   if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)c.st) != cudaSuccess)
@@ -253,11 +235,12 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
   for (int l2 = 0; l2 < N2; ++l2) {
     void* hist_l2 = at(p.tp3hist, l2 * n3, c.esz);
     const double* dt2 = p.dts + 1 + l2;
-    copy_k(c, p.rhs2, at(p.src2, l2 * nrhs2, c.esz), nrhs2 * c.esz);  // the step's source (computed once)
+    // rhs2 = the step's source (computed once for the call) + the coupling terms
+    const void* src = at(p.src2, l2 * nrhs2, c.esz);
     if (part2)
-      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, hist_l2, Tp3c, dt2);
+      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, hist_l2, Tp3c, dt2, src);
     else
-      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, nullptr, nullptr, nullptr);
+      couple_fields(c, p.c32, p.L3, T3c, ph3c, p.rhs2, p.rhs2_lo, p.rhs2_n, Tp3c, nullptr, nullptr, nullptr, src);
     void* T2n = p.T2w[l2 % 2];
     uint8_t* ph2n = p.ph2w[l2 % 2];
     level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 3, nullptr,

@@ -367,6 +367,8 @@ typedef struct gm_couple_args {
   long long partials_cap;
   int method;  /* 0: separable contraction when k and rho*c are constant and the scratch holds it, else
                   the element reduction; 1: element reduction; 2: separable (constant properties only) */
+  const void* base;  /* optional: out = base + scale * terms instead of out += (the output box must be
+                        the coupling box: out_lo = cb_lo, out_n = ncb + 1; base must not alias out) */
 } gm_couple_args;
 
 int gm_couple(const gm_couple_args* a, const gm_props* p, void* stream);

@@ -15,7 +15,7 @@ from test_gpu_separable import CFG, CONST_PROPS
 pytestmark = pytest.mark.gpu
 
 
-def coupling(method, dtype, fine, coarse, P, fields, scale=1.0):
+def coupling(method, dtype, fine, coarse, P, fields, scale=1.0, base=None):
     import _native as N
     import engine
     import kern
@@ -27,8 +27,8 @@ def coupling(method, dtype, fine, coarse, P, fields, scale=1.0):
     arena.upload(torch.cuda.current_stream())
     nodes = [int(n) for n in fine["nodes"]]
     h = [float(np.asarray(c)[1] - np.asarray(c)[0]) for c in fine["node_coords"]]
-    out_n = [n + 2 for n in cg.box_n]
-    out_lo = [lo - 1 for lo in cg.box_lo]
+    out_n = [n + 2 for n in cg.box_n] if base is None else list(cg.box_n)
+    out_lo = [lo - 1 for lo in cg.box_lo] if base is None else list(cg.box_lo)
     out = torch.zeros(int(np.prod(out_n)), dtype=dtype, device="cuda")
     part = torch.empty(cg.partials, dtype=dtype, device="cuda")
     a = N.gm_couple_args()
@@ -56,6 +56,10 @@ def coupling(method, dtype, fine, coarse, P, fields, scale=1.0):
     a.partials = part.data_ptr()
     a.partials_cap = part.numel()
     a.method = method
+    if base is not None:
+        base_t = torch.as_tensor(base(out.numel()), dtype=dtype, device="cuda")
+        keep.append(base_t)
+        a.base = kern.ptr(base_t)
     ps = N.props_struct(P)
     N.call("gm_couple", C.byref(a), C.byref(ps), kern.stream_ptr(None))
     torch.cuda.synchronize()
@@ -96,3 +100,24 @@ def test_separable_refuses_variable_properties():
     f = {"T": torch.full((n,), 400.0, device="cuda"), "Tp": torch.zeros(n, device="cuda")}
     with pytest.raises(N.GomeltError):
         coupling(2, torch.float64, L[3], L[2], P, f)
+
+
+@pytest.mark.parametrize("method", [1, 2])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_output_onto_base(method, dtype):
+    """out = base + scale * terms equals base added to the terms alone (to a
+    few ulps: base + scale * s may be one fused multiply-add)."""
+    P = O.SetupProperties(CONST_PROPS)
+    L = O.SetupLevels(CFG, P)
+    n = int(L[3]["nn"])
+    rng = np.random.default_rng(9)
+    f = {"T": torch.tensor(300 + 1500 * rng.random(n), device="cuda"),
+         "Tp": torch.tensor(50 * rng.standard_normal(n), device="cuda"),
+         "dTa": torch.tensor(20 * rng.standard_normal(n), device="cuda"),
+         "dTb": torch.tensor(20 * rng.standard_normal(n), device="cuda")}
+    b = lambda m: np.random.default_rng(4).standard_normal(m)  # noqa: E731
+    terms = coupling(method, dtype, L[3], L[2], P, f, scale=0.7, base=lambda m: np.zeros(m))
+    got = coupling(method, dtype, L[3], L[2], P, f, scale=0.7, base=b)
+    ref = torch.as_tensor(b(got.size), dtype=dtype).double().numpy() + terms
+    rtol, atol = (1e-6, 1e-7) if dtype == torch.float32 else (1e-14, 1e-15)
+    np.testing.assert_allclose(got, ref, rtol=rtol, atol=atol)
