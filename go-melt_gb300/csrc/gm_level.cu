@@ -1517,23 +1517,56 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
       for (int warps : {2, 4, 8})
         for (int zc : zcs)
           if (zc <= gm::SEP_ZMAX) cand.push_back(gm::TuneVal{1, gm::SEP_TILE, warps, rows, zc});
+  // Each candidate is timed as a CUDA graph of 4*reps back-to-back launches,
+  // programmatic dependents of one another (as gm_subcycle issues level
+  // steps), so that neither host launch overhead nor the launch gaps of
+  // stream order enter the comparison; on a stream that cannot be captured
+  // (the legacy default stream) the launches are timed as issued.
+  gm_level_args b = *a;
+  b.pdl = 1;  // the timed launches read the same dt, laser and factors throughout
+  auto launch = [&](const gm::TuneVal& v) {
+    return b.dtype == GM_F32 ? gm::launch_level<float>(&b, p, st, v) : gm::launch_level<double>(&b, p, st, v);
+  };
+  const int R = 4 * reps;
   gm::TuneVal best{0, gm::LT_X, 0, 0, 0};
   float best_us = -1.f;
   int status = GM_OK;
   for (const gm::TuneVal& v : cand) {
-    for (int r = -1; r < reps && status == GM_OK; ++r) {  // one untimed launch first
-      if (r == 0) cudaEventRecord(e0, st);
-      status = a->dtype == GM_F32 ? gm::launch_level<float>(a, p, st, v) : gm::launch_level<double>(a, p, st, v);
-    }
+    status = launch(v);  // untimed first launch
     if (status != GM_OK) break;
-    cudaEventRecord(e1, st);
-    if (cudaEventSynchronize(e1) != cudaSuccess) {
+    cudaGraphExec_t exec = nullptr;
+    if (st && cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (int r = 0; r < R && status == GM_OK; ++r) status = launch(v);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+      if (status == GM_OK && ec == cudaSuccess && graph &&
+          cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess && cudaGraphLaunch(exec, st) == cudaSuccess) {
+        cudaEventRecord(e0, st);
+        cudaGraphLaunch(exec, st);
+        cudaEventRecord(e1, st);
+      } else {
+        status = status != GM_OK ? status : GM_ERR_CUDA;
+      }
+      if (graph) cudaGraphDestroy(graph);
+    } else {
+      cudaGetLastError();  // not capturable: time the launches as issued
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < R && status == GM_OK; ++r) status = launch(v);
+      cudaEventRecord(e1, st);
+    }
+    if (status != GM_OK) {
+      if (exec) cudaGraphExecDestroy(exec);
+      break;
+    }
+    const bool synced = cudaEventSynchronize(e1) == cudaSuccess;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (!synced) {
       status = GM_ERR_CUDA;
       break;
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const float us = 1000.f * ms / reps;
+    const float us = 1000.f * ms / R;
     if (best_us < 0 || us < best_us) {
       best_us = us;
       best = v;

@@ -266,7 +266,9 @@ int gm_level_step_shape(const gm_level_args* a, const gm_props* p, const gm_leve
 /* Autotuner: times gm_level_step for this call over the element tiles
  * (32 x 8, 16 x 16) and, where it applies, the separable kernel (1, 2 or 4
  * rows a thread, 2, 4 or 8 warps a CTA), each over the z-chunks (every distinct
- * split of the node planes), with CUDA events, `reps` launches each after
+ * split of the node planes), with CUDA events over a CUDA graph of 4*reps
+ * back-to-back launches (programmatic dependents of one another, as
+ * gm_subcycle issues them; issued directly on the legacy default stream) after
  * one untimed launch, and keeps the fastest for later calls with the same
  * dtype, features and grid that leave zchunk at 0.  The timed launches write
  * T_out / ph_out / melt time as the call would (so pass scratch outputs, or
