@@ -465,7 +465,7 @@ def run_ours(args):
                      "alg_bytes": alg_bytes, "peak_kind": peak_kind},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
-        "autotuned": {f"L{lev}": shape_json(v) for lev, v in tuned.items()},
+        "autotuned": {f"L{lev}": shape_json(v) for lev, v in tuned.items()},  # L3acc: the corrector's step
     }
     if args.fp64_steps > 0:
         del eng

@@ -1006,9 +1006,8 @@ static int level_flags(const gm_level_args* g, const gm_props* p) {
   return f;
 }
 
-// Launch shapes measured by gm_level_autotune, per (dtype, feature flags
-// without melt time, grid); gm_level_step uses them when the caller leaves
-// zchunk at 0.
+// Launch shapes measured by gm_level_autotune, per (dtype, feature flags,
+// grid); gm_level_step uses them when the caller leaves zchunk at 0.
 struct TuneKey {
   int dtype, flags, nx, ny, nz;
   bool operator<(const TuneKey& o) const {
@@ -1240,7 +1239,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
   const bool sep_ok = sep_eligible(g, fl);
   if (sh.kernel < 0) {
     TuneVal v;
-    if (g->zchunk <= 0 && tuned_shape(TuneKey{g->dtype, fl & ~LF_ACCUM, g->nx, g->ny, g->nz}, &v)) {
+    if (g->zchunk <= 0 && tuned_shape(TuneKey{g->dtype, fl, g->nx, g->ny, g->nz}, &v)) {
       sh = v;
     } else if (sep_ok) {
       sh = sep_default<real>(g);
@@ -1577,7 +1576,7 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
   if (status != GM_OK) return status;
   {
     std::lock_guard<std::mutex> lock(gm::g_tuned_mutex);
-    gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a, p) & ~gm::LF_ACCUM, a->nx, a->ny, a->nz}] = best;
+    gm::g_tuned[gm::TuneKey{a->dtype, gm::level_flags(a, p), a->nx, a->ny, a->nz}] = best;
   }
   if (out) {
     out->kernel = best.kernel;

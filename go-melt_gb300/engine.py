@@ -303,7 +303,8 @@ class Engine:
         Level-2 and Level-1 steps as the subcycle issues them
         (gm_level_autotune); later level steps of the same shapes use the
         fastest.  Needs the tables of a move; writes only scratch outputs;
-        synchronises the stream.  Returns {level: kern.TunedShape}."""
+        synchronises the stream.  Returns {level: kern.TunedShape}, the
+        Level-3 step with the melt-time update under "3acc"."""
         g = self.geo
         t = self.tables
         if t is None:
@@ -326,6 +327,14 @@ class Engine:
                 kw = self.level_kwargs(lev, self.T[lev], To, rowd[5:6], self.ph[lev], Po if lev == 2 else None,
                                        rhs=rhs, box=box, **extra)
             out[lev] = kern.level_autotune(self.ps, reps=reps, stream=self.stream, **kw)
+            if lev == 3:  # the corrector's step with the melt-time update, on scratch accumulators
+                acc = self._buf("tuneAcc", L.nn)
+                macc = self._buf("tuneMacc", L.nn)
+                with torch.cuda.stream(self.stream):
+                    acc.zero_()
+                    macc.zero_()
+                kw.update(accum=acc, max_accum=macc)
+                out["3acc"] = kern.level_autotune(self.ps, reps=reps, stream=self.stream, **kw)
         return out
 
     def _l0_gather(self, idx, n, ph_out, prev_ph, prev_lo, prev_n):

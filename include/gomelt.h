@@ -270,7 +270,7 @@ int gm_level_step_shape(const gm_level_args* a, const gm_props* p, const gm_leve
  * back-to-back launches (programmatic dependents of one another, as
  * gm_subcycle issues them; issued directly on the legacy default stream) after
  * one untimed launch, and keeps the fastest for later calls with the same
- * dtype, features and grid that leave zchunk at 0.  The timed launches write
+ * dtype, features (melt time included) and grid that leave zchunk at 0.  The timed launches write
  * T_out / ph_out / melt time as the call would (so pass scratch outputs, or
  * tune a call whose repetition is harmless); synchronises the stream; not for
  * use during stream capture.  Result: the shape (fields as gm_level_shape;
