@@ -236,3 +236,24 @@ def test_tabulated_laser_factors_bit_identical(dtype):
     kw["src_tab"] = tab[L:]
     b = run(ps, (1, 2, 4, 5), nn, dtype, ph_out=torch.empty(nn, dtype=torch.uint8, device="cuda"), **kw)
     np.testing.assert_array_equal(a, b)
+
+
+# tiny Level-3 windows: 2 node planes, 2 node rows (all on the Dirichlet ring), 4 node columns
+SMALL = [
+    {"elements": [3, 2, 1], "bounds": {"x": [0.99, 1.005], "y": [0.99, 1.0], "z": [-0.005, 0]}},
+    {"elements": [40, 1, 3], "bounds": {"x": [0.95, 1.15], "y": [0.99, 0.995], "z": [-0.015, 0]}},
+    {"elements": [5, 7, 2], "bounds": {"x": [0.99, 1.015], "y": [0.98, 1.015], "z": [-0.01, 0]}},
+]
+
+
+@pytest.mark.parametrize("l3", range(len(SMALL)))
+@pytest.mark.parametrize("shape", [(None, 0, 0, 0), (1, 2, 2, 2), (1, 4, 1, 5), (1, 1, 8, 3)])
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
+def test_level3_small_grids(l3, shape, dtype, tol):
+    ps, nn, kw, ref, (S1n, S2n), _ = level3_case(dict(CFG, Level3=SMALL[l3]), 6 + l3, dtype, False)
+    ph_out = torch.empty(nn, dtype=torch.uint8, device="cuda")
+    out = run(ps, shape, nn, dtype, ph_out=ph_out, **kw)
+    assert relerr(out, ref) < tol
+    ph = ph_out.cpu().numpy()
+    np.testing.assert_array_equal(ph & 1, S1n.astype(np.uint8))
+    np.testing.assert_array_equal((ph >> 1) & 1, S2n.astype(np.uint8))
