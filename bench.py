@@ -85,6 +85,22 @@ def dist_env():
     return ws, rank, local
 
 
+def combine_ranks(t_ms, e2e_ms, mm, mm_e2e, device):
+    """Whole-job figures of the replicas (one independent instance per rank):
+    the slowest rank's timed-region lengths and the scan lengths summed over
+    ranks.  The identity on a single process."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return t_ms, e2e_ms, mm, mm_e2e
+    t = torch.tensor([t_ms, e2e_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    m = torch.tensor([mm, mm_e2e], dtype=torch.float64, device=device)
+    dist.all_reduce(m, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), float(m[0]), float(m[1])
+
+
 def workload(config=1):
     import createPath
     import levels
@@ -432,13 +448,7 @@ def run_ours(args):
             k_ms = t if k_ms is None else min(k_ms, t)
         del graph
 
-    if ws > 1:
-        t = torch.tensor([t_ms, e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms, e2e_ms = float(t[0]), float(t[1])
-        m = torch.tensor([mm, mm_e2e], device=dev)
-        dist.all_reduce(m, op=dist.ReduceOp.SUM)
-        mm, mm_e2e = float(m[0]), float(m[1])
+    t_ms, e2e_ms, mm, mm_e2e = combine_ranks(t_ms, e2e_ms, mm, mm_e2e, dev)
     if rank != 0:
         if ws > 1:
             dist.destroy_process_group()
