@@ -502,12 +502,15 @@ __global__ void __launch_bounds__(TX * BY, level_min_blocks<real, FL>()) level_s
 // lanes 0 and 31 are the x halo) and a strip of BYT consecutive y rows, and
 // marches its CTA's z-chunk.  T planes p-1 .. p+3 of the strip and its two
 // halo rows sit in a 6-deep register ring (plane p+3 is loaded while plane p
-// is computed, so a load has two plane iterations to arrive); the per-node
-// inputs (phase, melt time, RHS box) are loaded two planes ahead.  z and y stencils are register arithmetic and
-// the x stencil takes the neighbouring lanes' partial sums by shuffles, so
-// warps never wait on one another.  The Dirichlet nodes (x/y ring, bottom
-// plane) are written by the last z-slice of CTAs, which does no stencil work:
-// the marching warps neither load ring values nor store ring nodes.
+// is computed, so a load has two plane iterations to arrive); the phase and
+// RHS-box inputs are loaded two planes ahead, the melt-time accumulators one
+// plane ahead and only at liquid nodes.  z and y stencils are register
+// arithmetic and the x stencil takes the neighbouring lanes' partial sums by
+// shuffles, so warps never wait on one another.  The Dirichlet nodes (x/y
+// ring, bottom plane) are written by the last z-slice of CTAs, which does no
+// stencil work: the marching warps neither load ring values nor store ring
+// nodes.  The laser's 1-D source factors come from a table of the step
+// (gm_fine_source_tables) or are evaluated per lane in the prologue.
 // ---------------------------------------------------------------------------
 constexpr int SEP_TILE = 30;  // output node columns of a warp
 constexpr int SEP_ZMAX = 32;  // planes a CTA marches (one z source factor a lane)
@@ -518,16 +521,16 @@ constexpr int sep_min_blocks() {
   return sizeof(real) != 4 ? 2 : (BYT == 1 ? 4 : (BYT == 2 ? 3 : 2));
 }
 
-// Top-surface flux of the strip's nodes: each lane evaluates the faces of
-// elements (x, y0-1+i), i = 0..BYT, at their 2 x 2 Gauss points and the node
-// sums are gathered from the lane to the left.  Called by every lane of the
-// warp (shuffles); one call per warp and launch, kept out of line so that the
-// unrolled plane loop stays small.
 template <typename real, int N>
 struct RegCol {  // a strip column passed by value (stays in registers across the call)
   real v[N];
 };
 
+// Top-surface flux of the strip's nodes: each lane evaluates the faces of
+// elements (x, y0-1+i), i = 0..BYT, at their 2 x 2 Gauss points and the node
+// sums are gathered from the lane to the left.  Called by every lane of the
+// warp (shuffles); one call per warp and launch, kept out of line so that the
+// unrolled plane loop stays small.
 template <typename real, int BYT>
 __device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real w2, int x, int nx, int y0, int ny,
                                                       const RegCol<real, BYT + 2> T0c) {
