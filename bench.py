@@ -11,11 +11,12 @@ value : steps timed with CUDA events on the engine's stream, toolpath rows
         already on the device; L2 flushed between steps (untimed).
 e2e   : the same steps through the engine's public calls with the toolpath rows
         in host memory (H2D inside the timed region) and the per-step device->
-        host read of the Level-3 peak temperature that the driver's
-        temperature check does.
-roofline: the Level-3 level-step kernel timed alone with CUDA events (its
-        algorithmic bytes: 10 B per node: T read + write, phase byte read +
-        write) against the measured HBM copy bandwidth.
+        host read of the Level-3 peak temperature that go_melt.py's
+        temperature check (printLevelMaxMin) does.
+roofline: the Level-3 level-step kernel timed alone with CUDA events, 20
+        launches back to back as the subcycle issues them (its algorithmic
+        bytes: 10 B per node: T read + write, phase byte read + write) against
+        the measured HBM copy bandwidth.
 cpu_baseline / --impl reference: the NumPy FP64 oracle (a restatement of the
         reference's JAX code; JAX is not installed on the GPU host) timed on
         fine-level steps of the same workload.
