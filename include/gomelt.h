@@ -482,8 +482,9 @@ typedef struct gm_subcycle_plan {
   int graph;                 /* 1: capture the call's launches and run them as one CUDA graph, updated in
                                 place from call to call on the same stream (the first call on a stream
                                 issues directly) */
-  int pdl;                   /* 1: level steps launch as programmatic dependents of the kernel before
-                                them (their CTAs start while it drains) */
+  int pdl;                   /* 1: every kernel of the call after the factor table launches as a
+                                programmatic dependent of the kernel before it (its CTAs start while
+                                that one drains and wait for it before touching any field) */
   void* src3tab;             /* optional work (N2*N3 * (nx+ny+nz) of Level 3): the Level-3 laser factors
                                 of the call, tabulated at its start */
 } gm_subcycle_plan;
