@@ -121,10 +121,9 @@ template <typename real>
 __global__ void restrict_kernel(int n0, int n1, int n2, const Map3<real> m, const int* cx, const int* cy, const int* cz,
                                 int cnx, int cny, const real* fine, real* coarse) {
   pdl_begin();
-  const long long tot = (long long)n0 * n1 * n2;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+  const int tot = n0 * n1 * n2;  // < 2^31 (checked by the caller)
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+    const int i = t % n0, j = (t / n0) % n1, k = t / (n0 * n1);
     const real v = map3_apply(m, i, j, k, fine);
     coarse[cx[i] + (long long)cy[j] * cnx + (long long)cz[k] * cnx * cny] = v;
   }
@@ -282,6 +281,7 @@ extern "C" int gm_restrict(const gm_restrict_args* g, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
   if (tot == 0) return GM_OK;
+  if (tot >= (1LL << 31)) return GM_ERR_TOO_LARGE;
   if (g->dtype == GM_F32)
     launch_k(restrict_kernel<float>, dim3(grid_for(tot)), dim3(256), 0, st, g->n[0], g->n[1], g->n[2],
              make_map3<float>(g->map), g->cidx[0], g->cidx[1], g->cidx[2], g->cnx, g->cny, (const float*)g->fine,
@@ -366,28 +366,30 @@ template <typename real>
 __global__ void ring_kernel(int nx, int ny, int nz, const Map3<real> m, const real* srcA, const real* srcB,
                             real* outA, real* outB) {
   pdl_begin();
-  const long long nb = (long long)nx * ny;                // bottom plane
-  const long long nxf = 2LL * ny * (nz - 1);              // x faces above the bottom
-  const long long nyf = 2LL * (nx > 2 ? nx - 2 : 0) * (nz - 1);  // y faces, x interior
-  const long long tot = nb + nxf + nyf;
-  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < tot; r += (long long)gridDim.x * blockDim.x) {
+  // ring nodes in the order bottom plane, x faces, y faces, with x or y the
+  // fastest index inside each plane (contiguous stores on the bottom plane
+  // and the y faces); counts < 2^31 (checked by the caller)
+  const int nb = nx * ny;                               // bottom plane
+  const int nxf = 2 * ny * (nz - 1);                    // x faces above the bottom
+  const int nyi = nx > 2 ? nx - 2 : 0;
+  const int nyf = 2 * nyi * (nz - 1);                   // y faces, x interior
+  const int tot = nb + nxf + nyf;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < tot; r += gridDim.x * blockDim.x) {
     int ix, iy, iz;
     if (r < nb) {
-      ix = (int)(r % nx);
-      iy = (int)(r / nx);
+      ix = r % nx;
+      iy = r / nx;
       iz = 0;
     } else if (r < nb + nxf) {
-      const long long q = r - nb;
-      iz = 1 + (int)(q % (nz - 1));
-      const long long q2 = q / (nz - 1);
-      iy = (int)(q2 % ny);
-      ix = (q2 / ny) ? nx - 1 : 0;
+      const int q = r - nb, q2 = q / ny;
+      iy = q - q2 * ny;
+      ix = (q2 & 1) ? nx - 1 : 0;
+      iz = 1 + (q2 >> 1);
     } else {
-      const long long q = r - nb - nxf;
-      iz = 1 + (int)(q % (nz - 1));
-      const long long q2 = q / (nz - 1);
-      ix = 1 + (int)(q2 % (nx - 2));
-      iy = (q2 / (nx - 2)) ? ny - 1 : 0;
+      const int q = r - nb - nxf, q2 = q / nyi;
+      ix = 1 + (q - q2 * nyi);
+      iy = (q2 & 1) ? ny - 1 : 0;
+      iz = 1 + (q2 >> 1);
     }
     real w8[8];
     const int b = map3_weights(m, ix, iy, iz, w8);
@@ -399,7 +401,7 @@ __global__ void ring_kernel(int nx, int ny, int nz, const Map3<real> m, const re
       a += w8[j] * srcA[b + off[j]];
       if (srcB) c += w8[j] * srcB[b + off[j]];
     }
-    const long long id = ix + (long long)iy * nx + (long long)iz * nx * ny;
+    const int id = ix + iy * nx + iz * nb;
     outA[id] = a;
     if (outB) outB[id] = c;
   }
@@ -408,6 +410,7 @@ __global__ void ring_kernel(int nx, int ny, int nz, const Map3<real> m, const re
 extern "C" int gm_ring_prolong(const gm_ring_args* g, void* stream) {
   if (!g || !g->srcA || !g->outA || (g->srcB == nullptr) != (g->outB == nullptr)) return GM_ERR_ARG;
   if (g->nodes[0] < 2 || g->nodes[1] < 2 || g->nodes[2] < 2 || !map_ok(g->map, g->nodes)) return GM_ERR_ARG;
+  if ((long long)g->nodes[0] * g->nodes[1] * g->nodes[2] >= (1LL << 31)) return GM_ERR_TOO_LARGE;
   const long long nx = g->nodes[0], ny = g->nodes[1], nz = g->nodes[2];
   const long long tot = nx * ny + 2 * ny * (nz - 1) + 2 * (nx - 2) * (nz - 1);
   cudaStream_t st = (cudaStream_t)stream;
