@@ -506,14 +506,31 @@ __global__ void __launch_bounds__(TX * BY, level_min_blocks<real, FL>()) level_s
 // RHS-box inputs are loaded two planes ahead, the melt-time accumulators one
 // plane ahead and only at liquid nodes.  z and y stencils are register
 // arithmetic and the x stencil takes the neighbouring lanes' partial sums by
-// shuffles, so warps never wait on one another.  The Dirichlet nodes (x/y
-// ring, bottom plane) are written by the last z-slice of CTAs, which does no
-// stencil work: the marching warps neither load ring values nor store ring
+// shuffles, so warps never wait on one another.  The marching chunks cover
+// node planes 1 .. ntop-1 (and the inactive planes above ntop); the top plane
+// ntop (one-sided z operators, surface flux) is computed by a z-slice of its
+// own, so the marching loop carries no top-plane case.  The Dirichlet nodes
+// (x/y ring, bottom plane) are written by the last z-slice of CTAs, which does
+// no stencil work: the marching warps neither load ring values nor store ring
 // nodes.  The laser's 1-D source factors come from a table of the step
 // (gm_fine_source_tables) or are evaluated per lane in the prologue.
 // ---------------------------------------------------------------------------
 constexpr int SEP_TILE = 30;  // output node columns of a warp
 constexpr int SEP_ZMAX = 32;  // planes a CTA marches (one z source factor a lane)
+
+// Node planes [1, sep_march_end) are marched in z-chunks; plane ntop (the top
+// of the active element planes: one-sided z operators, surface flux) has a
+// z-slice of CTAs of its own, and plane 0 is Dirichlet.  With inactive planes
+// above ntop (reset to T_amb) the march runs to nz and passes over ntop.
+__host__ __device__ inline int sep_march_end(int nz, int ntop, bool inact) {
+  return inact && ntop < nz - 1 ? nz : ntop;
+}
+// z-slices of a separable launch: the marching chunks, then the top-plane
+// slice, then the Dirichlet slice
+__host__ __device__ inline int sep_march_chunks(int nz, int ntop, bool inact, int zc) {
+  const int mz = sep_march_end(nz, ntop, inact);
+  return mz > 1 ? cdiv(mz - 1, zc) : 0;
+}
 
 template <typename real, int BYT>
 constexpr int sep_min_blocks() {
@@ -569,7 +586,8 @@ __device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real 
 }
 
 // One CTA of the separable step: x-tile bx, strip group by, z-chunk bz of a
-// (gx, gy, ring_z + 1) grid; z-chunk ring_z is the Dirichlet slice.
+// (gx, gy, ring_z + 1) grid; z-slice ring_z - 1 is the top plane and ring_z
+// the Dirichlet slice.
 template <typename real, int BYT, int FL>
 __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, int bz, int gx, int gy,
                                          int ring_z) {
@@ -688,7 +706,11 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     return;
   }
 
-  const int Z0 = bz * a.zchunk, Z1 = min(nz, Z0 + a.zchunk);
+  // z-slice ring_z - 1 computes the top plane, the others march their chunk
+  const bool top_slice = bz == ring_z - 1;
+  if (top_slice && (ntop < 1 || ntop >= nz)) return;
+  const int Z0 = top_slice ? ntop : 1 + bz * a.zchunk;
+  const int Z1 = top_slice ? ntop + 1 : min(sep_march_end(nz, ntop, hInact), Z0 + a.zchunk);
   // stencil constants: A = a1 (Zm- + 4 Zm + Zm+), B = b1 Ky(Zm) + b2 My(Zk)
   const real a1 = a.sa1, b1 = a.sb1, b2 = a.sb2;
   const real minv = dt / a.smass;  // 1 / (8 elements' lumped mass)
@@ -780,12 +802,6 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     }
   };
 
-  load_plane(Tr[0], Z0 - 1);
-  load_plane(Tr[1], Z0);
-  load_plane(Tr[2], Z0 + 1);
-  load_plane(Tr[3], Z0 + 2);
-  prefetch(std::integral_constant<int, 0>(), Z0);
-  prefetch(std::integral_constant<int, 1>(), Z0 + 1);
   // the output rows of a strip column (strip rows 1..BYT)
   auto rows_of = [&](const real* c) {
     RegCol<real, BYT> o;
@@ -793,6 +809,99 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     for (int r = 0; r < BYT; ++r) o.v[r] = c[r + 1];
     return o;
   };
+  // register arrays passed by value to plane_out
+  auto strip_of = [&](const real* c) {
+    RegCol<real, RY> o;
+#pragma unroll
+    for (int i = 0; i < RY; ++i) o.v[i] = c[i];
+    return o;
+  };
+  auto node_of = [&](const real* c) {
+    RegCol<real, BYT> o;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) o.v[r] = c[r];
+    return o;
+  };
+  auto phase_of = [&](const uint32_t* c) {
+    RegCol<uint32_t, BYT> o;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) o.v[r] = c[r];
+    return o;
+  };
+
+  // New values of the strip's nodes of plane p from T planes p-1, p, p+1
+  // (Tm, T0, Tp; Tp unused on the top plane) and the plane's per-node inputs.
+  // TOP: one-sided z operators, the lumped mass of 4 elements, surface flux.
+  auto plane_out = [&](auto top_c, int p, const RegCol<real, RY> Tm, const RegCol<real, RY> T0,
+                       const RegCol<real, RY> Tp, const RegCol<real, BYT> surf, real sz,
+                       const RegCol<uint32_t, BYT> ph, const RegCol<real, BYT> rhs, const RegCol<real, BYT> acc,
+                       const RegCol<real, BYT> mac) {
+    constexpr bool TOP = decltype(top_c)::value;
+    // ---- z and y stencils in registers, x stencil by shuffles ----
+    real Zm[RY], Zk[RY];
+#pragma unroll
+    for (int i = 0; i < RY; ++i) {
+      if (TOP) {
+        Zm[i] = Tm.v[i] + (real)2 * T0.v[i];
+        Zk[i] = T0.v[i] - Tm.v[i];
+      } else {
+        const real s = Tm.v[i] + Tp.v[i];
+        Zm[i] = s + (real)4 * T0.v[i];
+        Zk[i] = (real)2 * T0.v[i] - s;
+      }
+    }
+    const real mi = TOP ? (real)2 * minv : minv;
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) {
+      const int i = r + 1;
+      const real u = Zm[i - 1] + Zm[i + 1];
+      const real w = Zk[i - 1] + Zk[i + 1];
+      const real A = a1 * (u + (real)4 * Zm[i]);
+      const real B = b1 * ((real)2 * Zm[i] - u) + b2 * (w + (real)4 * Zk[i]);
+      // x stencil: (2A - A(x-1) - A(x+1)) + (B(x-1) + 4B + B(x+1)) = 2A + 4B + D(x-1) + D(x+1), D = B - A
+      const real D = B - A;
+      const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
+      if (!row_out[r] || (!TOP && hInact && p == ntop)) continue;
+      const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
+      const real Told = T0.v[i];
+      real Rt = -KT;
+      if (hLaser) Rt += sxy[r] * sz;
+      if (hBox) Rt += rhs.v[r];
+      if (TOP && hSurf) Rt += surf.v[r];
+      real Tn = Told + Rt * mi;
+      if (!TOP && hInact && p > ntop) Tn = P.T_amb;
+      finish(x + (y0 + r) * nx + p * nxy, Tn, Told, ph.v[r], acc.v[r], mac.v[r]);
+    }
+  };
+
+  if (top_slice) {
+    real Tm[RY], T0[RY], surf[BYT];
+    load_plane(Tm, ntop - 1);
+    load_plane(T0, ntop);
+    prefetch(std::integral_constant<int, 0>(), ntop);
+    if (hAcc) prefetch_acc(std::integral_constant<int, 0>(), ntop, rows_of(T0));
+#pragma unroll
+    for (int r = 0; r < BYT; ++r) surf[r] = 0;
+    if (hSurf) {  // convection / radiation / evaporation on the faces of element plane ntop-1
+      RegCol<real, RY> col;
+#pragma unroll
+      for (int i = 0; i < RY; ++i) col.v[i] = T0[i];
+      const RegCol<real, BYT> sf = sep_surface<real, BYT>(P, a.w2, x, nx, y0, ny, col);
+#pragma unroll
+      for (int r = 0; r < BYT; ++r) surf[r] = sf.v[r];
+    }
+    const real sz = hLaser ? __shfl_sync(FULL, szl, 0) : (real)0;
+    plane_out(std::true_type(), ntop, strip_of(Tm), strip_of(T0), strip_of(T0), node_of(surf), sz, phase_of(nph[0]),
+              node_of(nrhs[0]), node_of(nacc[0]), node_of(nmac[0]));
+    return;
+  }
+
+  load_plane(Tr[0], Z0 - 1);
+  load_plane(Tr[1], Z0);
+  load_plane(Tr[2], Z0 + 1);
+  load_plane(Tr[3], Z0 + 2);
+  prefetch(std::integral_constant<int, 0>(), Z0);
+  prefetch(std::integral_constant<int, 1>(), Z0 + 1);
   if (hAcc) prefetch_acc(std::integral_constant<int, 0>(), Z0, rows_of(Tr[1]));
 
   // plane q lives in T slot (q - Z0 + 1) % 6 and per-node slot (q - Z0) % 3;
@@ -806,60 +915,9 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     if (p + 3 <= Z1) load_plane(Tr[(PAR + 4) % 6], p + 3);
     prefetch(std::integral_constant<int, (PAR + 2) % 3>(), p + 2);
     if (hAcc) prefetch_acc(std::integral_constant<int, (PAR + 1) & 1>(), p + 1, rows_of(Tp));
-
-    const bool top = p == ntop;
-    // ---- top surface (convection / radiation / evaporation on the faces of element plane ntop-1) ----
-    real surf[BYT];
-#pragma unroll
-    for (int r = 0; r < BYT; ++r) surf[r] = 0;
-    if (hSurf && top && ntop >= 1) {
-      RegCol<real, RY> col;
-#pragma unroll
-      for (int i = 0; i < RY; ++i) col.v[i] = T0[i];
-      const RegCol<real, BYT> sf = sep_surface<real, BYT>(P, a.w2, x, nx, y0, ny, col);
-#pragma unroll
-      for (int r = 0; r < BYT; ++r) surf[r] = sf.v[r];
-    }
-
-    // ---- z and y stencils in registers, x stencil by shuffles ----
-    real Zm[RY], Zk[RY];
-    if (top) {
-#pragma unroll
-      for (int i = 0; i < RY; ++i) {
-        Zm[i] = Tm[i] + (real)2 * T0[i];
-        Zk[i] = T0[i] - Tm[i];
-      }
-    } else {
-#pragma unroll
-      for (int i = 0; i < RY; ++i) {
-        const real s = Tm[i] + Tp[i];
-        Zm[i] = s + (real)4 * T0[i];
-        Zk[i] = (real)2 * T0[i] - s;
-      }
-    }
-    const real mi = top ? (real)2 * minv : minv;
     const real sz = hLaser ? __shfl_sync(FULL, szl, p - Z0) : (real)0;
-#pragma unroll
-    for (int r = 0; r < BYT; ++r) {
-      const int i = r + 1;
-      const real u = Zm[i - 1] + Zm[i + 1];
-      const real w = Zk[i - 1] + Zk[i + 1];
-      const real A = a1 * (u + (real)4 * Zm[i]);
-      const real B = b1 * ((real)2 * Zm[i] - u) + b2 * (w + (real)4 * Zk[i]);
-      // x stencil: (2A - A(x-1) - A(x+1)) + (B(x-1) + 4B + B(x+1)) = 2A + 4B + D(x-1) + D(x+1), D = B - A
-      const real D = B - A;
-      const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
-      if (!row_out[r] || p == 0) continue;
-      const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
-      const real Told = T0[i];
-      real Rt = -KT;
-      if (hLaser) Rt += sxy[r] * sz;
-      if (hBox) Rt += nrhs[NB][r];
-      if (hSurf) Rt += surf[r];
-      real Tn = Told + Rt * mi;
-      if (hInact && p > ntop) Tn = P.T_amb;
-      finish(x + (y0 + r) * nx + p * nxy, Tn, Told, nph[NB][r], nacc[PAR & 1][r], nmac[PAR & 1][r]);
-    }
+    plane_out(std::false_type(), p, strip_of(Tm), strip_of(T0), strip_of(Tp), node_of(nrhs[NB]), sz, phase_of(nph[NB]),
+              node_of(nrhs[NB]), node_of(nacc[PAR & 1]), node_of(nmac[PAR & 1]));
   };
 
   for (int p = Z0; p < Z1; p += 6) {
@@ -879,7 +937,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_ke
 
 // Many windows in one launch: instance b owns the linear CTAs
 // [first[b], first[b+1]) of the grid, laid out (bx, by, bz) with bx fastest
-// over its own (gx, gy, z-chunks + Dirichlet slice) grid; its parameters are
+// over its own (gx, gy, z-chunks + top and Dirichlet slices) grid; its parameters are
 // read from tab[b] into shared memory once per CTA.
 template <typename real, int BYT, int FL>
 __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>())
@@ -904,7 +962,7 @@ __global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>())
     sb[2] = local / (gx * gy);
     sb[3] = gx;
     sb[4] = gy;
-    sb[5] = cdiv(sa.nz, sa.zchunk);  // the Dirichlet slice
+    sb[5] = sep_march_chunks(sa.nz, sa.ne_planes, (FL & LF_INACT) != 0, sa.zchunk) + 1;  // the Dirichlet slice
   }
   __syncthreads();
   sep_body<real, BYT, FL>(sa, sb[0], sb[1], sb[2], sb[3], sb[4], sb[5]);
@@ -1075,8 +1133,9 @@ template <typename real, int FL, int BYT>
 static void launch_sep_t(const LevelK<real>& a, int warps, int zc, bool pdl, cudaStream_t st) {
   LevelK<real> b = a;
   b.zchunk = zc;
-  // the last z-slice of CTAs writes the Dirichlet nodes
-  const dim3 grid(cdiv(a.nx, SEP_TILE), cdiv(a.ny, warps * BYT), cdiv(a.nz, zc) + 1);
+  // z-slices: the marching chunks, the top plane, the Dirichlet nodes
+  const dim3 grid(cdiv(a.nx, SEP_TILE), cdiv(a.ny, warps * BYT),
+                  sep_march_chunks(a.nz, a.ne_planes, (FL & LF_INACT) != 0, zc) + 2);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = dim3(32 * warps);
@@ -1120,7 +1179,7 @@ static int launch_sep(const LevelK<real>& a, int fl, const TuneVal& v, bool pdl,
 // the 161 x 161 x 41 Level-3 window), and the z-chunk (<= SEP_ZMAX) whose CTA
 // count best fills the SMs: busiest SM's CTAs x (planes + 2 halo planes).
 template <typename real>
-static TuneVal sep_default(const gm_level_args* g) {
+static TuneVal sep_default(const gm_level_args* g, bool inact) {
   static int sms = 0;
   if (sms == 0) {
     int dev = 0, n = 0;
@@ -1133,7 +1192,7 @@ static TuneVal sep_default(const gm_level_args* g) {
   const long long gxy = (long long)cdiv(g->nx, SEP_TILE) * cdiv(g->ny, v.wys * v.rows);
   double best = -1;
   for (int zc = 2; zc <= min(g->nz, SEP_ZMAX); ++zc) {
-    const long long ctas = gxy * cdiv(g->nz, zc);
+    const long long ctas = gxy * (sep_march_chunks(g->nz, g->ne_planes, inact, zc) + 1);
     const long long waves = (ctas + (long long)sms * res - 1) / ((long long)sms * res);
     const double cost = (double)waves * (zc + 2);
     if (best < 0 || cost < best - 1e-9) {
@@ -1245,7 +1304,7 @@ static int launch_level(const gm_level_args* g, const gm_props* pr, cudaStream_t
     if (g->zchunk <= 0 && tuned_shape(TuneKey{g->dtype, fl, g->nx, g->ny, g->nz}, &v)) {
       sh = v;
     } else if (sep_ok) {
-      sh = sep_default<real>(g);
+      sh = sep_default<real>(g, (fl & LF_INACT) != 0);
       if (g->zchunk > 0) sh.zchunk = g->zchunk;
     } else {
       sh = TuneVal{0, 0, 0, 0, g->zchunk};
@@ -1291,6 +1350,7 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
   bool sep = true;
   for (int b = 0; b < nb; ++b) sep = sep && level_flags(&g[b], &p[b]) == fl && sep_eligible(&g[b], fl);
   if (sep) {
+    const bool inact = (fl & LF_INACT) != 0;
     // separable: one z-chunk for the batch from the wave model over all
     // instances' x/y tiles (6 resident 4-warp CTAs per SM in FP32, 3 in FP64)
     static int sms = 0;
@@ -1309,7 +1369,7 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
       long long ctas = 0;
       for (int b = 0; b < nb; ++b)
         ctas += (long long)cdiv(g[b].nx, SEP_TILE) * cdiv(g[b].ny, SEP_BATCH_WARPS * SEP_BATCH_ROWS) *
-                (cdiv(g[b].nz, zc) + 1);
+                (sep_march_chunks(g[b].nz, g[b].ne_planes, inact, zc) + 2);
       const long long waves = (ctas + (long long)sms * res - 1) / ((long long)sms * res);
       const double cost = (double)waves * (zc + 2);
       if (best < 0 || cost < best - 1e-9) {
@@ -1321,8 +1381,8 @@ static int prepare_batched(const gm_level_args* g, int nb, const gm_props* p, vo
       LevelK<real>& a = tabs[b];
       a = make_levelk<real>(&g[b], &p[b]);
       a.zchunk = (g[b].zchunk > 0 && g[b].zchunk <= SEP_ZMAX) ? g[b].zchunk : zc_batch;
-      const long long blocks = (long long)cdiv(a.nx, SEP_TILE) *
-                               cdiv(a.ny, SEP_BATCH_WARPS * SEP_BATCH_ROWS) * (cdiv(a.nz, a.zchunk) + 1);
+      const long long blocks = (long long)cdiv(a.nx, SEP_TILE) * cdiv(a.ny, SEP_BATCH_WARPS * SEP_BATCH_ROWS) *
+                               (sep_march_chunks(a.nz, a.ne_planes, inact, a.zchunk) + 2);
       if (first[b] + blocks >= (1LL << 31)) return GM_ERR_TOO_LARGE;
       first[b + 1] = first[b] + (int)blocks;
     }
