@@ -59,6 +59,8 @@ def parse_args():
                          "or 'tiles,TILE_X,ZCHUNK'")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the Level-3 level-step kernel --steps times (for profiling)")
+    ap.add_argument("--l3-accum", action="store_true",
+                    help="--kernel-only: the corrector's Level-3 step (with the melt-time update)")
     ap.add_argument("--precision", action="store_true",
                     help="FP32 against FP64 on the 2.5 um Level-3 window: T error and melt pool")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the FP32-vs-FP64 check")
@@ -821,13 +823,15 @@ def run_kernel_only(args):
             if args.l3_shape:
                 kern.level_step_shape(eng.ps, stream=eng.stream, **shape,
                                       **eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last,
-                                                         ring=ring, alpha=0.5))
+                                                         ring=ring, alpha=0.5, accum=args.l3_accum))
             else:
-                eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
+                eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5,
+                           accum=args.l3_accum)
         e1.record(eng.stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    print(json.dumps({"kernel_only": "level step (Level 3)", "launches": args.steps, "nodes": eng.geo.L[3].nn,
+    what = "level step (Level 3, melt-time update)" if args.l3_accum else "level step (Level 3)"
+    print(json.dumps({"kernel_only": what, "launches": args.steps, "nodes": eng.geo.L[3].nn,
                       "us_per_launch_host_issued": 1000 * e0.elapsed_time(e1) / args.steps,
                       "shape": args.l3_shape or shape_json(tuned[3])}))
 
