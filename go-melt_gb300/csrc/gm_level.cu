@@ -657,21 +657,24 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // ---- Dirichlet nodes, spread over the threads of this slice: the bottom
     // plane, then the x/y ring of planes 1..nz-1 (perimeter order y0, y1, x0, x1) ----
+    // 32-bit enumeration: nring <= nx ny nz < 2^31 (node ids are 32-bit), and
+    // an unsigned k + stride stays below 2^32
     const int perim = 2 * nx + 2 * (ny - 2);
-    const long long nring = (long long)nxy + (long long)(nz - 1) * perim;
-    const long long nthr = (long long)gx * gy * blockDim.x;
+    const unsigned nring = (unsigned)(nxy + (nz - 1) * perim);
     const long long t0 = ((long long)by * gx + bx) * blockDim.x + threadIdx.x;
+    if (t0 >= nring) return;
+    const unsigned nthr = (unsigned)min((long long)gx * gy * blockDim.x, (long long)nring);
 #pragma unroll 4
-    for (long long k = t0; k < nring; k += nthr) {
+    for (unsigned k = (unsigned)t0; k < nring; k += nthr) {
       int rx, ry, rp;
-      if (k < nxy) {
+      if (k < (unsigned)nxy) {
         rp = 0;
-        rx = (int)k % nx;
-        ry = (int)k / nx;
+        rx = (int)(k % (unsigned)nx);
+        ry = (int)(k / (unsigned)nx);
       } else {
-        const long long kk = k - nxy;
-        rp = 1 + (int)(kk / perim);
-        const int j = (int)(kk % perim);
+        const unsigned kk = k - (unsigned)nxy;
+        rp = 1 + (int)(kk / (unsigned)perim);
+        const int j = (int)(kk % (unsigned)perim);
         if (j < nx) {
           rx = j;
           ry = 0;
