@@ -1,0 +1,105 @@
+"""The algebra of the separable level step, restated on the CPU and checked
+against the oracle's element-by-element solveMatrixFreeFE.  CPU only.
+
+For constant k and rho*c the element sum of solveMatrixFreeFE
+(computeFunctions.py:582-642) is the assembled brick operator
+k [Kx (x) My (x) Mz + Mx (x) Ky (x) Mz + Mx (x) My (x) Kz] T with the lumped
+mass (rho c / dt)(hx hy hz / 8) times the element count of the node.  The
+separable kernel (level_sep_kernel in gm_level.cu) evaluates it per node as
+  Zm = Tm + Tp + 4 T0, Zk = 2 T0 - Tm - Tp   (one-sided on the top plane:
+  Zm = Tm + 2 T0, Zk = T0 - Tm),
+  u, w = y-neighbour sums of Zm, Zk,
+  A = a1 (u + 4 Zm), B = b1 (2 Zm - u) + b2 (w + 4 Zk),
+  K T = 2 A + 4 B + D(x-1) + D(x+1), D = B - A,
+with a1, b1, b2 = k hy hz / (36 hx), k hx hz / (36 hy), k hx hy / (36 hz),
+and T+ = T + (-K T) dt / (hx hy hz rho c) (twice that on the top plane).
+This file restates exactly those formulas in NumPy and compares them with the
+oracle on anisotropic grids, with all element planes active and with inactive
+planes above the top.
+"""
+
+import numpy as np
+import pytest
+
+import gomelt_oracle as O
+
+
+def level(nx, ny, nz, h):
+    coords, connect = O.createMesh3D((0.0, h[0] * (nx - 1), nx), (0.0, h[1] * (ny - 1), ny),
+                                     (-h[2] * (nz - 1), 0.0, nz))
+    return {"node_coords": coords, "connect": connect}
+
+
+def separable_step(T, k, rc, dt, h, ntop):
+    """New temperatures of the nodes off the x/y ring on node planes
+    1..ntop, in the kernel's order of operations (no source, no flux)."""
+    hx, hy, hz = h
+    a1, b1, b2 = k * hy * hz / (36 * hx), k * hx * hz / (36 * hy), k * hx * hy / (36 * hz)
+    minv = dt / (hx * hy * hz * rc)
+    out = {}
+    for p in range(1, ntop + 1):
+        Tm, T0 = T[p - 1], T[p]
+        if p < ntop:
+            Tp = T[p + 1]
+            s = Tm + Tp
+            Zm, Zk, mi = s + 4 * T0, 2 * T0 - s, minv
+        else:
+            Zm, Zk, mi = Tm + 2 * T0, T0 - Tm, 2 * minv
+        u = Zm[:-2] + Zm[2:]  # rows 1..ny-2
+        w = Zk[:-2] + Zk[2:]
+        A = a1 * (u + 4 * Zm[1:-1])
+        B = b1 * (2 * Zm[1:-1] - u) + b2 * (w + 4 * Zk[1:-1])
+        D = B - A
+        KT = (2 * A[:, 1:-1] + 4 * B[:, 1:-1]) + (D[:, :-2] + D[:, 2:])
+        out[p] = T0[1:-1, 1:-1] + (-KT) * mi
+    return out
+
+
+@pytest.mark.parametrize("dims,h,inactive", [
+    ((13, 9, 8), (0.010, 0.015, 0.007), 0),
+    ((7, 11, 5), (0.020, 0.005, 0.012), 0),
+    ((10, 8, 9), (0.005, 0.005, 0.005), 3),  # the top three node planes inactive
+    ((6, 6, 3), (0.004, 0.006, 0.005), 1),   # one active element plane
+])
+def test_separable_form_equals_element_sum(dims, h, inactive):
+    nx, ny, nz = dims
+    L = level(nx, ny, nz, h)
+    hs = [float(np.asarray(L["node_coords"][d])[1] - np.asarray(L["node_coords"][d])[0]) for d in range(3)]
+    ntop = nz - 1 - inactive  # top of the active element planes (node plane index)
+    ne = (nx - 1) * (ny - 1) * ntop
+    rng = np.random.default_rng(nx * 100 + ny * 10 + nz)
+    nn = nx * ny * nz
+    T = 300 + 1500 * rng.random(nn)
+    k, rc, dt = 0.022, 4.4e-6 * 700, 1.5e-6
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ref = O.solveMatrixFreeFE(L, nn, ne, np.full(nn, k), np.full(nn, rc), dt, T, np.zeros(nn), np.zeros(nn))
+    ref = ref.reshape(nz, ny, nx)
+    got = separable_step(T.reshape(nz, ny, nx), k, rc, dt, hs, ntop)
+    T3 = T.reshape(nz, ny, nx)
+    for p in range(1, ntop + 1):
+        inc_ref = ref[p, 1:-1, 1:-1] - T3[p, 1:-1, 1:-1]
+        inc_got = got[p] - T3[p, 1:-1, 1:-1]
+        scale = np.abs(inc_ref).max()
+        assert scale > 0
+        np.testing.assert_allclose(inc_got, inc_ref, rtol=0, atol=1e-10 * scale)
+
+
+def test_lumped_mass_counts():
+    """The lumped mass of solveMatrixFreeFE is (rho c / dt)(h^3 / 8) times the
+    node's element count: 8 inside, 4 on the top plane (the constants the
+    kernel folds into dt / (hx hy hz rho c) and twice that on the top)."""
+    nx, ny, nz = 6, 5, 4
+    h = (0.01, 0.02, 0.005)
+    L = level(nx, ny, nz, h)
+    nn = nx * ny * nz
+    ne = (nx - 1) * (ny - 1) * (nz - 1)
+    rc, dt = 3.08e-3, 2e-6
+    # with K T = 0 (uniform T) and F = 1 the update returns 1 + 1/M
+    T = np.ones(nn)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = O.solveMatrixFreeFE(L, nn, ne, np.full(nn, 0.02), np.full(nn, rc), dt, T, np.ones(nn), np.zeros(nn))
+    M = 1.0 / (out - 1.0)
+    M = M.reshape(nz, ny, nx)
+    m8 = rc / dt * h[0] * h[1] * h[2]
+    np.testing.assert_allclose(M[1:-1, 1:-1, 1:-1], m8, rtol=1e-12)
+    np.testing.assert_allclose(M[-1, 1:-1, 1:-1], m8 / 2, rtol=1e-12)
