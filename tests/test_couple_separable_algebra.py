@@ -1,0 +1,120 @@
+"""The algebra of the separable coupling terms, restated on the CPU and
+checked against the oracle's element reduction.  CPU only.
+
+For constant k and rho*c the subgrid flux and mass terms of the coarse level
+(computeCoarseTprimeTerm_jax / computeCoarseTprimeMassTerm_jax,
+computeFunctions.py:1396-1565, and the Part-1/Part-2 functions that call
+them) are tensor products of 1-D maps from the fine nodes of the window to
+the coarse nodes of its box:
+  V = k [cf0 (Dx Iy Iz) + cf1 (Ix Dy Iz) + cf2 (Ix Iy Dz)] T'
+      - (wq / dt) rho c (Ix Iy Iz)(dTa - dTb),
+  cf_d = -2 wq / (H_d h_d), wq = hx hy hz / 8,
+with, per axis, D[N, i] the coarse gradient sign times the fine difference
+over the fine elements assigned to coarse element N - A, and I[N, i] the
+Gauss-side coarse weights times the fine linear shape functions.  The
+per-axis tables come from the product's host geometry (geometry.couple_axis)
+and the contraction follows couple_sep_x/y/z of gm_couple.cu.  Fine elements
+are assigned to the coarse element of their first Gauss point while each
+point keeps the weights of its own element, as the reference does; the
+offset windows below make fine elements straddle coarse nodes.
+"""
+
+import numpy as np
+import pytest
+
+import gomelt_oracle as O
+from geometry import couple_axis
+
+PQ, MQ = (1 + 1 / np.sqrt(3)) / 2, (1 - 1 / np.sqrt(3)) / 2
+
+
+def level(lo, hi, n):
+    coords, connect = O.createMesh3D((lo[0], hi[0], n[0]), (lo[1], hi[1], n[1]), (lo[2], hi[2], n[2]))
+    return {"node_coords": coords, "connect": connect, "nn": n[0] * n[1] * n[2]}
+
+
+def axis_maps(ax):
+    """D and I of one axis over the box: (ncb + 1) coarse nodes x fine nodes."""
+    ncb, flo, fhi, cw = ax["ncb"], ax["flo"], ax["fhi"], ax["cw"]
+    f0 = int(flo[0])
+    nfn = int(fhi[ncb - 1]) - f0 + 1
+    D = np.zeros((ncb + 1, nfn))
+    I = np.zeros((ncb + 1, nfn))
+    for N in range(ncb + 1):
+        for A in (1, 0):
+            c = N - A
+            if c < 0 or c >= ncb:
+                continue
+            sg = 1.0 if A else -1.0
+            for e in range(flo[c], fhi[c]):
+                a0 = cw[e, 0, A] * PQ + cw[e, 1, A] * MQ
+                a1 = cw[e, 0, A] * MQ + cw[e, 1, A] * PQ
+                i = e - f0
+                D[N, i + 1] += sg
+                D[N, i] -= sg
+                I[N, i] += a0
+                I[N, i + 1] += a1
+    return D, I, f0, nfn
+
+
+def separable_terms(fine, coarse, k, rc, dt, Tp, dT):
+    axes = [couple_axis(fine["node_coords"][d], coarse["node_coords"][d]) for d in range(3)]
+    maps = [axis_maps(a) for a in axes]
+    h = [float(np.asarray(fine["node_coords"][d])[1] - np.asarray(fine["node_coords"][d])[0]) for d in range(3)]
+    wq = h[0] * h[1] * h[2] / 8
+    cf = [-2 * wq / (axes[d]["H"] * h[d]) for d in range(3)]
+    nf = [np.asarray(fine["node_coords"][d]).size for d in range(3)]
+    sl = tuple(slice(maps[d][2], maps[d][2] + maps[d][3]) for d in (2, 1, 0))
+    (Dx, Ix, _, _), (Dy, Iy, _, _), (Dz, Iz, _, _) = maps
+    F = Tp.reshape(nf[2], nf[1], nf[0])[sl]
+    G = dT.reshape(nf[2], nf[1], nf[0])[sl]
+    V = k * (cf[0] * np.einsum("ak,bj,ci,kji->abc", Iz, Iy, Dx, F)
+             + cf[1] * np.einsum("ak,bj,ci,kji->abc", Iz, Dy, Ix, F)
+             + cf[2] * np.einsum("ak,bj,ci,kji->abc", Dz, Iy, Ix, F))
+    V -= (wq * rc / dt) * np.einsum("ak,bj,ci,kji->abc", Iz, Iy, Ix, G)
+    return V, [a["lo"] for a in axes]
+
+
+def element_terms(fine, coarse, k, rc, dt, Tp, dT):
+    shape = O.computeCoarseFineShapeFunctions(coarse, fine)
+    nn = fine["nn"]
+    flux, wq = O._fine_flux(fine, Tp, np.full(nn, k))
+    mass, w = O._fine_mass(fine, dT, np.full(nn, rc), dt)
+    nnc = coarse["nn"]
+    return O._flux_project(shape, flux, wq, nnc) + O._mass_project(shape, mass, w, nnc)
+
+
+CASES = {
+    # Level-3 window in a Level-2 level (ratio 4), grids aligned
+    "l3_in_l2": (((0.6, 0.6, -0.2), (1.4, 1.4, 0.0), (41, 41, 11)),
+                 ((0.8, 0.9, -0.06), (1.2, 1.1, 0.0), (81, 41, 13))),
+    # Level-3 window in a Level-1 level (ratio 20 in x/y, 20 in z)
+    "l3_in_l1": (((0.0, 0.0, -0.6), (2.0, 2.0, 0.0), (21, 21, 7)),
+                 ((0.8, 0.9, -0.06), (1.2, 1.1, 0.0), (81, 41, 13))),
+    # offset window: fine elements straddle coarse nodes along every axis
+    "offset": (((0.6, 0.6, -0.2), (1.4, 1.4, 0.0), (41, 41, 11)),
+               ((0.813, 0.907, -0.0613), (1.0, 1.003, -0.0013), (35, 19, 9))),
+    # anisotropic fine spacing, ratio 3 / 5 / 2
+    "aniso": (((0.0, 0.0, -0.3), (1.2, 0.9, 0.0), (13, 10, 7)),
+              ((0.3, 0.2, -0.2), (0.6, 0.5, 0.0), (10, 16, 5))),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_separable_coupling_equals_element_reduction(case):
+    (clo, chi, cn), (flo, fhi, fn) = CASES[case]
+    coarse, fine = level(clo, chi, cn), level(flo, fhi, fn)
+    rng = np.random.default_rng(len(case))
+    nn = fine["nn"]
+    Tp = 50 * rng.standard_normal(nn)
+    dT = 20 * rng.standard_normal(nn)
+    k, rc, dt = 0.022, 4.4e-6 * 700, 1.575e-5
+    ref = element_terms(fine, coarse, k, rc, dt, Tp, dT).reshape(cn[2], cn[1], cn[0])
+    V, lo = separable_terms(fine, coarse, k, rc, dt, Tp, dT)
+    box = tuple(slice(lo[d], lo[d] + V.shape[2 - d]) for d in (2, 1, 0))
+    scale = np.abs(ref).max()
+    assert scale > 0
+    np.testing.assert_allclose(V, ref[box], rtol=0, atol=1e-11 * scale)
+    outside = ref.copy()
+    outside[box] = 0
+    assert np.abs(outside).max() <= 1e-12 * scale  # no term outside the box
