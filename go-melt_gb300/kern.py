@@ -9,11 +9,9 @@ from __future__ import annotations
 import ctypes as C
 from typing import NamedTuple
 
-import numpy as np
 import torch
 
 import _native as N
-from geometry import AxisMap
 
 
 def ptr(t):

@@ -20,12 +20,10 @@ import time
 import numpy as np
 import torch
 
-import _native as N
 import diagnostics
 import engine
 import levels
 import surrogate
-import workloads
 
 ACCEPT_RESIDUAL = 0.01
 

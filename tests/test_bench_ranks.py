@@ -2,7 +2,6 @@
 the slowest rank's time and the summed scan length, and the reference arm
 runs on rank 0 only.  Two gloo ranks on CPU."""
 
-import json
 import os
 import socket
 import subprocess

@@ -6,7 +6,6 @@ import numpy as np
 
 import diag_oracle as D
 import gomelt_oracle as O
-from test_gpu_level import PHASE_PROPS
 
 NODES = (21, 17, 9)
 H = (0.005, 0.005, 0.005)

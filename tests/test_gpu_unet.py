@@ -4,7 +4,6 @@ BF16-rounded inputs."""
 
 import ctypes as C
 
-import numpy as np
 import pytest
 import torch
 import torch.nn.functional as F
