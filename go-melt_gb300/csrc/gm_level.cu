@@ -919,6 +919,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     prefetch(std::integral_constant<int, (PAR + 2) % 3>(), p + 2);
     if (hAcc) prefetch_acc(std::integral_constant<int, (PAR + 1) & 1>(), p + 1, rows_of(Tp));
     const real sz = hLaser ? __shfl_sync(FULL, szl, p - Z0) : (real)0;
+    // the surface-flux column is read on the top plane only: any column serves here
     plane_out(std::false_type(), p, strip_of(Tm), strip_of(T0), strip_of(Tp), node_of(nrhs[NB]), sz, phase_of(nph[NB]),
               node_of(nrhs[NB]), node_of(nacc[PAR & 1]), node_of(nmac[PAR & 1]));
   };
