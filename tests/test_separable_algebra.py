@@ -15,7 +15,8 @@ with a1, b1, b2 = k hy hz / (36 hx), k hx hz / (36 hy), k hx hy / (36 hz),
 and T+ = T + (-K T) dt / (hx hy hz rho c) (twice that on the top plane).
 This file restates exactly those formulas in NumPy and compares them with the
 oracle on anisotropic grids, with all element planes active and with inactive
-planes above the top.
+planes above the top.  It also checks the Hadamard-mode form of the element
+matrix that the element-tile kernel applies (any material).
 """
 
 import numpy as np
@@ -103,3 +104,36 @@ def test_lumped_mass_counts():
     m8 = rc / dt * h[0] * h[1] * h[2]
     np.testing.assert_allclose(M[1:-1, 1:-1, 1:-1], m8, rtol=1e-12)
     np.testing.assert_allclose(M[-1, 1:-1, 1:-1], m8 / 2, rtol=1e-12)
+
+
+# reference local node order of a hex8 element (convert2XYZ, :676-687): (x, y, z) corner bits
+CORNERS = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+
+
+@pytest.mark.parametrize("h", [(0.005, 0.005, 0.005), (0.01, 0.02, 0.005), (0.1, 0.02, 0.0025)])
+def test_hadamard_stiffness_equals_element_matrix(h):
+    """The element-tile kernel (level_body in gm_level.cu) applies the brick
+    stiffness as a forward Hadamard butterfly of the 8 corner values, a
+    scaling of modes 1..7 by lam_m k and the inverse butterfly, with
+    lam_m = (Kx My Mz + Mx Ky Mz + Mx My Kz) / 8 from the 1-D eigenvalues
+    (K: 0 or 2/h, M: h/2 or h/6 for the constant or the difference mode).
+    That equals the reference's element matrix BTB * wq of
+    solveMatrixFreeFE (2x2x2 Gauss); the lumped mass per corner is
+    wq = hx hy hz / 8."""
+    hx, hy, hz = h
+    coords = np.array([[c[0] * hx, c[1] * hy, c[2] * hz] for c in CORNERS], dtype=float)
+    N, dNdx, wq = O.hex8_basis(coords)
+    BTB = sum(dNdx[:, :, d].T @ dNdx[:, :, d] for d in range(3))
+    K_ref = BTB * wq[0][0]
+    K_had = np.zeros((8, 8))
+    for m in range(8):
+        mx, my, mz = m & 1, (m >> 1) & 1, (m >> 2) & 1
+        Mx, My, Mz = (hx / 6 if mx else hx / 2), (hy / 6 if my else hy / 2), (hz / 6 if mz else hz / 2)
+        Kx, Ky, Kz = (2 / hx if mx else 0.0), (2 / hy if my else 0.0), (2 / hz if mz else 0.0)
+        lam = (Kx * My * Mz + Mx * Ky * Mz + Mx * My * Kz) / 8.0
+        v = np.array([np.prod([(1.0 if c[d] else -1.0) if (m >> d) & 1 else 1.0 for d in range(3)])
+                      for c in CORNERS])
+        K_had += lam * np.outer(v, v)
+    np.testing.assert_allclose(K_had, K_ref, rtol=0, atol=1e-12 * np.abs(K_ref).max())
+    # lumped mass: row sums of N^T N wq are the same for every corner
+    np.testing.assert_allclose((N.T @ N * wq[0][0]).sum(axis=0), hx * hy * hz / 8, rtol=1e-13)
