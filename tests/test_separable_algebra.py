@@ -137,3 +137,47 @@ def test_hadamard_stiffness_equals_element_matrix(h):
     np.testing.assert_allclose(K_had, K_ref, rtol=0, atol=1e-12 * np.abs(K_ref).max())
     # lumped mass: row sums of N^T N wq are the same for every corner
     np.testing.assert_allclose((N.T @ N * wq[0][0]).sum(axis=0), hx * hy * hz / 8, rtol=1e-13)
+
+
+def src_factor(i, n, rel, h, inv_r2):
+    """1-D laser factor of node i (src_factor in gm_common.cuh): the two
+    elements e = i-1, i at their two Gauss points, weighted by node i's
+    linear shape function there."""
+    g0, g1 = (1 - 1 / np.sqrt(3)) / 2, (1 + 1 / np.sqrt(3)) / 2
+    s = 0.0
+    for e in (i - 1, i):
+        if e < 0 or e >= n - 1:
+            continue
+        d0 = rel + h * (e + g0)
+        d1 = rel + h * (e + g1)
+        q0 = np.exp(-3 * d0 * d0 * inv_r2)
+        q1 = np.exp(-3 * d1 * d1 * inv_r2)
+        s += (g1 * q0 + g0 * q1) if i == e else (g0 * q0 + g1 * q1)
+    return s
+
+
+@pytest.mark.parametrize("laser", [(0.031, 0.052, -0.001), (0.0, 0.09, 0.0), (0.2, -0.05, -0.03)])
+def test_separable_laser_source_equals_gauss_point_sum(laser):
+    """The level kernels evaluate computeSourcesL3 (:2960-3012) as
+    src_c P fx(i) fy(j) fz(k), src_c = 6 sqrt(3) eta rc^2 dc (hx hy hz / 8),
+    rc = 1 / (r sqrt(pi)), dc = 1 / (d sqrt(pi)), with the 1-D factors above;
+    the reference sums the 3-D Gaussian at the 8 Gauss points of every
+    element.  The last laser position lies outside the window."""
+    nx, ny, nz = 17, 12, 7
+    h = (0.007, 0.011, 0.005)
+    L = level(nx, ny, nz, h)
+    props = {"laser_eta": 0.35, "laser_radius": 0.05, "laser_depth": 0.03}
+    P = 200.0
+    ne, nn = (nx - 1) * (ny - 1) * (nz - 1), nx * ny * nz
+    ref = O.computeSourcesL3(L, np.asarray(laser), (0, ne, 0, 0, nn), props, P).reshape(nz, ny, nx)
+    c = [np.asarray(L["node_coords"][d], dtype=float) for d in range(3)]
+    r, dd = props["laser_radius"], props["laser_depth"]
+    rc, dc = 1 / (r * np.sqrt(np.pi)), 1 / (dd * np.sqrt(np.pi))
+    src_c = 6 * np.sqrt(3) * props["laser_eta"] * rc * rc * dc * (h[0] * h[1] * h[2] / 8)
+    fx = np.array([src_factor(i, nx, c[0][0] - laser[0], h[0], 1 / r**2) for i in range(nx)])
+    fy = np.array([src_factor(j, ny, c[1][0] - laser[1], h[1], 1 / r**2) for j in range(ny)])
+    fz = np.array([src_factor(k, nz, c[2][0] - laser[2], h[2], 1 / dd**2) for k in range(nz)])
+    got = src_c * P * fz[:, None, None] * fy[None, :, None] * fx[None, None, :]
+    scale = np.abs(ref).max()
+    assert scale > 0
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-11 * scale)
