@@ -16,7 +16,8 @@ and T+ = T + (-K T) dt / (hx hy hz rho c) (twice that on the top plane).
 This file restates exactly those formulas in NumPy and compares them with the
 oracle on anisotropic grids, with all element planes active and with inactive
 planes above the top.  It also checks the Hadamard-mode form of the element
-matrix that the element-tile kernel applies (any material).
+matrix that the element-tile kernel applies (any material), the kernels'
+separable laser-source factors and their top-surface flux assembly.
 """
 
 import numpy as np
@@ -181,3 +182,61 @@ def test_separable_laser_source_equals_gauss_point_sum(laser):
     scale = np.abs(ref).max()
     assert scale > 0
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-11 * scale)
+
+
+def surface_flux(gp, Tq):
+    """surface_flux of gm_common.cuh on the product's gm_props [W/mm^2]."""
+    Tq = np.minimum(Tq, gp.T_boiling + 1000)
+    q = gp.h_conv * (gp.T_amb - Tq) + gp.sigma_sb * gp.emissivity * (gp.T_amb ** 4 - Tq ** 4)
+    if gp.evc != 0:
+        S = (gp.evc * gp.CP_coeff * np.exp(-gp.CT_coeff * (1 / Tq - 1 / gp.T_boiling)) * np.sqrt(gp.CM_coeff / Tq)
+             * (gp.Lev + gp.cp_fluid * (Tq - gp.T_amb)))
+        q = q - S
+    return q * 1e-6
+
+
+@pytest.mark.parametrize("evaporation", [0.0, 0.82])
+def test_surface_flux_assembly_equals_reference(evaporation):
+    """The top-surface flux of the level kernels (sep_surface in
+    gm_level.cu): per top element the 2 x 2 Gauss points of its upper face
+    with the bilinear weights (1 +- 1/sqrt3)/2, q(Tq) hx hy / 4, gathered to
+    the four corners; the flux constants come from the product's gm_props
+    (_native.props_struct).  Reference: computeConvRadBC (:2207-2301)."""
+    import _native as N
+
+    P = O.SetupProperties({
+        "thermal_conductivity_powder": 0.4, "thermal_conductivity_bulk_a0": 4.23,
+        "thermal_conductivity_bulk_a1": 0.016, "thermal_conductivity_fluid_a0": 29.0,
+        "heat_capacity_solid_a0": 383.1, "heat_capacity_solid_a1": 0.174, "heat_capacity_mushy": 3235.0,
+        "heat_capacity_fluid": 769.0, "density": 8e-06, "laser_radius": 0.04, "laser_depth": 0.03,
+        "laser_power": 250.0, "laser_absorptivity": 0.45, "T_amb": 298.15, "T_solidus": 1533,
+        "T_liquidus": 1609, "T_boiling": 3038.0, "h_conv": 1.5e-05, "emissivity": 0.3,
+        "evaporation_coefficient": evaporation, "layer_height": 0.02})
+    gp = N.props_struct(P)
+    nx, ny, nz = 11, 9, 4
+    hx, hy = 0.006, 0.009
+    L = level(nx, ny, nz, (hx, hy, 0.005))
+    nn, ne = nx * ny * nz, (nx - 1) * (ny - 1) * (nz - 1)
+    rng = np.random.default_rng(5)
+    T = 300 + 3500 * rng.random(nn)  # includes temperatures above T_boiling + 1000
+    ref = O.computeConvRadBC(L, T, ne, nn, P, np.zeros(nn)).reshape(nz, ny, nx)
+    Tt = T.reshape(nz, ny, nx)[-1]
+    PQ, MQ = (1 + 1 / np.sqrt(3)) / 2, (1 - 1 / np.sqrt(3)) / 2
+    w2 = hx * hy / 4
+    F = np.zeros((ny, nx))
+    for ey in range(ny - 1):
+        for ex in range(nx - 1):
+            t00, t10, t01, t11 = Tt[ey, ex], Tt[ey, ex + 1], Tt[ey + 1, ex], Tt[ey + 1, ex + 1]
+            for qy in (0, 1):
+                for qx in (0, 1):
+                    px0, px1 = (MQ, PQ) if qx else (PQ, MQ)
+                    py0, py1 = (MQ, PQ) if qy else (PQ, MQ)
+                    Tq = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11
+                    q = surface_flux(gp, Tq) * w2
+                    F[ey, ex] += px0 * py0 * q
+                    F[ey, ex + 1] += px1 * py0 * q
+                    F[ey + 1, ex] += px0 * py1 * q
+                    F[ey + 1, ex + 1] += px1 * py1 * q
+    scale = np.abs(ref).max()
+    assert scale > 0 and np.abs(ref[:-1]).max() == 0  # flux on the top plane only
+    np.testing.assert_allclose(F, ref[-1], rtol=0, atol=1e-12 * scale)
