@@ -104,12 +104,12 @@ def combine_ranks(t_ms, e2e_ms, mm, mm_e2e, device):
     return float(t[0]), float(t[1]), float(m[0]), float(m[1])
 
 
-def workload(config=1):
+def workload(precision=False):
     import createPath
     import levels
     import workloads
 
-    cfg = workloads.config2() if config == 2 else workloads.config1()
+    cfg = workloads.precision_window() if precision else workloads.part_scale_raster()
     P = levels.setup_properties(cfg["properties"])
     nm = levels.setup_nonmesh(cfg["nonmesh"])
     r = cfg["raster"]
@@ -553,7 +553,7 @@ def run_precision(args):
     window inside the part-scale Level 1 / 2)."""
     import torch
 
-    cfg, P, nm, rows = workload(config=2)
+    cfg, P, nm, rows = workload(precision=True)
     dev = torch.device("cuda", 0)
     r = compare_fp64(cfg, P, nm, rows, args.steps, dev, iso=P["T_liquidus"])
     r.update({"precision_study": "L3 0.5x0.5x0.1 mm @ 2.5 um (200x200x40) in L1 200x200x50 @ 100 um, "
@@ -574,7 +574,7 @@ def run_surrogate(args):
     import workloads
 
     dev = torch.device("cuda", 0)
-    inst = workloads.config3(n=args.instances)
+    inst = workloads.batched_instances(n=args.instances)
     snaps, t_gen = SR.generate(inst, dev)
     nodes0 = [81, 81, 21]
     net = surrogate.UNet(dev, seed=0)
@@ -662,7 +662,7 @@ def run_batched(args):
 
     dev = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=dev)
-    inst = workloads.config3(n=args.instances)
+    inst = workloads.batched_instances(n=args.instances)
     engs, rowsv = [], []
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):

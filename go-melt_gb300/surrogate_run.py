@@ -1,7 +1,7 @@
 """Snapshots, training and evaluation of the Level-3 surrogate.
 
 * ``generate`` — plain multilevel runs of the batched single-track instances
-  (``workloads.config3``); per Level-2 step of every subcycle call one
+  (``workloads.batched_instances``); per Level-2 step of every subcycle call one
   snapshot: the Level-2 field at the step's end prolongated to Level 3, the
   Level-3 field at its start and at its end, and the window / laser
   parameters.  Kept on the device (FP32).

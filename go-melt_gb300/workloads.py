@@ -39,7 +39,7 @@ def _cond(T=300.0):
     return {"x": [T, T], "y": [T, T], "z": [T, T]}
 
 
-def config0():
+def single_track():
     """Single 4 mm track on a 5x5x1 mm block (L1 50x50x10 @ 100 um, L2 1x1x0.2 mm
     window 50x50x10 @ 20 um, L3 0.4x0.4x0.1 mm window 80x80x20 @ 5 um)."""
     return {
@@ -55,7 +55,7 @@ def config0():
     }
 
 
-def config1():
+def part_scale_raster():
     """Part-scale raster: L1 20x20x5 mm, 200x200x50 @ 100 um; L2 2x2x0.3 mm window,
     100x100x15 @ 20 um; L3 0.8x0.8x0.2 mm window, 160x160x40 @ 5 um (element counts:
     with these the windows sit on the coarser grids' nodes, which the reference's
@@ -74,19 +74,19 @@ def config1():
     }
 
 
-def config2():
-    """Precision study: config 1 with a fine Level-3 window of 0.5 x 0.5 x 0.1 mm
+def precision_window():
+    """Precision study: the part-scale raster with a fine Level-3 window of 0.5 x 0.5 x 0.1 mm
     at 2.5 um (200 x 200 x 40 elements; Level-2 to Level-3 ratio 8), placed on
     Level-2 nodes around the raster start.  dt3 = 0.394 us."""
-    c = config1()
+    c = part_scale_raster()
     c["Level3"] = {"elements": [200, 200, 40], "bounds": {"x": [9.76, 10.26], "y": [9.76, 10.26], "z": [-0.1, 0.0]}}
     c["nonmesh"]["timestep_L3"] = dt_fine(0.0025)
     return c
 
 
-def config3(n=64, seed=0):
+def batched_instances(n=64, seed=0):
     """Batched single-track instances: Level-1 meshes of U{30..120} x U{30..120}
-    x U{8..20} elements at 100 um, Level-2 / Level-3 windows as in config 0
+    x U{8..20} elements at 100 um, Level-2 / Level-3 windows as in the single track
     (1 x 1 x 0.2 mm at 20 um, 0.4 x 0.4 x 0.1 mm at 5 um); laser power
     U[100, 400] W, speed U[0.5, 1.5] m/s, radius U[35, 70] um, track angle
     U[0, 180) deg; the track is centred with length min(4 mm, what fits with

@@ -117,7 +117,7 @@ def test_energy_balance_closes_on_plain_steps():
     import workloads
     from diagnostics import Diagnostics
 
-    cfg = workloads.config0()
+    cfg = workloads.single_track()
     P = levels.setup_properties(cfg["properties"])
     nm = levels.setup_nonmesh(cfg["nonmesh"])
     rows = np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)

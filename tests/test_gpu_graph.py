@@ -16,7 +16,7 @@ def run(use_graph, nsteps=4):
     import levels
     import workloads
 
-    cfg = workloads.config0()
+    cfg = workloads.single_track()
     P = levels.setup_properties(cfg["properties"])
     nm = levels.setup_nonmesh(cfg["nonmesh"])
     rows = np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)
