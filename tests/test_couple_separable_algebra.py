@@ -16,7 +16,9 @@ per-axis tables come from the product's host geometry (geometry.couple_axis)
 and the contraction follows couple_sep_x/y/z of gm_couple.cu.  Fine elements
 are assigned to the coarse element of their first Gauss point while each
 point keeps the weights of its own element, as the reference does; the
-offset windows below make fine elements straddle coarse nodes.
+offset windows below make fine elements straddle coarse nodes.  The coarse
+laser source (computeLevelSource, :2667-2730) factorises the same way and is
+checked against the oracle's Gauss-point sum.
 """
 
 import numpy as np
@@ -118,3 +120,63 @@ def test_separable_coupling_equals_element_reduction(case):
     outside = ref.copy()
     outside[box] = 0
     assert np.abs(outside).max() <= 1e-12 * scale  # no term outside the box
+
+
+def coarse_source_separable(fine, coarse, props, rows):
+    """coarse_source_tables / coarse_source_assemble of gm_couple.cu: per
+    position p and axis d the 1-D table S_d[p][t] = sum over the fine Gauss
+    points assigned to coarse node t of their coarse weight times
+    exp(-3 (x_q - v_p)^2 / s^2) (s = r in x, y; laser depth in z), the x
+    table times cpre P_p; coarse node value = mean over p of Sx Sy Sz."""
+    axes = [couple_axis(fine["node_coords"][d], coarse["node_coords"][d]) for d in range(3)]
+    h = [float(np.asarray(fine["node_coords"][d])[1] - np.asarray(fine["node_coords"][d])[0]) for d in range(3)]
+    r, dd = props["laser_radius"], props["laser_depth"]
+    rc, dc = 1 / (r * np.sqrt(np.pi)), 1 / (dd * np.sqrt(np.pi))
+    cpre = 6 * np.sqrt(3) * props["laser_eta"] * rc * rc * dc * (h[0] * h[1] * h[2] / 8)
+    out = 0.0
+    for row in rows:
+        S = []
+        for d in range(3):
+            ax = axes[d]
+            s2 = dd * dd if d == 2 else r * r
+            t = np.zeros(ax["ncb"] + 1)
+            for N in range(ax["ncb"] + 1):
+                for A in (1, 0):
+                    c = N - A
+                    if c < 0 or c >= ax["ncb"]:
+                        continue
+                    for e in range(ax["flo"][c], ax["fhi"][c]):
+                        for sd in (0, 1):
+                            dx = ax["xq"][e, sd] - row[d]
+                            t[N] += ax["cw"][e, sd, A] * np.exp(-3 * dx * dx / s2)
+            S.append(t * (cpre * row[6]) if d == 0 else t)
+        out = out + np.einsum("a,b,c->abc", S[2], S[1], S[0])
+    return out / len(rows), [a["lo"] for a in axes]
+
+
+@pytest.mark.parametrize("case", ["l3_in_l2", "offset", "aniso"])
+def test_separable_coarse_source_equals_gauss_point_sum(case):
+    """gm_coarse_source against computeLevelSource (:2667-2730): the Level-3
+    Gauss-point source averaged over the coarse step's laser positions and
+    projected onto the coarse nodes."""
+    (clo, chi, cn), (flo, fhi, fn) = CASES[case]
+    coarse, fine = level(clo, chi, cn), level(flo, fhi, fn)
+    props = {"laser_eta": 0.35, "laser_radius": 0.05, "laser_depth": 0.03}
+    c = [np.asarray(fine["node_coords"][d]) for d in range(3)]
+    mid = [0.5 * (c[d][0] + c[d][-1]) for d in range(3)]
+    rows = np.zeros((5, 7))
+    for i in range(5):  # a short track across the window, the last position outside it
+        rows[i, :3] = [mid[0] - 0.02 + 0.01 * i, mid[1] + 0.004 * i, c[2][-1]]
+        rows[i, 6] = 150.0 + 10 * i
+    rows[4, 0] = c[0][-1] + 0.08
+    shape = O.computeCoarseFineShapeFunctions(coarse, fine)
+    ref = O.computeLevelSource({3: fine}, None, rows, shape, props, rows[:, 6], coarse["nn"])
+    ref = ref.reshape(cn[2], cn[1], cn[0])
+    V, lo = coarse_source_separable(fine, coarse, props, rows)
+    box = tuple(slice(lo[d], lo[d] + V.shape[2 - d]) for d in (2, 1, 0))
+    scale = np.abs(ref).max()
+    assert scale > 0
+    np.testing.assert_allclose(V, ref[box], rtol=0, atol=1e-11 * scale)
+    outside = ref.copy()
+    outside[box] = 0
+    assert np.abs(outside).max() <= 1e-12 * scale
