@@ -18,7 +18,8 @@ are assigned to the coarse element of their first Gauss point while each
 point keeps the weights of its own element, as the reference does; the
 offset windows below make fine elements straddle coarse nodes.  The coarse
 laser source (computeLevelSource, :2667-2730) factorises the same way and is
-checked against the oracle's Gauss-point sum.
+checked against the oracle's Gauss-point sum; the prolongation's per-axis
+tables and validity rule are checked against interpolatePoints.
 """
 
 import numpy as np
@@ -180,3 +181,39 @@ def test_separable_coarse_source_equals_gauss_point_sum(case):
     outside = ref.copy()
     outside[box] = 0
     assert np.abs(outside).max() <= 1e-12 * scale
+
+
+def test_separable_prolongation_equals_reference():
+    """The transfer kernels (interp_kernel, ring_kernel in gm_transfer.cu)
+    interpolate through per-axis tables of the host (geometry.axis_map: the
+    clipped-floor source element and the two linear weights per target
+    coordinate): the eight weights are products of per-axis weights in the
+    order (x0 y0 z0, x1 y0 z0, x1 y1 z0, x0 y1 z0, then z1), all eight in
+    [-0.01, 1.01] or the point gets zero, clipped to [0, 1].  Reference:
+    interpolatePoints (:1131-1210); targets here reach outside the source grid
+    on every axis."""
+    from geometry import axis_map
+
+    src = level((0.6, 0.6, -0.2), (1.4, 1.4, 0.0), (41, 41, 11))
+    rng = np.random.default_rng(3)
+    u = 300 + 1500 * rng.random(src["nn"])
+    tgt = [np.sort(rng.uniform(0.55, 1.45, 23)), np.sort(rng.uniform(0.58, 1.43, 17)),
+           np.sort(rng.uniform(-0.23, 0.02, 9))]
+    ref = O.interpolatePoints(src, u, tgt)
+    m = [axis_map(src["node_coords"][d], tgt[d]) for d in range(3)]
+    nx, ny = 41, 41
+    got = np.zeros((tgt[2].size, tgt[1].size, tgt[0].size))
+    for k in range(tgt[2].size):
+        for j in range(tgt[1].size):
+            for i in range(tgt[0].size):
+                (x0, x1), (y0, y1), (z0, z1) = m[0].w[i], m[1].w[j], m[2].w[k]
+                w8 = np.array([x0 * y0 * z0, x1 * y0 * z0, x1 * y1 * z0, x0 * y1 * z0,
+                               x0 * y0 * z1, x1 * y0 * z1, x1 * y1 * z1, x0 * y1 * z1])
+                ok = (w8 >= -1e-2).all() and (w8 <= 1 + 1e-2).all()
+                w8 = np.clip(w8, 0, 1) if ok else np.zeros(8)
+                b = m[0].elem[i] + m[1].elem[j] * nx + m[2].elem[k] * nx * ny
+                sx, sy, sz = 1, nx, nx * ny
+                corners = [b, b + sx, b + sx + sy, b + sy, b + sz, b + sx + sz, b + sx + sy + sz, b + sy + sz]
+                got[k, j, i] = (w8 * u[corners]).sum()
+    assert (ref == 0).any() and (ref != 0).any()  # both valid and rejected points
+    np.testing.assert_allclose(got.reshape(-1), ref, rtol=1e-13, atol=1e-9)
