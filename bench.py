@@ -43,6 +43,7 @@ WORKLOAD_NAME = ("part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, 
                  "first layer, N2=N3=10, dt3=1.575us")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_FILE = os.path.join(ROOT, "profiles", "level_sep_l3_part_scale.txt")
+PERSIST_PROFILE = os.path.join(ROOT, "profiles", "level3_persist_part_scale.txt")
 
 
 def parse_args():
@@ -70,6 +71,8 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
+    ap.add_argument("--no-persist", action="store_true",
+                    help="one launch per Level-3 fine step instead of the persistent Level-3 kernel")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the library's untuned launch shapes (for ncu launch lists: timings under ncu would "
                          "steer the autotuner)")
@@ -114,6 +117,7 @@ def workload(precision=False):
     nm = levels.setup_nonmesh(cfg["nonmesh"])
     r = cfg["raster"]
     gcode = createPath.serpentine_gcode(r["x0"], r["y0"], r["length"], r["hatch"], r["ntracks"])
+    cfg["gcode"] = gcode
     import numpy as np
 
     rows = np.asarray(createPath.toolpath(nm, P, gcode), dtype=np.float64)
@@ -186,16 +190,27 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per Level-3 level-step launch from the committed ncu summary."""
+def profile_traffic(path):
+    """DRAM bytes per launch of the dominant kernel, read from the committed
+    ncu summary of that kernel (a figure of an ncu capture of this workload,
+    not of this run: the bench cannot run under ncu)."""
     try:
-        with open(PROFILE_FILE) as f:
+        with open(path) as f:
             for line in f:
                 if line.startswith("dram_bytes_per_launch_full:"):
                     return float(line.split(":", 1)[1].split()[0])
     except (OSError, ValueError):
         pass
     return None
+
+
+def bench_config(ws):
+    """The workload description both arms print (the same keys and values)."""
+    return {"workload": WORKLOAD_NAME, "step": "moveEverything + subcycleGOMELT (100 fine steps)",
+            "l2": "flushed between steps (value: untimed; e2e: inside the timed region)",
+            "e2e": "toolpath rows generated on the device in FP64, window tables H2D per step, peak-T D2H per "
+                   "step read one step later",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
 
 
 # ---------------------------------------------------------------------------
@@ -216,10 +231,11 @@ def shape_json(v):
 
 # CPU oracle sample (reference arm and cpu_baseline)
 # ---------------------------------------------------------------------------
-def oracle_sample(cfg, rows, nsteps, warm=1):
+def oracle_sample(cfg, rows, nsteps, warm=1, keep=False):
     """Fine-level (Level 3) steps of the NumPy oracle along the toolpath:
     computeStateProperties + computeSourcesL3 + computeConvRadBC +
-    computeSolutions_L3 + clamp, per row.  Returns (mm/s, seconds, steps)."""
+    computeSolutions_L3 + clamp, per row, from the set-up state.  Returns
+    (mm/s, seconds, steps), and the final Level-3 field if ``keep``."""
     import numpy as np
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -247,14 +263,19 @@ def oracle_sample(cfg, rows, nsteps, warm=1):
         one(rows[i])
     dt = time.perf_counter() - t0
     mm = scan_mm(rows[warm - 1:warm + nsteps])
+    if keep:
+        return mm / dt, dt, nsteps, T
     return mm / dt, dt, nsteps
 
 
 def _oracle_worker(job):
     start, nsteps, warm = job
     cfg, P, nm, rows = workload()
+    if start == 0:  # the first worker's field is kept for the parity check
+        v, secs, n, T = oracle_sample(cfg, rows[start:], nsteps, warm=warm, keep=True)
+        return v * secs, secs, n, T
     v, secs, n = oracle_sample(cfg, rows[start:], nsteps, warm=warm)
-    return v * secs, secs, n
+    return v * secs, secs, n, None
 
 
 def oracle_parallel(nsteps, warm, workers=None):
@@ -271,6 +292,7 @@ def oracle_parallel(nsteps, warm, workers=None):
         res = pool.map(_oracle_worker, [(w * 500, nsteps, warm) for w in range(workers)])
     mm = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
+    oracle_parallel.first_field = res[0][3]  # worker 0's Level-3 field after warm + nsteps rows
     return mm / wall, wall, nsteps, workers
 
 
@@ -284,8 +306,7 @@ def run_reference(args):
         "unit": "mm/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * secs / n, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (generated G-code raster)",
-        "config": {"workload": WORKLOAD_NAME, "step": "moveEverything + subcycleGOMELT (100 fine steps)",
-                   "sample": "Level-3 fine steps on every host core"},
+        "config": bench_config(ws),
         "cpu_baseline": {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
                          "sample": f"{cores} processes x {n} Level-3 steps of the NumPy FP64 oracle (props, "
                                    f"source, surface flux, solve, Dirichlet ring, clamp), each on its own "
@@ -299,11 +320,67 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def persist_launcher(eng, chunk_rows, accum=False):
+    """The persistent Level-3 kernel as the subcycle launches it on the
+    engine's window (one launch = the N3 fine steps of one Level-2 step, ring
+    from the precomputed prolongation arrays, laser factors from the step's
+    table).  Returns launch(base) -> None and the number of fine steps a
+    launch runs; writes only scratch outputs."""
+    import ctypes as C
+
+    import torch
+
+    import _native as N
+    import kern
+
+    L3 = eng.geo.L[3]
+    N3 = eng.N3
+    nn = L3.nn
+    dev = eng.dev
+    rows_d = torch.as_tensor(chunk_rows[:N3], device=dev).contiguous()
+    Lw = int(sum(L3.nodes))
+    tab = torch.empty(N3 * Lw, dtype=eng.dtype, device=dev)
+    N.call("gm_fine_source_tables", kern.dtype_code(tab), (C.c_int * 3)(*L3.nodes), (C.c_double * 3)(*L3.origin()),
+           (C.c_double * 3)(*L3.spacing()), rows_d.data_ptr(), N3, C.byref(eng.ps), tab.data_ptr(),
+           kern.stream_ptr(eng.stream))
+    ring = eng._ring(3, eng.T[2], eng.T[2])
+    nf = int(N.lib().gm_level3_persist_flags((C.c_int * 3)(*L3.nodes)))
+    keep = dict(rows=rows_d, tab=tab, ring=ring, flags=torch.zeros(nf, dtype=torch.int32, device=dev),
+                xb=[torch.empty(nn, dtype=eng.dtype, device=dev) for _ in range(2)],
+                Tout=torch.empty_like(eng.T[3]), pout=torch.empty_like(eng.ph[3]),
+                acc=torch.zeros(nn, dtype=eng.dtype, device=dev), macc=torch.zeros(nn, dtype=eng.dtype, device=dev),
+                status=torch.zeros(1, dtype=torch.int32, device=dev))
+    a = N.gm_persist_args()
+    a.dtype = kern.dtype_code(eng.T[3])
+    for d in range(3):
+        a.nodes[d] = L3.nodes[d]
+        a.h[d] = L3.spacing()[d]
+    a.nsteps = a.nsub = N3
+    a.T_in, a.T_out = eng.T[3].data_ptr(), keep["Tout"].data_ptr()
+    a.ph_in, a.ph_out = eng.ph[3].data_ptr(), keep["pout"].data_ptr()
+    a.substrate = eng.substrate[3]
+    a.ring_new, a.ring_old = ring[0].data_ptr(), ring[1].data_ptr()
+    a.src_tab, a.rows = tab.data_ptr(), rows_d.data_ptr()
+    if accum:
+        a.accum, a.max_accum = keep["acc"].data_ptr(), keep["macc"].data_ptr()
+    a.xbuf[0], a.xbuf[1] = keep["xb"][0].data_ptr(), keep["xb"][1].data_ptr()
+    a.flags, a.flags_cap = keep["flags"].data_ptr(), nf
+    a.status = keep["status"].data_ptr()
+
+    def launch(base):
+        a.base = base
+        N.call("gm_level3_persist", C.byref(a), C.byref(eng.ps), kern.stream_ptr(eng.stream))
+
+    launch.keep = keep
+    return launch, N3
+
+
 def run_ours(args):
     import numpy as np
     import torch
 
     import _native as N
+    import createPath
     import engine
     import kern
 
@@ -316,6 +393,7 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     N.lib()
     cfg, P, nm, rows = workload()
+    runs = createPath.toolpath_runs(nm, P, cfg["gcode"])
     N2, N3 = nm["subcycle_num_L2"], nm["subcycle_num_L3"]
     n23 = N2 * N3
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
@@ -332,19 +410,32 @@ def run_ours(args):
         eng.move(rows[0], vstart)
         tuned = {} if args.no_autotune else eng.autotune(rows[0])  # launch shapes, measured (set-up, untimed)
         eng.use_graph = not args.no_graph  # each subcycle call as one CUDA graph
+        eng.use_persist = not args.no_persist
+        persist = eng.use_persist and eng.persist_shape() is not None
+        # toolpath rows generated on the device (FP64 accumulation) from the run table
+        tp = engine.DeviceToolpath(runs, dev, stream)
+        rows_buf = torch.empty(n23 * 7, dtype=torch.float64, device=dev)
+        dts_buf = torch.empty(N2 + 1, dtype=torch.float64, device=dev)
 
         def chunk(k):
             return rows[k * n23:(k + 1) * n23]
 
+        def device_step(k, plan=None):
+            """moveEverything + subcycleGOMELT of chunk k with its rows made on the device."""
+            if tp.emitted != k * n23:
+                raise SystemExit(f"toolpath generator at row {tp.emitted}, chunk {k} starts at {k * n23}")
+            tp.next(n23, N2, rows_buf, dts_buf)
+            eng.move(chunk(k)[0], vstart, plan)  # the host plans the window move from its mirror of the path
+            eng.subcycle(None, rows_device=rows_buf, dts_device=dts_buf)
+
         k = 0
         for _ in range(args.warmup):
-            eng.move(chunk(k)[0], vstart)
-            eng.subcycle(chunk(k))
+            device_step(k)
             k += 1
         stream.synchronize()
+        eng.check_status()
 
-        # ---- value: rows resident on the device --------------------------
-        dev_rows = [torch.as_tensor(chunk(k + i), device=dev) for i in range(args.steps)]
+        # ---- value: every input resident on the device ------------------
         clocks = Clocks(local)
         N.reset_launch_count()
         if ws > 1:
@@ -357,8 +448,7 @@ def run_ours(args):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.record(stream)
-            eng.move(chunk(k + i)[0], vstart)
-            eng.subcycle(chunk(k + i), rows_device=dev_rows[i])
+            device_step(k + i)
             e.record(stream)
             ev.append((s, e))
         torch.cuda.synchronize()
@@ -367,21 +457,20 @@ def run_ours(args):
         t_ms = sum(s.elapsed_time(e) for s, e in ev)
         mm = sum(scan_mm(chunk(k + i)) for i in range(args.steps))
         k += args.steps
+        eng.check_status()
 
-        # ---- e2e: host rows, H2D inside, D2H of the peak temperature -------
-        for _ in range(2):  # untimed: first use of the host-row and readback paths
-            c = chunk(k)
-            eng.move(c[0], vstart)
-            eng.subcycle(c)
+        # ---- e2e: through the engine API, tables H2D and peak D2H inside -----
+        for _ in range(2):  # untimed: first use of the readback path
+            device_step(k)
             float(eng.T[3].max().item())
             k += 1
         if ws > 1:
             dist.barrier()
         torch.cuda.synchronize()
-        # One step deep pipeline through the public API: step i+1 is issued
-        # (its table upload and host rows H2D included) before step i's peak
-        # temperature, copied to pinned memory, is read back and checked.  The
-        # 512 MB L2 flush runs inside the timed region before every step.
+        # One step deep pipeline: step i+1 is issued (its window-table upload
+        # included) before step i's peak temperature, copied to pinned memory,
+        # is read back and checked.  The toolpath rows are generated on the
+        # device; the 512 MB L2 flush runs inside the timed region.
         mm_e2e = 0.0
         h2d = 0
         peak = torch.empty(args.steps, dtype=eng.T[3].dtype, pin_memory=True)
@@ -390,42 +479,42 @@ def run_ours(args):
         plan = eng.plan_move(chunk(k)[0], vstart)
         for i in range(args.steps):
             flush.zero_()
-            c = chunk(k + i)
-            eng.move(c[0], vstart, plan)
-            eng.subcycle(c)
+            device_step(k + i, plan)
             peak[i:i + 1].copy_(eng.T[3].max().reshape(1), non_blocking=True)  # the per-chunk temperature check
-            ev = torch.cuda.Event()
-            ev.record(stream)
-            done.append(ev)
+            evt = torch.cuda.Event()
+            evt.record(stream)
+            done.append(evt)
             plan = eng.plan_move(chunk(k + i + 1)[0], vstart)  # host half of the next move, device busy
             if i > 0:
                 done[i - 1].synchronize()
                 tmax = float(peak[i - 1])
                 if not np.isfinite(tmax) or tmax > 1e5:
                     raise SystemExit(f"non-finite or invalid temperature {tmax}")
-            mm_e2e += scan_mm(c)
-            h2d += eng.last_table_bytes + 8 * (n23 * 7 + N2 + 1)
+            mm_e2e += scan_mm(chunk(k + i))
+            h2d += eng.last_table_bytes
         done[-1].synchronize()
         tmax = float(peak[args.steps - 1])
         e2e_ms = 1000.0 * (time.perf_counter() - t0)
         if not np.isfinite(tmax) or tmax > 1e5:
             raise SystemExit(f"non-finite or invalid temperature {tmax}")
-        eng.move(chunk(k + args.steps)[0], vstart, plan)
+        device_step(k + args.steps, plan)
         k += args.steps + 1
+        stream.synchronize()
+        eng.check_status()
 
         clk = clocks.stop()
 
-        # ---- dominant kernel alone: Level-3 level step as the subcycle runs it
-        # (Dirichlet ring from the precomputed ring arrays, bc_mode 3) --------
+        # ---- dominant kernel alone, as the subcycle runs it -------------------
         L3 = eng.geo.L[3]
+        last_chunk = chunk(k - 1)
+        reps = 20
+        # one-step separable kernel: Dirichlet ring from the precomputed ring
+        # arrays (bc_mode 3), programmatic dependent launches replayed from a
+        # CUDA graph so that the host's argument marshalling does not gap them
         Tout = torch.empty_like(eng.T[3])
         phout = torch.empty_like(eng.ph[3])
-        last = torch.as_tensor(chunk(k - 1)[-1], device=dev)
-        # Launched back to back from a CUDA graph, so that the host's per-call
-        # argument marshalling does not gap the launches, and as programmatic
-        # dependents of one another as the subcycle launches them.
+        last = torch.as_tensor(last_chunk[-1], device=dev)
         ring = eng._ring(3, eng.T[2], eng.T[2])
-        reps = 20
         l3kw = eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
 
         def l3():
@@ -439,7 +528,7 @@ def run_ours(args):
             for _ in range(reps):
                 l3()
         torch.cuda.synchronize()
-        k_ms = None
+        k1_ms = None
         for _ in range(3):
             flush.zero_()
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -448,8 +537,30 @@ def run_ours(args):
             e.record(stream)
             torch.cuda.synchronize()
             t = s.elapsed_time(e) / reps
-            k_ms = t if k_ms is None else min(k_ms, t)
+            k1_ms = t if k1_ms is None else min(k1_ms, t)
         del graph
+        # persistent kernel: N3 fine steps a launch, launches back to back
+        kp_ms = None
+        if persist:
+            launch, nper = persist_launcher(eng, last_chunk)
+            for b in range(3):
+                launch(b * nper)
+            base = 3 * nper
+            torch.cuda.synchronize()
+            preps = 10
+            for _ in range(3):
+                flush.zero_()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                for _ in range(preps):
+                    launch(base)
+                    base += nper
+                e.record(stream)
+                torch.cuda.synchronize()
+                t = s.elapsed_time(e) / preps
+                kp_ms = t if kp_ms is None else min(kp_ms, t)
+            if int(launch.keep["status"].item()) != 0:
+                raise SystemExit("persistent Level-3 kernel reported a failure")
 
     t_ms, e2e_ms, mm, mm_e2e = combine_ranks(t_ms, e2e_ms, mm, mm_e2e, dev)
     if rank != 0:
@@ -457,27 +568,37 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     peak, peak_kind = measured_peak()
-    alg_bytes = 10.0 * L3.nn
+    if persist:
+        alg_bytes = 10.0 * L3.nn * N3
+        k_ms = kp_ms
+        kname = f"level3_persist_kernel (Level 3, {N3} fine steps a launch, window in shared memory)"
+        traffic = profile_traffic(PERSIST_PROFILE)
+        tsrc = "profiles/level3_persist_part_scale.txt (ncu capture of this workload, not of this run)"
+    else:
+        alg_bytes = 10.0 * L3.nn
+        k_ms = k1_ms
+        kname = l3_kernel_name(tuned.get(3))
+        traffic = profile_traffic(PROFILE_FILE)
+        tsrc = "profiles/level_sep_l3_part_scale.txt (ncu capture of this workload, not of this run)"
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-    traffic = profile_traffic()
     line = {
         "metric": "simulated scan mm per wall-s (plain multilevel explicit step)",
         "value": mm / (t_ms * 1e-3), "unit": "mm/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if dtype == torch.float32 else "f64", "data": "synthetic (generated G-code raster)",
-        "config": {"workload": WORKLOAD_NAME,
-                   "step": "moveEverything + subcycleGOMELT (100 fine steps)",
-                   "l2": "flushed between steps (value: untimed; e2e: inside the timed region)",
-                   "e2e": "host rows and tables H2D per step, peak-T D2H per step read one step later",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": bench_config(ws),
         "e2e": {"value": mm_e2e / (e2e_ms * 1e-3), "unit": "mm/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": 4 if dtype == torch.float32 else 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": l3_kernel_name(tuned.get(3)), "kernel_ms": k_ms,
-                     "alg_bytes": alg_bytes, "peak_kind": peak_kind},
+                     "traffic": traffic, "traffic_source": tsrc, "kernel": kname, "kernel_ms": k_ms,
+                     "alg_bytes": alg_bytes, "alg_bytes_rule": "10 B per node per fine step (T read + write, "
+                     "phase byte read + write)", "peak_kind": peak_kind,
+                     "one_step_kernel": {"kernel": l3_kernel_name(tuned.get(3)), "ms": k1_ms,
+                                         "frac": 10.0 * L3.nn / (k1_ms * 1e-3) / 1e9 / peak}},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
+        "level3_persistent": persist,
         "autotuned": {f"L{lev}": shape_json(v) for lev, v in tuned.items()},  # L3acc: the corrector's step
     }
     if args.fp64_steps > 0:
@@ -493,9 +614,44 @@ def run_ours(args):
         line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
                                 "sample": f"{cores} processes x {n} Level-3 steps of the NumPy FP64 oracle "
                                           f"({secs:.1f} s); Level-1/2 work and coupling terms excluded"}
+        Tref = getattr(oracle_parallel, "first_field", None)
+        if Tref is not None:
+            line["parity_vs_oracle"] = parity_sample(cfg, P, nm, rows, args.cpu_steps + 1, Tref, dev, dtype)
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def parity_sample(cfg, P, nm, rows, nsteps, Tref, dev, dtype):
+    """The CPU baseline's first sample on the GPU: the same Level-3 fine steps
+    from the set-up state of the part-scale window (phase, source, surface
+    flux, solve with the ring of the resting Level-2 field, clamp), against the
+    oracle's field; max error relative to the oracle's peak."""
+    import numpy as np
+    import torch
+
+    import engine
+
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        eng = engine.Engine(cfg, P, nm["subcycle_num_L2"], nm["subcycle_num_L3"], dtype=dtype, device=dev,
+                            stream=stream)
+        eng.build_tables()
+        ring = eng._ring(3, eng.T[2], eng.T[2])
+        Ta, Tb = eng.T[3].clone(), torch.empty_like(eng.T[3])
+        pa, pb = eng.ph[3].clone(), torch.empty_like(eng.ph[3])
+        rd = torch.as_tensor(rows[:nsteps], device=dev)
+        for i in range(nsteps):
+            eng._level(3, Ta, Tb, rd[i, 5:6], pa, pb, laser=rd[i], ring=ring, alpha=1.0)
+            Ta, Tb, pa, pb = Tb, Ta, pb, pa
+        stream.synchronize()
+    got = Ta.double().cpu().numpy()
+    ref = np.asarray(Tref, dtype=float)
+    err = float(np.max(np.abs(got - ref)))
+    return {"what": f"part-scale Level-3 window, {nsteps} fine steps from rest along the raster: GPU "
+                    f"{'FP32' if dtype == torch.float32 else 'FP64'} against the NumPy FP64 oracle",
+            "max_abs_K": err, "max_rel": err / float(np.max(np.abs(ref))), "oracle_peak_K": float(np.max(ref)),
+            "bar": 1e-4}
 
 
 def compare_fp64(cfg, P, nm, rows, nsteps, dev, iso=None, stream=None):

@@ -184,18 +184,36 @@ class gm_subcycle_plan(C.Structure):
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("src2", vp), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
         ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int),
-        ("pdl", C.c_int), ("src3tab", vp)]
+        ("pdl", C.c_int), ("src3tab", vp), ("persist", C.c_int), ("xch3", vp * 2), ("pflags", vp),
+        ("pflags_cap", C.c_longlong), ("pstatus", vp)]
 
 
-def subcycle_kernel_count(N2: int, N3: int, separable: bool = False) -> int:
+class gm_persist_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("nodes", C.c_int * 3), ("h", C.c_double * 3), ("nsteps", C.c_int),
+                ("nsub", C.c_int), ("T_in", vp), ("T_out", vp), ("ph_in", vp), ("ph_out", vp),
+                ("substrate", C.c_longlong), ("ring_new", vp), ("ring_old", vp), ("src_tab", vp), ("rows", vp),
+                ("accum", vp), ("max_accum", vp), ("xbuf", vp * 2), ("flags", vp), ("flags_cap", C.c_longlong),
+                ("base", C.c_uint), ("status", vp), ("hold", C.c_int)]
+
+
+GM_PERSIST_TIMEOUT, GM_PERSIST_BAD_T = 1, 2
+
+
+class gm_toolpath_state(C.Structure):
+    _fields_ = [("run", C.c_longlong), ("k", C.c_longlong), ("row", C.c_longlong), ("x", C.c_double),
+                ("y", C.c_double), ("t", C.c_double)]
+
+
+def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bool = False) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
     steps (coupling 2 onto the step's source, Level-2 solve, Level-3 ring, N3
     Level-3 solves, restriction, T'), the T'2/mass/corrector block (7) and the tail
     (3).  For a constant-property material (separable kernels) each of the
     4 + 2 N2 coupling calls is one kernel more and the Level-3 laser factors
-    are tabulated once (one kernel)."""
-    n = 20 + 2 * (1 + N2 * (6 + N3))
+    are tabulated once (one kernel).  With persistent Level-3 steps the N3
+    solves of a Level-2 step are one kernel."""
+    n = 20 + 2 * (1 + N2 * (6 + (1 if persist else N3)))
     return n + (4 + 2 * N2 + 1 if separable else 0)
 
 
@@ -235,12 +253,17 @@ def lib():
         L.gm_unet_wgrad_scratch.restype = C.c_longlong
         L.gm_unet_head_scratch.argtypes = [C.c_longlong, C.c_int]
         L.gm_unet_head_scratch.restype = C.c_longlong
+        L.gm_level3_persist_flags.argtypes = [C.POINTER(C.c_int)]
+        L.gm_level3_persist_flags.restype = C.c_longlong
         _lib = L
     return _lib
 
 
 SIGNATURES = {
     "gm_level_step": [C.POINTER(gm_level_args), C.POINTER(gm_props), vp],
+    "gm_level3_persist": [C.POINTER(gm_persist_args), C.POINTER(gm_props), vp],
+    "gm_toolpath_rows": [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp],
+    "gm_level3_persist_shape": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "gm_state_properties": [C.POINTER(gm_state_props_args), C.POINTER(gm_props), vp],
     "gm_fine_source": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), vp,
                        C.POINTER(gm_props), vp, vp],

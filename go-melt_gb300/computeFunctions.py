@@ -625,13 +625,34 @@ def interpolatePoints(Level, u, node_coords_new):
 
 
 def getNewTprime(Fine, FineT0, CoarseT, Coarse, C2F):
-    """(:2060-2099) -> (T' of the fine level, coarse T with the overlap restricted)."""
-    val = interpolatePoints(Fine, FineT0, Fine["overlapCoords"])
-    idx = torch.as_tensor(_l0_index([int(n) for n in Coarse["nodes"]], Fine["overlapNodes"]),
-                          device=val.device)
-    CT = CoarseT.clone()
-    CT[idx] = val
-    return FineT0 - interpolate_w_matrix(C2F, CT), CT
+    """(:2060-2099) -> (T' of the fine level, coarse T with the overlap restricted).
+
+    The restriction (the fine field interpolated at the coarse overlap nodes,
+    written into a copy of the coarse field) is gm_restrict; T' = T_f - I(T_c)
+    is one gm_interp with the fine field as its base when C2F carries its
+    separable map (interpolatePointsMatrix, moveEverything), else
+    gm_interp_w_matrix over the materialised [Nc, node] pair."""
+    e = Fine.engine
+    FT = _dev_tensor(FineT0, e)
+    CT = _dev_tensor(CoarseT, e).clone()
+    rmap = _map_to(Fine, Fine["overlapCoords"])
+    cn = [int(n) for n in Coarse["nodes"]]
+    onodes = Fine["overlapNodes"]
+    idx_t = []
+    for d in range(3):
+        a = np.asarray(onodes[d])
+        if a.size == 0 or a.min() < 0 or a.max() >= cn[d]:
+            raise GomeltError(f"getNewTprime: overlap nodes of axis {d} outside the coarse grid")
+        idx_t.append(torch.as_tensor(a.astype(np.int32), device=e.dev))
+    idx = [C.cast(t.data_ptr(), C.POINTER(C.c_int)) for t in idx_t]
+    e._restrict(rmap, idx, cn, FT, CT)
+    cmap = getattr(C2F, "map", None)
+    if cmap is not None:
+        Tp = torch.empty_like(FT)
+        e._interp([(cmap, CT, -1.0)], e.geo.L[Fine.lev].nodes, Tp, base=FT)
+    else:
+        Tp = FT - interpolate_w_matrix(C2F, CT)
+    return Tp, CT
 
 
 def getBothNewTprimes(Levels, FineT, MesoT, M2F, CoarseT, C2M):

@@ -890,12 +890,17 @@ void* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
 
 // Device address of g_couple_scratch on the current device, looked up once per
-// device (host code cannot use the symbol itself as a device pointer).
-int scratch_address(void** out) {
+// device (host code cannot use the symbol itself as a device pointer).  The
+// look-up is refused while `stream` is being captured: a first call inside a
+// capture would otherwise run cudaGetSymbolAddress in the middle of it.
+int scratch_address(void* stream, void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GM_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (g_scratch_addr[dev] == nullptr) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &cs) != cudaSuccess) return GM_ERR_CUDA;
+    if (cs != cudaStreamCaptureStatusNone) return GM_ERR_ARG;  // first call on this device during a capture
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_couple_scratch) != cudaSuccess || p == nullptr) return GM_ERR_CUDA;
     g_scratch_addr[dev] = p;
@@ -907,14 +912,16 @@ int scratch_address(void** out) {
 
 extern "C" int gm_couple_noalloc(const gm_couple_args* g, const gm_props* p, void* stream) {
   if (!g || !p || !geom_ok(&g->geom)) return GM_ERR_ARG;
+  if (g->dtype != GM_F32 && g->dtype != GM_F64) return GM_ERR_ARG;
   const size_t esz = g->dtype == GM_F64 ? sizeof(double) : sizeof(float);
-  const long long need = gm_couple_partials_size(&g->geom);
-  if (need < 0) return GM_ERR_ARG;
-  if ((unsigned long long)need * esz > (unsigned long long)GM_COUPLE_NOALLOC_SCRATCH_BYTES) return GM_ERR_TOO_LARGE;
   void* scratch = nullptr;
-  const int rc = scratch_address(&scratch);
+  const int rc = scratch_address(stream, &scratch);
   if (rc != GM_OK) return rc;
-  gm_couple_args a = *g;  // same arguments; the caller's partials/partials_cap are not used
+  // Same arguments with the library's array as the partials: gm_couple picks
+  // its path against this capacity (the separable contraction when it fits,
+  // else the element reduction) and returns GM_ERR_TOO_LARGE when the path it
+  // takes needs more than the array holds.
+  gm_couple_args a = *g;
   a.partials = scratch;
   a.partials_cap = (long long)(GM_COUPLE_NOALLOC_SCRATCH_BYTES / esz);
   return gm_couple(&a, p, stream);

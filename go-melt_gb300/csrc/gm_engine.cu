@@ -29,6 +29,8 @@ struct Ctx {
   void* st;
   size_t esz;
   int rc = GM_OK;
+  bool persist = false;   // Level-3 steps of a Level-2 step as one persistent launch
+  unsigned pbase = 0;     // flag value at the next persistent launch
 };
 
 inline char* at(void* base, long long elems, size_t esz) { return (char*)base + elems * (long long)esz; }
@@ -246,7 +248,41 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
     level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 3, nullptr,
           p.ring2[0], p.ring2[1], (l2 + 1) / (double)N2, nullptr, nullptr);
     ring(c, p.L3, p.bc23, T2n, T2c, p.ring3[0], p.ring3[1]);
-    for (int l3 = 0; l3 < N3; ++l3) {
+    if (c.persist) {  // all N3 fine steps in one launch
+      const int i0 = l2 * N3;
+      const long long L3n = (long long)p.L3.nodes[0] + p.L3.nodes[1] + p.L3.nodes[2];
+      gm_persist_args a;
+      memset(&a, 0, sizeof(a));
+      a.dtype = p.dtype;
+      for (int d = 0; d < 3; ++d) {
+        a.nodes[d] = p.L3.nodes[d];
+        a.h[d] = p.L3.h[d];
+      }
+      a.nsteps = N3;
+      a.nsub = N3;
+      a.T_in = T3c;
+      a.T_out = p.T3w[l2 % 2];
+      a.ph_in = ph3c;
+      a.ph_out = p.ph3w[l2 % 2];
+      a.substrate = p.L3.substrate;
+      a.ring_new = p.ring3[0];
+      a.ring_old = p.ring3[1];
+      a.src_tab = at(p.src3tab, i0 * L3n, c.esz);
+      a.rows = p.rows + (long long)i0 * 7;
+      a.accum = part2 ? p.acc3 : nullptr;
+      a.max_accum = part2 ? p.macc3 : nullptr;
+      a.xbuf[0] = p.xch3[0];
+      a.xbuf[1] = p.xch3[1];
+      a.flags = p.pflags;
+      a.flags_cap = p.pflags_cap;
+      a.base = c.pbase;
+      a.status = p.pstatus;
+      GM_TRY(gm_level3_persist(&a, c.pr, c.st));
+      c.pbase += (unsigned)N3;
+      T3c = a.T_out;
+      ph3c = a.ph_out;
+    }
+    for (int l3 = 0; l3 < (c.persist ? 0 : N3); ++l3) {
       const int i = l2 * N3 + l3;
       void* Tn = p.T3w[i % 2];
       uint8_t* phn = p.ph3w[i % 2];
@@ -306,6 +342,18 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   if (p->src3tab)
     GM_TRY(gm_fine_source_tables(p->dtype, p->L3.nodes, p->L3.origin, p->L3.h, p->rows, p->N2 * p->N3, props,
                                  p->src3tab, stream));
+  // persistent Level-3 steps: needs the factor table, the work buffers and a
+  // constant-property material; the window must have a persistent shape
+  if (p->persist && p->src3tab && p->xch3[0] && p->xch3[1] && p->pflags && p->pstatus) {
+    int shp[4];
+    const long long nf = gm_level3_persist_flags(p->L3.nodes);
+    c.persist = nf > 0 && nf <= p->pflags_cap && gm_level3_persist_shape(p->dtype, p->L3.nodes, shp) == GM_OK &&
+                props->k_powder == props->k_bulk_a0 && props->k_fluid == props->k_bulk_a0 &&
+                props->k_bulk_a1 == 0.0 && props->cp_solid_a1 == 0.0 && props->cp_mushy == props->cp_solid_a0 &&
+                props->cp_fluid == props->cp_solid_a0;
+    if (c.persist && cudaMemsetAsync(p->pflags, 0, sizeof(unsigned) * nf, (cudaStream_t)stream) != cudaSuccess)
+      return GM_ERR_CUDA;
+  }
   // every later kernel of the call launches as a programmatic dependent of the one before it
   const gm::PdlScope pdl(p->pdl != 0);
 

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "gm_common.cuh"
+#include "gm_sep.cuh"
 
 namespace gm {
 
@@ -536,53 +537,6 @@ template <typename real, int BYT>
 constexpr int sep_min_blocks() {
   // 256-thread CTAs: 64, 85 or 128 registers a thread
   return sizeof(real) != 4 ? 2 : (BYT == 1 ? 4 : (BYT == 2 ? 3 : 2));
-}
-
-template <typename real, int N>
-struct RegCol {  // a strip column passed by value (stays in registers across the call)
-  real v[N];
-};
-
-// Top-surface flux of the strip's nodes: each lane evaluates the faces of
-// elements (x, y0-1+i), i = 0..BYT, at their 2 x 2 Gauss points and the node
-// sums are gathered from the lane to the left.  Called by every lane of the
-// warp (shuffles); one call per warp and launch, kept out of line so that the
-// unrolled plane loop stays small.
-template <typename real, int BYT>
-__device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real w2, int x, int nx, int y0, int ny,
-                                                      const RegCol<real, BYT + 2> T0c) {
-  constexpr unsigned FULL = 0xffffffffu;
-  const real* T0 = T0c.v;
-  RegCol<real, BYT> out;
-  real* surf = out.v;
-  const real PQ = (real)0.78867513459481288225, MQ = (real)0.21132486540518711775;  // (1 +- 1/sqrt3)/2
-  real c00[BYT + 1], c10[BYT + 1], c01[BYT + 1], c11[BYT + 1];
-#pragma unroll
-  for (int i = 0; i <= BYT; ++i) {  // element (x, y0 - 1 + i): strip rows i, i+1
-    const real t10 = __shfl_down_sync(FULL, T0[i], 1), t11 = __shfl_down_sync(FULL, T0[i + 1], 1);
-    c00[i] = c10[i] = c01[i] = c11[i] = 0;
-    const int ey = y0 - 1 + i;
-    if (x >= 0 && x < nx - 1 && ey >= 0 && ey < ny - 1) {
-      const real t00 = T0[i], t01 = T0[i + 1];
-#pragma unroll
-      for (int qy = 0; qy < 2; ++qy)
-#pragma unroll
-        for (int qx = 0; qx < 2; ++qx) {
-          const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
-          const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
-          const real Tq4 = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
-          const real q = surface_flux(P, Tq4) * w2;
-          c00[i] += px0 * py0 * q;
-          c10[i] += px1 * py0 * q;
-          c01[i] += px0 * py1 * q;
-          c11[i] += px1 * py1 * q;
-        }
-    }
-  }
-  // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
-#pragma unroll
-  for (int r = 0; r < BYT; ++r) surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
-  return out;
 }
 
 // One CTA of the separable step: x-tile bx, strip group by, z-chunk bz of a

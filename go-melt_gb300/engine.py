@@ -116,6 +116,55 @@ class CoupleGeom:
         self.partials = int(N.lib().gm_couple_partials_size(C.byref(g)))
 
 
+def step_dts(rows, N2):
+    """dt of the Level-1 step and of each of the N2 Level-2 steps of a chunk of
+    toolpath rows: sums of the rows' dt in row order (the order the device
+    toolpath generator, gm_toolpath_rows, sums them in)."""
+    dt = [float(v) for v in np.asarray(rows, dtype=np.float64)[:, 5]]
+    per = len(dt) // N2
+    out = [0.0] * (N2 + 1)
+    for i, v in enumerate(dt):
+        out[0] += v
+        out[1 + i // per] += v
+    return np.asarray(out, dtype=np.float64)
+
+
+class DeviceToolpath:
+    """Toolpath rows generated on the device (gm_toolpath_rows): the run table
+    of createPath.toolpath_runs is uploaded once; each ``next`` call expands
+    the next chunk into device rows and step dts, with the position and the
+    elapsed time accumulated in FP64 in a device-resident state."""
+
+    def __init__(self, runs, device, stream=None):
+        import createPath
+
+        runs = np.ascontiguousarray(np.asarray(runs, dtype=np.float64).reshape(-1, 11))
+        self.nruns = runs.shape[0]
+        self.total = createPath.run_rows(runs)
+        self.dev = torch.device(device)
+        self.stream = stream
+        self.runs = torch.as_tensor(runs.reshape(-1), device=self.dev)
+        self.state = torch.zeros(C.sizeof(N.gm_toolpath_state) // 8, dtype=torch.int64, device=self.dev)
+        self.emitted = 0
+
+    def next(self, nrows, ngroups, rows_out, dts_out):
+        """Expand rows [emitted, emitted + nrows) into rows_out (nrows x 7
+        float64) and their dts (ngroups + 1 float64) on the stream."""
+        if rows_out.dtype != torch.float64 or dts_out.dtype != torch.float64:
+            raise N.GomeltError("toolpath rows and dts are float64")
+        if rows_out.numel() < 7 * nrows or dts_out.numel() < ngroups + 1:
+            raise N.GomeltError("toolpath output buffers too small")
+        N.call("gm_toolpath_rows", self.runs.data_ptr(), self.nruns, self.state.data_ptr(), int(nrows), int(ngroups),
+               kern.ptr(rows_out), kern.ptr(dts_out), kern.stream_ptr(self.stream))
+        self.emitted += int(nrows)
+
+    def state_host(self):
+        """(run, k, rows emitted, x, y, elapsed time) of the device state."""
+        raw = self.state.cpu().numpy()
+        f = raw.view(np.float64)
+        return int(raw[0]), int(raw[1]), int(raw[2]), float(f[3]), float(f[4]), float(f[5])
+
+
 class MovePlan:
     """Host half of one window move (see Engine.plan_move)."""
 
@@ -148,6 +197,8 @@ class Engine:
         self._pending = None  # MovePlan made by plan_move and not yet applied
         self.use_graph = False  # run gm_subcycle as one CUDA graph per call
         self.use_pdl = True  # level steps as programmatic dependent launches
+        self.use_persist = True  # a Level-2 step's Level-3 steps as one persistent launch, where the window allows
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)  # GM_PERSIST_* bits of the device kernels
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
         self.tmp = None
@@ -494,27 +545,34 @@ class Engine:
     # ------------------------------------------------------------------
     # subcycleGOMELT (:3224-3632)
     # ------------------------------------------------------------------
-    def subcycle(self, laser_rows, history=False, rows_device=None):
+    def subcycle(self, laser_rows, history=False, rows_device=None, dts_device=None):
         """One subcycleGOMELT call, issued natively (gm_subcycle).  laser_rows:
         N2*N3 host rows (x, y, z, jump, dwell, dt, P); rows_device: the same
-        rows already on the device.  Returns (L2all, L3all, L3pall) device
-        tensors when ``history``, else None."""
+        rows already on the device; dts_device: also their step dts on the
+        device (step_dts; with rows_device, e.g. from a DeviceToolpath, no
+        host-to-device copy at all; laser_rows may then be None).  Returns
+        (L2all, L3all, L3pall) device tensors when ``history``, else None."""
         g = self.geo
         L1, L2, L3 = g.L[1], g.L[2], g.L[3]
         N2, N3 = self.N2, self.N3
-        rows_h = np.ascontiguousarray(np.asarray(laser_rows, dtype=np.float64))
-        if rows_h.shape != (N2 * N3, 7):
-            raise N.GomeltError(f"expected {N2 * N3} laser rows of 7 values, got {rows_h.shape}")
         if self.tmp is None:
             raise N.GomeltError("active Level-1 region not set (call set_layer first)")
-        dts = np.concatenate([[rows_h[:, 5].sum()], rows_h[:, 5].reshape(N2, N3).sum(axis=1)])
-        need = 8 * (rows_h.size + dts.size) + 2 * TableArena.ALIGN
-        if need > self.rarena.nbytes:
-            self.rarena = TableArena(2 * need, self.dev)
-        self.rarena.begin()
-        rows = rows_device.data_ptr() if rows_device is not None else self.rarena.put(rows_h, np.float64)
-        dtd = self.rarena.put(dts, np.float64)
-        self.rarena.upload(self.stream)
+        if dts_device is not None:
+            if rows_device is None or rows_device.numel() < 7 * N2 * N3 or dts_device.numel() < N2 + 1:
+                raise N.GomeltError("device dts need the chunk's device rows")
+            rows, dtd = kern.ptr(rows_device), kern.ptr(dts_device)
+        else:
+            rows_h = np.ascontiguousarray(np.asarray(laser_rows, dtype=np.float64))
+            if rows_h.shape != (N2 * N3, 7):
+                raise N.GomeltError(f"expected {N2 * N3} laser rows of 7 values, got {rows_h.shape}")
+            dts = step_dts(rows_h, N2)
+            need = 8 * (rows_h.size + dts.size) + 2 * TableArena.ALIGN
+            if need > self.rarena.nbytes:
+                self.rarena = TableArena(2 * need, self.dev)
+            self.rarena.begin()
+            rows = rows_device.data_ptr() if rows_device is not None else self.rarena.put(rows_h, np.float64)
+            dtd = self.rarena.put(dts, np.float64)
+            self.rarena.upload(self.stream)
         out_hist = None
         if history:
             out_hist = (torch.empty(N2, L2.nn, dtype=self.dtype, device=self.dev),
@@ -522,7 +580,7 @@ class Engine:
                         torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev))
         p = self._plan(rows, dtd, out_hist)
         N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
-               kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps)))
+               kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps), persist=bool(p.persist)))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         return out_hist
 
@@ -595,7 +653,35 @@ class Engine:
         p.pdl = 1 if self.use_pdl else 0
         if N.props_constant(self.ps):  # the separable Level-3 step reads tabulated laser factors
             p.src3tab = self._buf("src3tab", N2 * N3 * int(sum(L3.nodes))).data_ptr()
+            if self.use_persist and self.persist_shape() is not None:
+                nf = int(N.lib().gm_level3_persist_flags((C.c_int * 3)(*L3.nodes)))
+                p.persist = 1
+                p.xch3[0], p.xch3[1] = self._buf("xch3a", nn3).data_ptr(), self._buf("xch3b", nn3).data_ptr()
+                p.pflags, p.pflags_cap = self._buf("pflags", nf, torch.int32).data_ptr(), nf
+                p.pstatus = self.status.data_ptr()
         return p
+
+    def persist_shape(self):
+        """Tile shape of the persistent Level-3 kernel on this window ({tiles,
+        x columns, y rows, z segments}), or None if the window has none."""
+        out = (C.c_int * 4)()
+        rc = N.lib().gm_level3_persist_shape(kern.dtype_code(self.T[3]), (C.c_int * 3)(*self.geo.L[3].nodes), out)
+        return list(out) if rc == N.GM_OK else None
+
+    def check_status(self):
+        """Raise GomeltError if a device kernel reported a failure (a bounded
+        wait that ran out, a non-finite or out-of-range Level-3 field); reading
+        the status synchronises with the engine's stream.  The word is cleared."""
+        v = int(self.status.item())
+        if v:
+            with torch.cuda.stream(self.stream or torch.cuda.current_stream()):
+                self.status.zero_()
+            what = []
+            if v & N.GM_PERSIST_TIMEOUT:
+                what.append("a wait between Level-3 tiles ran out")
+            if v & N.GM_PERSIST_BAD_T:
+                what.append("non-finite or out-of-range Level-3 temperature")
+            raise N.GomeltError("device status: " + ", ".join(what or [f"code {v}"]))
 
     # ------------------------------------------------------------------
     # stepGOMELT (:2304-2397) and stepGOMELTDwellTime (:2617-2664)

@@ -102,7 +102,7 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
         name = os.path.join(ckpt_dir, f"Checkpoint{str(Nonmesh['layer_num']).zfill(4)}.pkl")
         with open(name, "rb") as f:
             st = pickle.load(f)
-        restore_state(eng, acc, st)
+        restore_state(eng, acc, st, s1_storage)
         record_inc = st["record_inc"]
         line_len = len(fh.readline())
         fh.seek(st["time_inc"] * line_len)
@@ -181,7 +181,8 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
                 os.makedirs(ckpt_dir, exist_ok=True)
                 name = os.path.join(ckpt_dir, f"Checkpoint{str(Nonmesh['layer_num']).zfill(4)}.pkl")
                 with open(name, "wb") as f:
-                    pickle.dump(snapshot_state(eng, acc, time_inc, record_inc), f, pickle.HIGHEST_PROTOCOL)
+                    pickle.dump(snapshot_state(eng, acc, time_inc, record_inc, s1_storage), f,
+                                pickle.HIGHEST_PROTOCOL)
                 if Nonmesh["layer_num"] == layer_check:
                     fh.close()
                     return Levels
@@ -263,9 +264,12 @@ def save_accum(acc, Nonmesh):
              accum_time=a.double().cpu().numpy())
 
 
-def snapshot_state(eng, acc, time_inc, record_inc):
+def snapshot_state(eng, acc, time_inc, record_inc, s1_storage):
+    """Host copy of everything the reference's checkpoint holds (Levels with
+    its Level-1 S1 layer store, the melt-time records, time and record
+    counters; go_melt.py:390-411)."""
     g = eng.geo
-    st = {"time_inc": time_inc, "record_inc": record_inc,
+    st = {"time_inc": time_inc, "record_inc": record_inc, "s1_storage": s1_storage.cpu(),
           "T": {k: v.cpu() for k, v in eng.T.items()}, "Tp": {k: v.cpu() for k, v in eng.Tp.items()},
           "ph": {k: v.cpu() for k, v in eng.ph.items()}, "L0": eng.L0.cpu(), "accum": acc.accum.cpu(),
           "max_accum": acc.max_accum.cpu(), "s2_prev_lo": eng.s2_prev_lo,
@@ -277,8 +281,9 @@ def snapshot_state(eng, acc, time_inc, record_inc):
     return st
 
 
-def restore_state(eng, acc, st):
+def restore_state(eng, acc, st, s1_storage):
     g = eng.geo
+    s1_storage.copy_(st["s1_storage"].to(eng.dev))
     for k, v in st["T"].items():
         eng.T[k].copy_(v.to(eng.dev))
     for k, v in st["Tp"].items():

@@ -383,10 +383,13 @@ int gm_couple(const gm_couple_args* a, const gm_props* p, void* stream);
  * live in a library-owned __device__ array of GM_COUPLE_NOALLOC_SCRATCH_BYTES
  * (4 MiB: 1 Mi float or 512 Ki double partials), which every GPU that loads
  * the library keeps until exit.  Arguments are those of gm_couple; `partials`
- * and `partials_cap` are ignored.  Returns GM_ERR_TOO_LARGE when the coupling
- * needs more partials than the array holds (gm_couple_partials_size * element
- * size > 4 MiB).  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * and `partials_cap` are ignored.  The path is chosen as gm_couple chooses it
+ * with a 4 MiB scratch: with method 0 and constant properties the separable
+ * contraction when its partials fit, else the element reduction.  Returns
+ * GM_ERR_TOO_LARGE when the path taken needs more partials than the array
+ * holds.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture (a
+ * first call on a stream that is being captured returns GM_ERR_ARG).
  * The array is shared by all calls and keeps the last call's contents; every
  * call overwrites all partials it reads, so nothing needs clearing, but calls
  * that overlap on the GPU (different streams, no ordering) race on it. */
@@ -487,10 +490,105 @@ typedef struct gm_subcycle_plan {
                                 that one drains and wait for it before touching any field) */
   void* src3tab;             /* optional work (N2*N3 * (nx+ny+nz) of Level 3): the Level-3 laser factors
                                 of the call, tabulated at its start */
+  int persist;               /* 1: the N3 Level-3 steps of each Level-2 step run as one gm_level3_persist
+                                launch (constant-property materials with src3tab and the work below; a
+                                window without a persistent shape falls back to one launch a step) */
+  void* xch3[2];             /* work of persist: two nn3 fields (halo exchange) */
+  unsigned* pflags;          /* work of persist: gm_level3_persist_flags(L3 nodes) counters, zeroed by the call */
+  long long pflags_cap;
+  int* pstatus;              /* device word of persist: GM_PERSIST_* bits are or-ed into it (never cleared
+                                by the call) */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
 int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream);
+
+/* ------------------------------------------------------------------------
+ * The N3 Level-3 fine steps of one Level-2 step in ONE launch (persistent
+ * kernel).  Replaces the inner lax.scan of subcycleGOMELT
+ * (go_melt/computeFunctions.py:3404-3430 predictor, :3586-3622 corrector):
+ * per step computeStateProperties, computeSourcesL3, computeConvRadBC,
+ * computeSolutions_L3 with the blended Level-2 ring, the T >= T_amb clamp and,
+ * with accumulators, the melt-time update (:3568-3578) -- the same arithmetic
+ * as gm_level_step's separable kernel with bc_mode 3 and a laser factor table,
+ * bit for bit.  Constant-property materials, every element plane active.
+ * Step s blends the ring as alpha = (s+1)/nsub, beta = 1 - alpha.
+ *
+ * One cooperative launch keeps the window in shared memory (a tile of node
+ * columns per CTA) and exchanges tile edges through `xbuf` between steps,
+ * synchronised by per-tile counters in `flags`: every flag must equal `base`
+ * when the launch starts and equals base + nsteps after it completes (zero
+ * the flags once, then pass base += nsteps from launch to launch).  Waits are
+ * bounded (about one second): a timeout sets GM_PERSIST_TIMEOUT in *status
+ * and the launch ends with T_out incomplete (zero the flags again before the
+ * next launch).  A final field with a non-finite value or a value above 1e5 K
+ * sets GM_PERSIST_BAD_T.  GM_ERR_UNSUPPORTED when the window's tiles cannot
+ * all be resident at once (the caller then issues gm_level_step per step).
+ * No counterpart in the reference.
+ * ------------------------------------------------------------------------ */
+#define GM_PERSIST_TIMEOUT 1
+#define GM_PERSIST_BAD_T 2
+
+typedef struct gm_persist_args {
+  int dtype;
+  int nodes[3];
+  double h[3];
+  int nsteps;                  /* fine steps of this launch */
+  int nsub;                    /* ring blend denominator (N3) */
+  const void* T_in;            /* window at the first step's start */
+  void* T_out;                 /* window after the last step (may be xbuf[nsteps % 2], not T_in) */
+  const uint8_t* ph_in;
+  uint8_t* ph_out;
+  long long substrate;         /* nodes with id < substrate are always S1 */
+  const void* ring_new;        /* coarse field at the step's end, prolongated onto the ring nodes */
+  const void* ring_old;        /* coarse field at the step's start, likewise (gm_ring_prolong) */
+  const void* src_tab;         /* nsteps rows of laser factors (gm_fine_source_tables) */
+  const double* rows;          /* nsteps toolpath rows (x, y, z, jump, dwell, dt, P) */
+  void* accum;                 /* optional melt-time accumulators (both or neither) */
+  void* max_accum;
+  void* xbuf[2];               /* work: two full-size fields, neither aliasing T_in */
+  unsigned* flags;             /* work: per-tile step counters (gm_level3_persist_flags) */
+  long long flags_cap;
+  unsigned base;               /* value of every flag when the launch starts */
+  int* status;                 /* device word: GM_PERSIST_* bits are or-ed into it */
+  int hold;                    /* 0 in every ordinary call.  t > 0: tile t-1 withholds its step counters
+                                  (failure injection for tests: its neighbours' waits run out) */
+} gm_persist_args;
+
+/* Number of flags (tiles) of a window, or -1 if the window has no persistent
+ * shape; the flag array of a call must hold at least this many. */
+long long gm_level3_persist_flags(const int nodes[3]);
+/* Tile shape of a window: out = {tiles, x columns a tile, y rows a tile, z
+ * segments a tile row}; GM_ERR_UNSUPPORTED if the window has none. */
+int gm_level3_persist_shape(int dtype, const int nodes[3], int out[4]);
+int gm_level3_persist(const gm_persist_args* a, const gm_props* p, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Toolpath rows on the device, positions and time accumulated in FP64.
+ * Replaces the text round trip of the reference (createPath.py:126-160
+ * writes x += vx*dt per fine step as %.8e text; go_melt.py:140-160 reads N2*N3
+ * lines a chunk).  `runs` (device, nruns x 11 doubles: kind, count, x, y, z,
+ * jump, ux, uy, dt, P, short; kind 0 = move: position set to (x, y), count
+ * rows after x += ux*dt, y += uy*dt, then one row after += u*short if short
+ * > 0; kind 1 = hold: count rows at (x, y), dwell flag 0, power 0) is built
+ * by createPath.toolpath_runs.  Each call writes the next `nrows` rows
+ * (x, y, z, jump, dwell, dt, P) and dts = {sum of their dt, then the sum of
+ * each of `ngroups` equal groups}, sums in row order; rows past the end of the
+ * table are zero.  Products are rounded before the sums (no fused
+ * multiply-add), so the rows equal the host's float64 ones bit for bit.
+ * *state (device, zeroed before the first call) carries the cursor, the
+ * position and the elapsed time t between calls.  No counterpart in the
+ * reference (its accumulation is host Python).
+ * ------------------------------------------------------------------------ */
+typedef struct gm_toolpath_state {
+  long long run, k;  /* run index and rows emitted of it */
+  long long row;     /* rows emitted in all */
+  double x, y;       /* position of the current move */
+  double t;          /* elapsed time: sum of the emitted rows' dt */
+} gm_toolpath_state;
+
+int gm_toolpath_rows(const double* runs, int nruns, gm_toolpath_state* state, int nrows, int ngroups, double* rows,
+                     double* dts, void* stream);
 
 /* Library identification: returns a static string; never fails. */
 const char* gm_version(void);

@@ -1,0 +1,240 @@
+"""Multilevel parity at the benchmarked sizes: the GPU engine against the
+oracle (pinned to the reference by tests/test_oracle_golden.py) on the full
+single-track workload and on the real part-scale Level-3 window.
+
+* single track (L1 50x50x10 @ 100 um, L2 50x50x10 @ 20 um, L3 80x80x20 @
+  5 um, N2 = N3 = 10): two moveEverything + subcycleGOMELT calls along the
+  track's toolpath (200 toolpath rows, 400 Level-3 solves);
+* the minimum slice: 100 moving-source Level-3 steps on the single-track
+  Level-3 window (phase, source, surface flux, solve, ring, clamp);
+* the part-scale Level-3 window (160x160x40 elements @ 5 um) inside the
+  part-scale Level 2 (100x100x15 @ 20 um) and a Level 1 cropped to 4x4x1 mm
+  @ 100 um around it (the oracle's element tables of the full 20x20x5 mm
+  Level 1 would not finish in a test): one move + subcycle with N2 = 2, N3 = 3.
+
+The GPU runs with the launch shapes Engine.autotune measures (as the bench
+does) and each subcycle call as one CUDA graph.  Bars: FP64 1e-10 and FP32
+1e-4 relative max temperature per level (the benchmark spec's FP32 bar); T' to
+the same bars relative to the peak temperature; phases and melt time exactly
+(FP64) or on all but a few threshold-straddling nodes (FP32: a node within
+rounding of T_liquidus may flip).
+"""
+
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+import gomelt_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = [(torch.float64, 1e-10), (torch.float32, 1e-4)]
+
+
+def _rows(cfg):
+    import createPath
+    import levels
+
+    P = levels.setup_properties(cfg["properties"])
+    nm = levels.setup_nonmesh(cfg["nonmesh"])
+    return np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)
+
+
+def _single_track():
+    import workloads
+
+    cfg = workloads.single_track()
+    return cfg, _rows(cfg)
+
+
+def _part_scale_window():
+    import createPath
+    import workloads
+
+    cfg = workloads.part_scale_raster()
+    cfg["Level1"] = {"elements": [40, 40, 10], "bounds": {"x": [8.0, 12.0], "y": [8.0, 12.0], "z": [-1.0, 0.0]},
+                     "conditions": cfg["Level1"]["conditions"]}
+    r = cfg["raster"]
+    cfg["gcode"] = createPath.serpentine_gcode(r["x0"] + 1.5, r["y0"] + 1.5, 1.0, r["hatch"], 2)
+    return cfg, _rows(cfg)
+
+
+def _ratios(L, P):
+    r12 = [int(np.round(L[1]["h"][i] / L[2]["h"][i])) for i in range(2)] + [
+        int(np.round(P["layer_height"] / L[2]["h"][2]))]
+    r23 = [int(np.round(L[2]["h"][i] / L[3]["h"][i])) for i in range(3)]
+    return r12, r23
+
+
+_ORACLE = {}
+
+
+def oracle_run(name, cfg, rows, N2, N3, calls):
+    """moveEverything + subcycleGOMELT `calls` times on consecutive chunks of
+    N2*N3 rows (cached per workload)."""
+    if name in _ORACLE:
+        return _ORACLE[name]
+    P = O.SetupProperties(cfg["properties"])
+    L = O.SetupLevels(copy.deepcopy(cfg), P)
+    r12, r23 = _ratios(L, P)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    mv = [0, 0, 0]
+    macc = acc = None
+    n23 = N2 * N3
+    sc = (N2, N3, n23, float(N2), float(N3), float(n23))
+    for c in range(calls):
+        ch = rows[c * n23:(c + 1) * n23]
+        L, shapes, interp, mv = O.moveEverything(ch[0], vstart, L, mv, [None, None], r12, r23, P["layer_height"])
+        ne_nn = O.getStaticNodesAndElements(L)
+        tmp = O.calcStaticTmpNodesAndElements(L, ch[0])
+        sub = O.getSubstrateNodes(L)
+        if macc is None:
+            macc, acc = np.zeros(ne_nn[4]), np.zeros(ne_nn[4])
+        L, _, _, _, macc, acc = O.subcycleGOMELT(L, ne_nn, shapes, sub, interp, tmp, ch, P, ch[:, 6], sc, macc, acc)
+    out = {"L": L, "macc": np.asarray(macc), "acc": np.asarray(acc)}
+    _ORACLE[name] = out
+    return out
+
+
+def gpu_run(cfg, rows, N2, N3, calls, dtype):
+    from engine import Engine
+    from levels import setup_properties
+
+    P = setup_properties(cfg["properties"])
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        eng = Engine(copy.deepcopy(cfg), P, N2, N3, dtype=dtype, stream=stream)
+        n23 = N2 * N3
+        vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+        eng.set_layer(rows[0])
+        tuned = None
+        for c in range(calls):
+            ch = rows[c * n23:(c + 1) * n23]
+            eng.move(ch[0], vstart)
+            if tuned is None:
+                tuned = eng.autotune(ch[0])  # launch shapes as the bench measures them
+                eng.use_graph = True
+            eng.subcycle(ch)
+        stream.synchronize()
+    return eng, tuned
+
+
+def compare(eng, ref, dtype, tol):
+    L = ref["L"]
+    out = eng.fields_numpy()
+    Tscale = max(float(np.max(np.asarray(L[lev]["T0"]))) for lev in (1, 2, 3))
+    assert Tscale > 2000.0  # the laser has heated the windows
+    errs = {}
+    for lev in (1, 2, 3):
+        r = np.asarray(L[lev]["T0"], dtype=float)
+        errs[f"T{lev}"] = float(np.max(np.abs(out[lev]["T0"] - r)) / np.max(np.abs(r)))
+    for lev in (2, 3):
+        r = np.asarray(L[lev]["Tprime0"], dtype=float)
+        errs[f"Tp{lev}"] = float(np.max(np.abs(out[lev]["Tprime0"] - r)) / Tscale)
+    for k, v in errs.items():
+        assert v < tol, (k, v, errs)
+    exact = dtype == torch.float64
+    for lev in (1, 2, 3):
+        got, want = out[lev]["S1"] > 0.5, np.asarray(L[lev]["S1"]) > 0.499
+        nbad = int(np.count_nonzero(got != want))
+        assert nbad == 0 if exact else nbad <= max(8, got.size // 10000), (lev, nbad)
+    got, want = out[3]["S2"], np.asarray(L[3]["S2"]).astype(bool)
+    nbad = int(np.count_nonzero(got != want))
+    assert nbad == 0 if exact else nbad <= max(8, got.size // 10000), nbad
+    s1_0 = out[0]["S1"] > 0.5
+    nbad = int(np.count_nonzero(s1_0 != (np.asarray(L[0]["S1"]) > 0.499)))
+    assert nbad == 0 if exact else nbad <= max(8, s1_0.size // 100000), nbad
+    for name, key in (("acc", eng.acc3), ("macc", eng.macc3)):
+        got = key.double().cpu().numpy()
+        want = ref[name]
+        if exact:
+            np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-15)
+        else:  # all but threshold-straddling nodes agree to FP32 rounding
+            bad = np.abs(got - want) > 1e-4 * max(float(np.max(want)), 1e-12) + 1e-12
+            assert int(np.count_nonzero(bad)) <= max(8, got.size // 10000), (name, int(np.count_nonzero(bad)))
+    return errs
+
+
+@pytest.mark.parametrize("dtype,tol", TOL)
+def test_single_track_two_subcycle_calls(dtype, tol):
+    cfg, rows = _single_track()
+    ref = oracle_run("single_track", cfg, rows, 10, 10, 2)
+    eng, tuned = gpu_run(cfg, rows, 10, 10, 2, dtype)
+    errs = compare(eng, ref, dtype, tol)
+    print(f"single track, {dtype}: {errs}; shapes {tuned}")
+
+
+@pytest.mark.parametrize("dtype,tol", TOL)
+def test_part_scale_level3_window(dtype, tol):
+    cfg, rows = _part_scale_window()
+    ref = oracle_run("part_scale", cfg, rows, 2, 3, 1)
+    eng, tuned = gpu_run(cfg, rows, 2, 3, 1, dtype)
+    assert tuple(eng.geo.L[3].nodes) == (161, 161, 41)
+    errs = compare(eng, ref, dtype, tol)
+    print(f"part-scale window, {dtype}: {errs}; shapes {tuned}")
+
+
+_SLICE = {}
+
+
+def _slice_oracle(cfg, rows, nsteps):
+    """nsteps Level-3 steps of the oracle on the moved single-track window:
+    phase/properties, fine source, surface flux, solve, Dirichlet ring from the
+    (fixed) Level-2 field, clamp."""
+    if "ref" in _SLICE:
+        return _SLICE["ref"]
+    P = O.SetupProperties(cfg["properties"])
+    L = O.SetupLevels(copy.deepcopy(cfg), P)
+    r12, r23 = _ratios(L, P)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    L, _, interp, _ = O.moveEverything(rows[0], vstart, L, [0, 0, 0], [None, None], r12, r23, P["layer_height"])
+    ne_nn = O.getStaticNodesAndElements(L)
+    sub = O.getSubstrateNodes(L)
+    T = np.asarray(L[3]["T0"], dtype=float)
+    S1 = np.asarray(L[3]["S1"], dtype=float)
+    for r in rows[:nsteps]:
+        S1n, S2n, k, rc = O.computeStateProperties(T, S1, P, sub[3])
+        F = O.computeSourcesL3(L[3], r, ne_nn, P, r[6])
+        F = O.computeConvRadBC(L[3], T, ne_nn[1], ne_nn[4], P, F)
+        T = np.maximum(P["T_amb"], O.computeSolutions_L3(L[2]["T0"], interp[1], L, ne_nn, T, F, k, rc, r[5]))
+        S1 = S1n
+    _SLICE["ref"] = (T, S1, S2n)
+    return _SLICE["ref"]
+
+
+@pytest.mark.parametrize("dtype,tol", TOL)
+def test_min_slice_100_level3_steps(dtype, tol):
+    """100 moving-source Level-3 steps on the single-track Level-3 window."""
+    from engine import Engine
+    from levels import setup_properties
+
+    cfg, rows = _single_track()
+    nsteps = 100
+    T_ref, S1_ref, S2_ref = _slice_oracle(cfg, rows, nsteps)
+    P = setup_properties(cfg["properties"])
+    eng = Engine(copy.deepcopy(cfg), P, 10, 10, dtype=dtype)
+    vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
+    eng.set_layer(rows[0])
+    eng.move(rows[0], vstart)
+    eng.autotune(rows[0])
+    ring = eng._ring(3, eng.T[2], eng.T[2])
+    L3 = eng.geo.L[3]
+    Ta, Tb = eng.T[3].clone(), torch.empty_like(eng.T[3])
+    pa, pb = eng.ph[3].clone(), torch.empty_like(eng.ph[3])
+    rows_d = torch.as_tensor(rows[:nsteps], device="cuda")
+    for i in range(nsteps):
+        r = rows_d[i]
+        eng._level(3, Ta, Tb, r[5:6], pa, pb, laser=r, ring=ring, alpha=1.0)
+        Ta, Tb, pa, pb = Tb, Ta, pb, pa
+    torch.cuda.synchronize()
+    got = Ta.double().cpu().numpy()
+    err = float(np.max(np.abs(got - T_ref)) / np.max(np.abs(T_ref)))
+    assert np.max(T_ref) > 2000.0
+    assert err < tol, err
+    ph = pa.cpu().numpy()
+    exact = dtype == torch.float64
+    nbad = int(np.count_nonzero(((ph & 1) != 0) != (np.asarray(S1_ref) > 0.499)))
+    assert nbad == 0 if exact else nbad <= max(8, L3.nn // 10000), nbad
+    print(f"min slice, {dtype}: {nsteps} Level-3 steps, max rel err {err:.3e}")

@@ -29,7 +29,10 @@ CFG_WIDE = dict(CFG, Level3={"elements": [299, 12, 6], "bounds": {"x": [0.85, 1.
                                                                    "z": [-0.03, 0]}})
 
 # (kernel, rows, warps a CTA, zchunk); kernel None = the library's own choice
-SHAPES = [(None, 0, 0, 0), (0, 0, 0, 5), (1, 4, 1, 2), (1, 2, 2, 3), (1, 4, 4, 5), (1, 2, 8, 32)]
+# (1, 4, 4, 6) and (1, 2, 2, 9) are the Level-3 and Level-1 shapes the autotuner chose on the part-scale
+# workload; (1, 1, 2, 7) a one-row strip with an odd z-chunk
+SHAPES = [(None, 0, 0, 0), (0, 0, 0, 5), (1, 4, 1, 2), (1, 2, 2, 3), (1, 4, 4, 5), (1, 2, 8, 32), (1, 4, 4, 6),
+          (1, 2, 2, 9), (1, 1, 2, 7)]
 
 
 def setup(cfg, seed):
