@@ -60,6 +60,9 @@ def parse_args():
                          "or 'tiles,TILE_X,ZCHUNK'")
     ap.add_argument("--kernel-only", action="store_true",
                     help="run only the Level-3 level-step kernel --steps times (for profiling)")
+    ap.add_argument("--persist-steps", type=int, default=0, help="--persist-only: fine steps a launch (default N3)")
+    ap.add_argument("--persist-only", action="store_true",
+                    help="--kernel-only: the persistent Level-3 kernel instead of the one-step kernel")
     ap.add_argument("--l3-accum", action="store_true",
                     help="--kernel-only: the corrector's Level-3 step (with the melt-time update)")
     ap.add_argument("--precision", action="store_true",
@@ -71,14 +74,17 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
-    ap.add_argument("--no-persist", action="store_true",
-                    help="one launch per Level-3 fine step instead of the persistent Level-3 kernel")
+    ap.add_argument("--persist", action="store_true",
+                    help="the persistent Level-3 kernel (N3 fine steps a launch) instead of one launch a fine step")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the library's untuned launch shapes (for ncu launch lists: timings under ncu would "
                          "steer the autotuner)")
     ap.add_argument("--unet-only", action="store_true",
                     help="surrogate kernels alone: forward passes on the part-scale grid and training steps "
                          "(for profiling)")
+    ap.add_argument("--layers", type=int, default=0,
+                    help="the part-scale raster over this many layers through the JSON driver (layer changes, "
+                         "Level-0 store, checkpoints)")
     ap.add_argument("--batched", action="store_true",
                     help="batched single-track instances: per-instance vs batched level launches (CUDA graphs)")
     return ap.parse_args()
@@ -320,7 +326,7 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
-def persist_launcher(eng, chunk_rows, accum=False):
+def persist_launcher(eng, chunk_rows, accum=False, nsteps=None):
     """The persistent Level-3 kernel as the subcycle launches it on the
     engine's window (one launch = the N3 fine steps of one Level-2 step, ring
     from the precomputed prolongation arrays, laser factors from the step's
@@ -334,7 +340,7 @@ def persist_launcher(eng, chunk_rows, accum=False):
     import kern
 
     L3 = eng.geo.L[3]
-    N3 = eng.N3
+    N3 = nsteps or eng.N3
     nn = L3.nn
     dev = eng.dev
     rows_d = torch.as_tensor(chunk_rows[:N3], device=dev).contiguous()
@@ -410,7 +416,7 @@ def run_ours(args):
         eng.move(rows[0], vstart)
         tuned = {} if args.no_autotune else eng.autotune(rows[0])  # launch shapes, measured (set-up, untimed)
         eng.use_graph = not args.no_graph  # each subcycle call as one CUDA graph
-        eng.use_persist = not args.no_persist
+        eng.use_persist = args.persist
         persist = eng.use_persist and eng.persist_shape() is not None
         # toolpath rows generated on the device (FP64 accumulation) from the run table
         tp = engine.DeviceToolpath(runs, dev, stream)
@@ -541,7 +547,7 @@ def run_ours(args):
         del graph
         # persistent kernel: N3 fine steps a launch, launches back to back
         kp_ms = None
-        if persist:
+        if eng.persist_shape() is not None:
             launch, nper = persist_launcher(eng, last_chunk)
             for b in range(3):
                 launch(b * nper)
@@ -595,7 +601,10 @@ def run_ours(args):
                      "alg_bytes": alg_bytes, "alg_bytes_rule": "10 B per node per fine step (T read + write, "
                      "phase byte read + write)", "peak_kind": peak_kind,
                      "one_step_kernel": {"kernel": l3_kernel_name(tuned.get(3)), "ms": k1_ms,
-                                         "frac": 10.0 * L3.nn / (k1_ms * 1e-3) / 1e9 / peak}},
+                                         "frac": 10.0 * L3.nn / (k1_ms * 1e-3) / 1e9 / peak},
+                     "persistent_kernel": None if kp_ms is None else {
+                         "kernel": f"level3_persist_kernel ({N3} fine steps a launch)", "ms_per_launch": kp_ms,
+                         "ms_per_fine_step": kp_ms / N3, "frac": 10.0 * L3.nn * N3 / (kp_ms * 1e-3) / 1e9 / peak}},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
         "level3_persistent": persist,
@@ -800,6 +809,68 @@ def run_surrogate(args):
     print(json.dumps(line), flush=True)
 
 
+def run_layers(args):
+    """The part-scale raster over --layers 50 um layers through the JSON driver
+    (go_melt.py): G-code -> toolpath file, chunks of N2*N3 rows as subcycled
+    steps, single steps and dwell steps around each layer change, the
+    Level-1 re-sampling and Level-0 shift of a new layer, checkpoints and the
+    per-layer melt-time records.  Reports the driver's wall time for the whole
+    path (set-up, toolpath generation and file output included) and the
+    Level-0 store size."""
+    import contextlib
+    import io
+    import shutil
+
+    import numpy as np
+    import torch
+
+    import createPath
+    import go_melt
+    import levels
+    import workloads
+
+    cfg = workloads.part_scale_layers(layers=args.layers)
+    P = levels.setup_properties(cfg["properties"])
+    nm = levels.setup_nonmesh(cfg["nonmesh"])
+    rows = np.asarray(createPath.toolpath(nm, P, cfg["gcode"]), dtype=np.float64)
+    work = tempfile.mkdtemp(prefix="gm_layers_")
+    try:
+        free_gb = shutil.disk_usage(work).free / 1e9
+        with open(os.path.join(work, "path.gcode"), "w") as f:
+            f.write(cfg.pop("gcode"))
+        cfg.pop("raster")
+        cfg["nonmesh"].update(gcode=os.path.join(work, "path.gcode"), save_path=os.path.join(work, "out") + "/",
+                              toolpath=os.path.join(work, "toolpath.txt"))
+        os.makedirs(cfg["nonmesh"]["save_path"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        log = io.StringIO()
+        with contextlib.redirect_stdout(log):
+            Levels = go_melt.go_melt(cfg, dtype=torch.float32 if args.dtype == "f32" else torch.float64)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        eng = Levels.engine
+        g = eng.geo
+        outs = sorted(os.listdir(cfg["nonmesh"]["save_path"]))
+        ck = sorted(os.listdir(os.path.join(cfg["nonmesh"]["save_path"], "checkpoint")))
+        fin = np.load(os.path.join(cfg["nonmesh"]["save_path"], "FinalTemperatureFields.npz"))
+        line = {
+            "mode": "layers", "workload": f"part-scale raster, {args.layers} layers of 50 um, L1 200x200x53 @ 100 um "
+                                          f"(to z = 0.3 mm), L2 100x100x15 @ 20 um, L3 160x160x40 @ 5 um",
+            "dtype": args.dtype, "toolpath_rows": int(len(rows)), "scan_mm": scan_mm(rows),
+            "driver_wall_s": wall, "scan_mm_per_wall_s": scan_mm(rows) / wall,
+            "checkpoints": ck, "outputs": [o for o in outs if o != "checkpoint"],
+            "level0": {"nodes": list(g.L0_nodes), "store_bytes": eng.L0.numel() * 4,
+                       "byte_per_node_bytes": int(g.L0_nn), "s1_nodes": int(eng.l0_s1().sum())},
+            "final_T_max_K": {k: float(fin[k].max()) for k in ("L1T", "L2T", "L3T")},
+            "disk_free_gb_at_start": free_gb,
+            "driver_log_tail": log.getvalue().strip().splitlines()[-2:],
+        }
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    print(json.dumps(line), flush=True)
+
+
 def run_batched(args):
     """The 64 batched single-track instances after two plain steps each: one
     fine step of every instance's Level 3 (uniform 81 x 81 x 21 windows) and
@@ -898,7 +969,61 @@ def run_batched(args):
         res["nodes"] = nodes
         res["shapes"] = "uniform 81x81x21" if lev == 3 else "uneven 31..121 x 31..121 x 9..21"
         out[f"L{lev}"] = res
+    out["subcycle"] = batched_subcycles(engs, inst, stream, K=max(args.steps // 4, 3))
     print(json.dumps(out), flush=True)
+
+
+def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
+    """Whole steps (moveEverything + subcycleGOMELT) of every instance: the
+    subcycle calls issued one instance after another (each as its own CUDA
+    graph) or as ONE graph of parallel branches (gm_subcycle_batched).  Scan
+    throughput over all instances, GPU time of the subcycles alone and wall
+    time per step (host planning of the 64 window moves included)."""
+    import numpy as np
+    import torch
+
+    import engine
+    import surrogate_run as SR
+
+    rows = [SR._instance_rows(cfg)[2] for cfg in inst]
+    vst = [np.asarray(cfg["properties"]["laser_center"], dtype=float) for cfg in inst]
+    mm = lambda k: sum(scan_mm(r[k * 100:(k + 1) * 100]) for r in rows)  # noqa: E731
+    nsteps = lambda e: 2 * e.N2 * e.N3 * e.geo.L[3].nn + 2 * e.N2 * e.geo.L[2].nn + 2 * e.geo.L[1].nn  # noqa: E731
+    node_steps = sum(nsteps(e) for e in engs)
+    for e in engs:
+        e.use_persist = False
+        e.use_graph = True
+    out = {"instances": len(engs), "steps": K, "node_steps_per_step": node_steps}
+    k = first_chunk
+    for mode in ("per_instance", "batched", "per_instance", "batched"):  # the first pair warms up
+        t_gpu, t_wall, dist = 0.0, 0.0, 0.0
+        for _ in range(K):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                for e, r, v in zip(engs, rows, vst):
+                    e.move(r[k * 100], v)
+                s, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                if mode == "batched":
+                    engine.subcycle_batched(engs, [r[k * 100:(k + 1) * 100] for r in rows])
+                else:
+                    for e, r in zip(engs, rows):
+                        e.subcycle(r[k * 100:(k + 1) * 100])
+                e_.record(stream)
+            torch.cuda.synchronize()
+            t_wall += time.perf_counter() - t0
+            t_gpu += s.elapsed_time(e_) * 1e-3
+            dist += mm(k)
+            k += 1
+        out[mode] = {"subcycle_gpu_ms_per_step": 1e3 * t_gpu / K, "wall_ms_per_step": 1e3 * t_wall / K,
+                     "scan_mm_per_s_wall": dist / t_wall, "scan_mm_per_s_subcycle_gpu": dist / t_gpu,
+                     "gnode_steps_per_s_subcycle_gpu": node_steps * K / t_gpu / 1e9}
+    out["speedup_subcycle_gpu"] = (out["per_instance"]["subcycle_gpu_ms_per_step"] /
+                                   out["batched"]["subcycle_gpu_ms_per_step"])
+    for e in engs:
+        e.check_status()
+    return out
 
 
 def run_unet_only(args):
@@ -960,6 +1085,24 @@ def run_kernel_only(args):
     for k in range(args.warmup):
         eng.move(rows[k * n23], vstart)
         eng.subcycle(rows[k * n23:(k + 1) * n23])
+    if args.persist_only:  # the persistent Level-3 kernel: --steps launches of N3 fine steps
+        eng.autotune(rows[0])
+        launch, nper = persist_launcher(eng, rows[(args.warmup - 1) * n23:args.warmup * n23], accum=args.l3_accum,
+                                        nsteps=args.persist_steps or None)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(eng.stream)
+        for i in range(args.steps):
+            launch(i * nper)
+        e1.record(eng.stream)
+        torch.cuda.synchronize()
+        st = int(launch.keep["status"].item())
+        print(json.dumps({"kernel_only": "level3_persist_kernel", "launches": args.steps, "fine_steps": nper,
+                          "nodes": eng.geo.L[3].nn, "shape": eng.persist_shape(), "status": st,
+                          "us_per_launch": 1000 * e0.elapsed_time(e1) / args.steps}))
+        if st:
+            raise SystemExit("persistent kernel status %d" % st)
+        return
     if args.l3_shape:  # e.g. "separable,4,2,6" (rows, thread rows, z-chunk) or "tiles,32,14"
         f = args.l3_shape.split(",")
         shape = (dict(kernel=1, rows=int(f[1]), tile_y=int(f[2]), zchunk=int(f[3])) if f[0] == "separable"
@@ -1002,6 +1145,8 @@ def main():
         run_precision(args)
     elif args.surrogate:
         run_surrogate(args)
+    elif args.layers > 0:
+        run_layers(args)
     elif args.batched:
         run_batched(args)
     elif args.impl == "reference":

@@ -132,7 +132,7 @@ class gm_restrict_s1_args(C.Structure):
 
 class gm_l0_args(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("idx", C.POINTER(C.c_int) * 3), ("l0_nx", C.c_longlong),
-                ("l0_ny", C.c_longlong), ("l0_s1", C.POINTER(C.c_uint8)), ("ph", C.POINTER(C.c_uint8)),
+                ("l0_ny", C.c_longlong), ("l0_bits", vp), ("ph", C.POINTER(C.c_uint8)),
                 ("prev_ph", C.POINTER(C.c_uint8)), ("prev_lo", C.c_int * 3), ("prev_n", C.c_int * 3)]
 
 
@@ -178,7 +178,7 @@ class gm_subcycle_plan(C.Structure):
         ("bc12", gm_map3), ("bc23", gm_map3), ("r32", gm_map3), ("r21", gm_map3), ("r32_idx", _P_INT * 3),
         ("r21_idx", _P_INT * 3), ("c32", gm_couple_geom), ("c31", gm_couple_geom), ("c21", gm_couple_geom),
         ("xq32", _P_DBL * 3), ("xq31", _P_DBL * 3), ("rhs1_lo", C.c_int * 3), ("rhs1_n", C.c_int * 3),
-        ("rhs2_lo", C.c_int * 3), ("rhs2_n", C.c_int * 3), ("L0", _P_U8), ("L0_nx", C.c_longlong),
+        ("rhs2_lo", C.c_int * 3), ("rhs2_n", C.c_int * 3), ("L0", vp), ("L0_nx", C.c_longlong),
         ("L0_ny", C.c_longlong), ("l0_idx3", _P_INT * 3), ("rows", vp), ("dts", vp), ("T1p", vp), ("T1c", vp),
         ("T2w", vp * 2), ("T3w", vp * 2), ("tp3w", vp * 2), ("Tp2w", vp), ("rhs1", vp), ("rhs2", vp),
         ("tp3hist", vp), ("ph2w", _P_U8 * 2), ("ph3w", _P_U8 * 2), ("partials", vp), ("partials_cap", C.c_longlong),
@@ -255,6 +255,8 @@ def lib():
         L.gm_unet_head_scratch.restype = C.c_longlong
         L.gm_level3_persist_flags.argtypes = [C.POINTER(C.c_int)]
         L.gm_level3_persist_flags.restype = C.c_longlong
+        L.gm_l0_words.argtypes = [C.c_longlong, C.c_longlong, C.c_longlong]
+        L.gm_l0_words.restype = C.c_longlong
         _lib = L
     return _lib
 
@@ -263,6 +265,7 @@ SIGNATURES = {
     "gm_level_step": [C.POINTER(gm_level_args), C.POINTER(gm_props), vp],
     "gm_level3_persist": [C.POINTER(gm_persist_args), C.POINTER(gm_props), vp],
     "gm_toolpath_rows": [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp],
+    "gm_l0_fill": [vp, C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong, C.c_int, vp],
     "gm_level3_persist_shape": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "gm_state_properties": [C.POINTER(gm_state_props_args), C.POINTER(gm_props), vp],
     "gm_fine_source": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), vp,
@@ -280,6 +283,7 @@ SIGNATURES = {
     "gm_couple": [C.POINTER(gm_couple_args), C.POINTER(gm_props), vp],
     "gm_coarse_source": [C.POINTER(gm_coarse_source_args), C.POINTER(gm_props), vp],
     "gm_subcycle": [C.POINTER(gm_subcycle_plan), C.POINTER(gm_props), vp],
+    "gm_subcycle_batched": [C.POINTER(gm_subcycle_plan), C.c_int, C.POINTER(gm_props), vp],
     "gm_ring_prolong": [C.POINTER(gm_ring_args), vp],
     "gm_level_step_batched": [vp, C.c_int, vp, vp, C.c_longlong, vp],
     "gm_level_batched_prepare": [vp, C.c_int, vp, vp, C.c_longlong, C.POINTER(gm_batch_info), vp],
@@ -292,6 +296,10 @@ SIGNATURES = {
     "gm_melt_pool": [C.POINTER(gm_meltpool_args), vp],
     "gm_field_error": [C.c_int, vp, C.c_int, vp, C.c_longlong, vp, C.c_longlong, vp, vp],
     "gm_unet_conv3": [C.POINTER(gm_conv_args), vp],
+    "gm_unet_conv3_tc": [C.POINTER(gm_conv_args), vp],
+    "gm_unet_conv3_mma": [C.POINTER(gm_conv_args), vp],
+    "gm_unet_conv3_tc_eligible": [C.POINTER(gm_conv_args)],
+    "gm_unet_tc_status": [],
     "gm_unet_wgrad": [C.POINTER(gm_wgrad_args), vp],
     "gm_unet_bias_grad": [C.POINTER(C.c_int), C.c_int, vp, C.c_int, C.c_int, vp, C.c_longlong, vp, vp],
     "gm_unet_pool2": [C.POINTER(C.c_int), C.c_int, vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp],

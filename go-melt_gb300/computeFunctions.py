@@ -59,7 +59,7 @@ class LevelView(dict):
         e, lv = self.engine, self.lev
         if lv == 0:
             if k == "S1":
-                return e.L0.to(e.dtype)
+                return e.l0_s1().to(e.dtype)
             if k == "S2":
                 return self._l0_s2()
             raise KeyError(k)
@@ -77,7 +77,7 @@ class LevelView(dict):
 
     def _l0_s2(self):
         e = self.engine
-        out = torch.zeros(e.L0.numel(), dtype=torch.bool, device=e.dev)
+        out = torch.zeros(e.geo.L0_nn, dtype=torch.bool, device=e.dev)
         if e.s2_prev_lo is not None:
             idx = _l0_index(e.geo.L0_nodes, [np.asarray(e.s2_prev_lo[d]) + np.arange(e.geo.L[3].nodes[d])
                                              for d in range(3)])
@@ -89,7 +89,9 @@ class LevelView(dict):
         t = torch.as_tensor(v, device=e.dev)
         if lv == 0:
             if k == "S1":
-                e.L0.copy_((t > 0.499).to(torch.uint8).reshape(-1))
+                from engine import l0_pack
+
+                e.L0.copy_(l0_pack(t.reshape(-1), e.geo.L0_nodes))
                 return
             raise KeyError(f"Level 0 field {k} is not assignable")
         if k in ("T0", "T"):
@@ -781,11 +783,11 @@ def saveFinalResult(Level, save_str, save_path, zoffset):
 
 
 def saveState(Level, save_str, record_lab, save_path, zoffset):
-    """:2024-2057: S1 only (Level 0 written as its one-byte store)."""
+    """:2024-2057: S1 only (Level 0 unpacked from its bit store to one byte a node)."""
     import vtk
 
     c = [np.asarray(Level["node_coords"][d], dtype=np.float64) for d in range(3)]
-    s1 = Level.engine.L0 if isinstance(Level, LevelView) and Level.lev == 0 else Level["S1"]
+    s1 = Level.engine.l0_s1() if isinstance(Level, LevelView) and Level.lev == 0 else Level["S1"]
     vtk.write_vtr(f"{save_path}{save_str}{record_lab:08}", c[0], c[1], c[2] - zoffset,
                   {"State (Powder/Solid)": _host(s1)})
 

@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <vector>
+
 #include "gm_common.cuh"
 #include "gomelt.h"
 
@@ -413,7 +415,7 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   }
   l0.l0_nx = p->L0_nx;
   l0.l0_ny = p->L0_ny;
-  l0.l0_s1 = p->L0;
+  l0.l0_bits = p->L0;
   l0.ph = p->L3.ph;
   GM_TRY(gm_l0_scatter(&l0, c.st));
   return c.rc;
@@ -470,6 +472,101 @@ int subcycle_graph(const gm_subcycle_plan* p, const gm_props* props, void* strea
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Many instances: their subcycle calls as one CUDA graph of parallel branches.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Streams and events of the branches, created once per (calling thread,
+// branch) and kept for the life of the process.
+struct Branches {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  int ensure(int nb) {
+    if (!fork && cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return GM_ERR_CUDA;
+    while ((int)streams.size() < nb) {
+      cudaStream_t s;
+      cudaEvent_t e;
+      if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return GM_ERR_CUDA;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return GM_ERR_CUDA;
+      streams.push_back(s);
+      joins.push_back(e);
+    }
+    return GM_OK;
+  }
+};
+thread_local Branches g_branches;
+
+struct BatchSlot {
+  void* stream = nullptr;
+  int nb = 0;
+  cudaGraphExec_t exec = nullptr;
+  int calls = 0;
+};
+thread_local BatchSlot g_bslots[4];
+
+// Issue the nb calls, instance i on branch stream i forked from `stream` and
+// joined back into it (captured or not).
+int issue_branches(const gm_subcycle_plan* plans, int nb, const gm_props* props, cudaStream_t st) {
+  Branches& b = g_branches;
+  if (cudaEventRecord(b.fork, st) != cudaSuccess) return GM_ERR_CUDA;
+  int rc = GM_OK;
+  for (int i = 0; i < nb && rc == GM_OK; ++i) {
+    if (cudaStreamWaitEvent(b.streams[i], b.fork, 0) != cudaSuccess) return GM_ERR_CUDA;
+    rc = subcycle_issue(&plans[i], &props[i], b.streams[i]);
+    if (cudaEventRecord(b.joins[i], b.streams[i]) != cudaSuccess) return GM_ERR_CUDA;
+    if (cudaStreamWaitEvent(st, b.joins[i], 0) != cudaSuccess) return GM_ERR_CUDA;
+  }
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int gm_subcycle_batched(const gm_subcycle_plan* plans, int nb, const gm_props* props, void* stream) {
+  if (!plans || !props || nb < 1 || !stream) return GM_ERR_ARG;
+  for (int i = 0; i < nb; ++i) {
+    if (!plan_ok(&plans[i]) || (plans[i].dtype != GM_F32 && plans[i].dtype != GM_F64)) return GM_ERR_ARG;
+    if (plans[i].persist) return GM_ERR_ARG;  // cooperative launches of concurrent branches are not co-scheduled
+  }
+  if (g_branches.ensure(nb) != GM_OK) return GM_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchSlot* slot = nullptr;
+  for (auto& sl : g_bslots)
+    if (sl.calls > 0 && sl.stream == stream && sl.nb == nb) slot = &sl;
+  if (!slot)
+    for (auto& sl : g_bslots)
+      if (sl.calls == 0) {
+        sl.stream = stream;
+        sl.nb = nb;
+        slot = &sl;
+        break;
+      }
+  // the first call of a batch issues directly (it fills the launch-shape caches)
+  if (!slot || slot->calls++ == 0) return issue_branches(plans, nb, props, st);
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return GM_ERR_CUDA;
+  const int rc = issue_branches(plans, nb, props, st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (rc != GM_OK || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != GM_OK ? rc : GM_ERR_CUDA;
+  }
+  int out = GM_OK;
+  if (slot->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(slot->exec, graph, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(slot->exec);
+      slot->exec = nullptr;
+    }
+  }
+  if (!slot->exec && cudaGraphInstantiate(&slot->exec, graph, 0) != cudaSuccess) out = GM_ERR_CUDA;
+  if (out == GM_OK && cudaGraphLaunch(slot->exec, st) != cudaSuccess) out = GM_ERR_LAUNCH;
+  cudaGraphDestroy(graph);
+  return out;
+}
 
 extern "C" int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream) {
   if (!plan_ok(p) || !props || (p->dtype != GM_F32 && p->dtype != GM_F64)) return GM_ERR_ARG;

@@ -65,8 +65,10 @@ struct PersistK {
 constexpr int PERSIST_MAX_THREADS = 768;
 constexpr long long PERSIST_WAIT_CYCLES = 2000000000LL;  // about one second at the GB300's clocks
 
+// Publish a counter: a release fence at GPU scope (it orders the CTA's
+// writes, which the preceding barrier made this thread's) and the store.
 __device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+  asm volatile("fence.acq_rel.gpu;\n st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -121,8 +123,11 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
   const int y = Y0 + 1 + r;
   const bool own = lane >= 1 && lane <= TW && xin && y < ny;  // the lane's node column belongs to the tile
   const bool dir = x == 0 || x == nx - 1 || y == 0 || y == ny - 1;  // Dirichlet column
-  const int nint = ntop - 1;  // interior planes 1 .. ntop-1
-  const int za = 1 + (seg * nint) / a.nseg, zb = 1 + ((seg + 1) * nint) / a.nseg;
+  // interior planes 1 .. ntop-1 split over the segments, the top plane
+  // (surface flux) counted as two planes of work of the last segment
+  const int nint = ntop - 1, units = nint + 2;
+  const int za = 1 + (seg * units) / a.nseg;
+  const int zb = seg == a.nseg - 1 ? ntop : 1 + ((seg + 1) * units) / a.nseg;
   const bool top_task = seg == a.nseg - 1, bottom_task = seg == 0;
   const real a1 = a.sa1, b1 = a.sb1, b2 = a.sb2;
   const int L = nx + ny + nz;
@@ -139,11 +144,16 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
     const real sx = xin ? tb[x] : (real)0;
     const real sxy = sx * ((y < ny) ? tb[nx + y] : (real)0);
 
-    // new phase, value and melt time of the owned node at plane p
+    // step s+1 lives in exchange field (s+1) & 1; the last step publishes nothing
+    real* const xbn = s == a.nsteps - 1 ? nullptr : ((s & 1) ? a.xb0 : a.xb1);
+    const bool edge = lane == 1 || lane == TW || r == 0 || r == TY - 1;  // read by a neighbouring tile
+    // new phase, value and melt time of the owned node at plane p; edge
+    // nodes also go to the exchange field at once
     auto finish = [&](int p, real Tn, real Told) {
       Tn = fmax(Tn, P.T_amb);
       nxt[(p * RYH + r + 1) * 32 + lane] = Tn;
       const int id = col + p * nxy;
+      if (edge && xbn) __stcg(&xbn[id], Tn);
       uint8_t& phr = PH[(p * TY + r) * 32 + lane];
       const uint32_t ph = phr;
       const bool s2 = Told >= P.T_liquidus;
@@ -163,48 +173,47 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
     };
     auto at = [&](const real* b, int p, int i) { return b[(p * RYH + i) * 32 + lane]; };
 
-    // interior planes [za, zb): rows r .. r+2 of the halo-indexed buffer
+    // the step's z source factors of this warp's planes za .. za+31, one a lane
+    const real szl = (za + lane <= ntop) ? tb[nx + ny + za + lane] : (real)0;
+    // interior planes [za, zb): rows r .. r+2 of the halo-indexed buffer,
+    // walked with pointers (plane stride `plane` values)
     if (za < zb) {
-      real Tm[3], T0[3], Tp[3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        Tm[i] = at(cur, za - 1, r + i);
-        T0[i] = at(cur, za, r + i);
-      }
+      const real* c = cur + (size_t)(za - 1) * plane + r * 32 + lane;
+      real Tm0 = c[0], Tm1 = c[32], Tm2 = c[64];
+      c += plane;
+      real T00 = c[0], T01 = c[32], T02 = c[64];
       for (int p = za; p < zb; ++p) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i) Tp[i] = at(cur, p + 1, r + i);
-        real Zm[3], Zk[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const real sm = Tm[i] + Tp[i];
-          Zm[i] = sm + (real)4 * T0[i];
-          Zk[i] = (real)2 * T0[i] - sm;
-        }
-        const real u = Zm[0] + Zm[2];
-        const real w = Zk[0] + Zk[2];
-        const real A = a1 * (u + (real)4 * Zm[1]);
-        const real B = b1 * ((real)2 * Zm[1] - u) + b2 * (w + (real)4 * Zk[1]);
+        c += plane;
+        const real Tp0 = c[0], Tp1 = c[32], Tp2 = c[64];
+        const real s0 = Tm0 + Tp0, s1 = Tm1 + Tp1, s2 = Tm2 + Tp2;
+        const real Zm0 = s0 + (real)4 * T00, Zm1 = s1 + (real)4 * T01, Zm2 = s2 + (real)4 * T02;
+        const real Zk0 = (real)2 * T00 - s0, Zk1 = (real)2 * T01 - s1, Zk2 = (real)2 * T02 - s2;
+        const real u = Zm0 + Zm2;
+        const real w = Zk0 + Zk2;
+        const real A = a1 * (u + (real)4 * Zm1);
+        const real B = b1 * ((real)2 * Zm1 - u) + b2 * (w + (real)4 * Zk1);
         const real D = B - A;
         const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
+        const real sz = __shfl_sync(FULL, szl, p - za);
         if (own) {
-          const real Told = T0[1];
+          const real Told = T01;
           real Tn;
           if (dir) {
             Tn = ring_value(p);
           } else {
             const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
             real Rt = -KT;
-            Rt += sxy * tb[nx + ny + p];
+            Rt += sxy * sz;
             Tn = Told + Rt * minv;
           }
           finish(p, Tn, Told);
         }
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          Tm[i] = T0[i];
-          T0[i] = Tp[i];
-        }
+        Tm0 = T00;
+        Tm1 = T01;
+        Tm2 = T02;
+        T00 = Tp0;
+        T01 = Tp1;
+        T02 = Tp2;
       }
     }
     // top plane ntop: one-sided z operators, lumped mass of 4 elements, surface flux
@@ -217,6 +226,7 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
         t0c.v[i] = at(cur, ntop, r + i);
       }
       const RegCol<real, 1> sf = sep_surface<real, 1>(P, a.w2, x, nx, y, ny, t0c);
+      const real szt = __shfl_sync(FULL, szl, ntop - za);
       real Zm[3], Zk[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
@@ -237,7 +247,7 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
         } else {
           const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
           real Rt = -KT;
-          Rt += sxy * tb[nx + ny + ntop];
+          Rt += sxy * szt;
           Rt += sf.v[0];
           Tn = Told + Rt * ((real)2 * minv);
         }
@@ -250,32 +260,10 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
 
     if (s == a.nsteps - 1) break;
 
-    // ---- publish this tile's edge columns of step s+1 ----
-    real* xb = (s & 1) ? a.xb0 : a.xb1;  // step s+1 lives in exchange field (s+1) & 1
-    const int E = TY > 1 ? 2 * TW + 2 * (TY - 2) : TW;
-    for (int k = threadIdx.x; k < nz * E; k += blockDim.x) {
-      const int z = k / E, e = k - z * E;
-      int rr, l;
-      if (e < TW) {
-        rr = 0;
-        l = 1 + e;
-      } else if (e < 2 * TW) {
-        rr = TY - 1;
-        l = 1 + e - TW;
-      } else {
-        const int j = e - 2 * TW;
-        rr = 1 + (j >> 1);
-        l = (j & 1) ? TW : 1;
-      }
-      const int xx = X0 + l, yy = Y0 + 1 + rr;
-      if (xx < nx && yy < ny) __stcg(&xb[xx + yy * nx + z * nxy], nxt[(z * RYH + rr + 1) * 32 + l]);
-    }
-    __syncthreads();
+    // ---- publish step s+1: every edge node was written to the exchange field above ----
+    const real* xb = xbn;
     const unsigned target = a.base + (unsigned)(s + 1);
-    if (threadIdx.x == 0 && tile + 1 != a.hold) {
-      __threadfence();
-      st_release(a.flags + tile, target);
-    }
+    if (threadIdx.x == 0 && tile + 1 != a.hold) st_release(a.flags + tile, target);
     // ---- wait for the neighbours' step s+1 (bounded) ----
     if (threadIdx.x < 9 && threadIdx.x != 4) {
       const int nbx = bx + (int)(threadIdx.x % 3) - 1, nby = by + (int)(threadIdx.x / 3) - 1;
@@ -393,6 +381,7 @@ bool persist_shape(int nx, int ny, int nz, size_t esz, PersistShape* s) {
   if (nseg > seg_cap) nseg = seg_cap;
   if (nseg < 1) nseg = 1;
   s->nseg = nseg;
+  if ((nint + 2) / nseg + 3 > 32) return false;  // a segment's planes, top included, one z factor a lane
   s->threads = 32 * s->ty * nseg;
   s->smem = persist_smem(nz, s->ty, esz);
   return s->smem <= smem_cap();

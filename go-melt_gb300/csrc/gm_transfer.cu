@@ -161,18 +161,25 @@ __global__ void restrict_s1_kernel(int n0, int n1, int n2, const Map3<real> m, c
     coarse_ph[id] |= PH_S1;
 }
 
+// Level-0 S1 store: one bit per node in 32-bit words, each (y, z) row of
+// l0_nx nodes padded to whole words: node (x, y, z) is bit x % 32 of word
+// (z * l0_ny + y) * l0_words_per_row(l0_nx) + x / 32.
+__host__ __device__ inline long long l0_words_per_row(long long lnx) { return (lnx + 31) / 32; }
+
 // Level-0 gather (moveEverything :2500-2502): window phase from the Level-0
 // S1 store; S2 from the previous window's phase where the windows overlap
 // (Level 0 holds S2 only inside the last scattered window, :2390-2392).
 __global__ void l0_gather_kernel(int n0, int n1, int n2, const int* ix, const int* iy, const int* iz, long long lnx,
-                                 long long lny, const uint8_t* l0, uint8_t* ph, const uint8_t* prev_ph, int plo0,
+                                 long long lny, const uint32_t* l0, uint8_t* ph, const uint8_t* prev_ph, int plo0,
                                  int plo1, int plo2, int pn0, int pn1, int pn2) {
   const long long tot = (long long)n0 * n1 * n2;
+  const long long wpr = l0_words_per_row(lnx);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
        t += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
-    const long long id = ix[i] + iy[j] * lnx + iz[k] * lnx * lny;
-    uint8_t p = l0[id] ? PH_S1 : 0;
+    const int x = ix[i];
+    const uint32_t w = l0[(iz[k] * lny + iy[j]) * wpr + (x >> 5)];
+    uint8_t p = ((w >> (x & 31)) & 1u) ? PH_S1 : 0;
     if (prev_ph) {
       const int a = ix[i] - plo0, b = iy[j] - plo1, c = iz[k] - plo2;
       if (a >= 0 && a < pn0 && b >= 0 && b < pn1 && c >= 0 && c < pn2)
@@ -182,14 +189,45 @@ __global__ void l0_gather_kernel(int n0, int n1, int n2, const int* ix, const in
   }
 }
 
-// Level-0 scatter (subcycleGOMELT :3628-3630): store the window's S1.
+// Level-0 scatter (subcycleGOMELT :3628-3630): store the window's S1.  A bit
+// that already holds the value is left alone; the others are set or cleared
+// with an atomic on their word (neighbouring nodes share words).
 __global__ void l0_scatter_kernel(int n0, int n1, int n2, const int* ix, const int* iy, const int* iz, long long lnx,
-                                  long long lny, uint8_t* l0, const uint8_t* ph) {
+                                  long long lny, uint32_t* l0, const uint8_t* ph) {
   const long long tot = (long long)n0 * n1 * n2;
+  const long long wpr = l0_words_per_row(lnx);
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
        t += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
-    l0[ix[i] + iy[j] * lnx + iz[k] * lnx * lny] = (ph[t] & PH_S1) ? 1 : 0;
+    const int x = ix[i];
+    uint32_t* w = l0 + (iz[k] * lny + iy[j]) * wpr + (x >> 5);
+    const uint32_t bit = 1u << (x & 31);
+    const bool s1 = (ph[t] & PH_S1) != 0;
+    const bool cur = (*w & bit) != 0;
+    if (s1 && !cur) atomicOr(w, bit);
+    if (!s1 && cur) atomicAnd(w, ~bit);
+  }
+}
+
+// Node range [first, last) of the store set to `value` (whole words where the
+// range covers them, atomics on the partial words at its ends per row).
+__global__ void l0_fill_kernel(long long lnx, long long lny, long long lnz, long long first, long long last,
+                               uint32_t* l0, int value) {
+  const long long wpr = l0_words_per_row(lnx);
+  const long long words = wpr * lny * lnz;
+  for (long long wi = blockIdx.x * (long long)blockDim.x + threadIdx.x; wi < words;
+       wi += (long long)gridDim.x * blockDim.x) {
+    const long long row = wi / wpr, x0 = (wi - row * wpr) * 32;
+    const long long id0 = row * lnx + x0;  // node id of bit 0 of this word
+    uint32_t mask = 0;
+    for (int b = 0; b < 32; ++b) {
+      const long long id = id0 + b;
+      if (x0 + b < lnx && id >= first && id < last) mask |= 1u << b;
+    }
+    if (mask == 0xffffffffu)
+      l0[wi] = value ? 0xffffffffu : 0u;
+    else if (mask)
+      value ? atomicOr(l0 + wi, mask) : atomicAnd(l0 + wi, ~mask);
   }
 }
 
@@ -316,21 +354,38 @@ extern "C" int gm_restrict_s1(const gm_restrict_s1_args* g, void* stream) {
 }
 
 extern "C" int gm_l0_gather(const gm_l0_args* g, void* stream) {
-  if (!g || !g->l0_s1 || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2] || g->ph == g->prev_ph) return GM_ERR_ARG;
+  if (!g || !g->l0_bits || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2] || g->ph == g->prev_ph ||
+      g->l0_nx < 1 || g->l0_ny < 1)
+    return GM_ERR_ARG;
   const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
   if (tot == 0) return GM_OK;
   l0_gather_kernel<<<grid_for(tot), 256, 0, (cudaStream_t)stream>>>(
-      g->n[0], g->n[1], g->n[2], g->idx[0], g->idx[1], g->idx[2], g->l0_nx, g->l0_ny, g->l0_s1, g->ph, g->prev_ph,
+      g->n[0], g->n[1], g->n[2], g->idx[0], g->idx[1], g->idx[2], g->l0_nx, g->l0_ny, g->l0_bits, g->ph, g->prev_ph,
       g->prev_lo[0], g->prev_lo[1], g->prev_lo[2], g->prev_n[0], g->prev_n[1], g->prev_n[2]);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 
 extern "C" int gm_l0_scatter(const gm_l0_args* g, void* stream) {
-  if (!g || !g->l0_s1 || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2]) return GM_ERR_ARG;
+  if (!g || !g->l0_bits || !g->ph || !g->idx[0] || !g->idx[1] || !g->idx[2] || g->l0_nx < 1 || g->l0_ny < 1)
+    return GM_ERR_ARG;
   const long long tot = (long long)g->n[0] * g->n[1] * g->n[2];
   if (tot == 0) return GM_OK;
   l0_scatter_kernel<<<grid_for(tot), 256, 0, (cudaStream_t)stream>>>(g->n[0], g->n[1], g->n[2], g->idx[0], g->idx[1],
-                                                                      g->idx[2], g->l0_nx, g->l0_ny, g->l0_s1, g->ph);
+                                                                      g->idx[2], g->l0_nx, g->l0_ny, g->l0_bits, g->ph);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" long long gm_l0_words(long long nx, long long ny, long long nz) {
+  if (nx < 1 || ny < 1 || nz < 1) return -1;
+  return l0_words_per_row(nx) * ny * nz;
+}
+
+extern "C" int gm_l0_fill(uint32_t* l0_bits, long long nx, long long ny, long long nz, long long first,
+                          long long last, int value, void* stream) {
+  if (!l0_bits || nx < 1 || ny < 1 || nz < 1 || first < 0 || last > nx * ny * nz || first > last) return GM_ERR_ARG;
+  if (first == last) return GM_OK;
+  l0_fill_kernel<<<grid_for(l0_words_per_row(nx) * ny * nz), 256, 0, (cudaStream_t)stream>>>(nx, ny, nz, first, last,
+                                                                                              l0_bits, value);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
 }
 

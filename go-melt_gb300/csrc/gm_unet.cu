@@ -541,7 +541,9 @@ using namespace gm;
 
 static Grid5 grid5(const int g[4]) { return Grid5{g[0], g[1], g[2], g[3]}; }
 
-extern "C" int gm_unet_conv3(const gm_conv_args* c, void* stream) {
+// The warp-level (mma.sync) form of the convolution: any slice alignment,
+// Cout in {16, 32, 64, 96, 128, 192}.
+extern "C" int gm_unet_conv3_mma(const gm_conv_args* c, void* stream) {
   if (!c || !c->in || !c->w || !c->out) return GM_ERR_ARG;
   if (c->cin < 16 || c->cin % 16 || c->cin + c->in_off > c->in_stride || c->cout + c->out_off > c->out_stride)
     return GM_ERR_ARG;
@@ -592,6 +594,19 @@ extern "C" int gm_unet_conv3(const gm_conv_args* c, void* stream) {
   }
 #undef GM_CONV_CASE
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_unet_conv3_tc_eligible(const gm_conv_args* c);
+extern "C" int gm_unet_conv3_tc(const gm_conv_args* c, void* stream);
+
+// The tensor-core (tcgen05) form where the call allows it, else mma.sync.
+extern "C" int gm_unet_conv3(const gm_conv_args* c, void* stream) {
+  if (c && gm_unet_conv3_tc_eligible(c)) {
+    for (int d = 0; d < 4; ++d)
+      if (c->grid[d] < 1) return GM_ERR_ARG;
+    return gm_unet_conv3_tc(c, stream);
+  }
+  return gm_unet_conv3_mma(c, stream);
 }
 
 extern "C" long long gm_unet_wgrad_scratch(const int grid[4], int cin, int cout) {

@@ -29,6 +29,38 @@ from levels import Geometry
 PH_S1, PH_S2 = 1, 2
 
 
+def l0_words(nodes):
+    """32-bit words of the bit-packed Level-0 S1 store of a node grid (each
+    (y, z) row of nodes[0] bits padded to whole words)."""
+    return ((int(nodes[0]) + 31) // 32) * int(nodes[1]) * int(nodes[2])
+
+
+def l0_pack(s1, nodes):
+    """Bit-pack a Level-0 S1 array (nodes[0]*nodes[1]*nodes[2] values, set
+    where > 0.499) into the store's int32 words (torch, on s1's device; one
+    byte of work space per node)."""
+    t = torch.as_tensor(s1)
+    nx, ny, nz = (int(v) for v in nodes)
+    wpr = (nx + 31) // 32
+    rows = nz * ny
+    pad = torch.zeros(rows, wpr * 32, dtype=torch.uint8, device=t.device)
+    pad[:, :nx] = (t.reshape(rows, nx) > 0.499).to(torch.uint8)
+    sh = torch.arange(8, dtype=torch.uint8, device=t.device)
+    byt = (pad.reshape(rows, wpr * 4, 8) << sh).sum(dim=2, dtype=torch.uint8)  # little-endian bytes of the words
+    return byt.reshape(-1).view(torch.int32).clone()
+
+
+def l0_unpack(words, nodes):
+    """Level-0 S1 (uint8 0/1 per node, node-major) from the store's words."""
+    nx, ny, nz = (int(v) for v in nodes)
+    wpr = (nx + 31) // 32
+    rows = nz * ny
+    byt = words.contiguous().view(torch.uint8).reshape(rows, wpr * 4)
+    sh = torch.arange(8, dtype=torch.uint8, device=words.device)
+    bits = (byt[:, :, None] >> sh) & 1
+    return bits.reshape(rows, wpr * 32)[:, :nx].reshape(-1).contiguous()
+
+
 class TableArena:
     """Per-window tables of one move packed into a pinned host buffer and copied
     to a device buffer with one non-blocking H2D copy.  Two pinned buffers
@@ -190,14 +222,16 @@ class Engine:
         self.T = {lv: torch.full((g.L[lv].nn,), Tamb, **f) for lv in (1, 2, 3)}
         self.Tp = {lv: torch.zeros(g.L[lv].nn, **f) for lv in (2, 3)}
         self.ph = {lv: torch.zeros(g.L[lv].nn, dtype=torch.uint8, device=self.dev) for lv in (1, 2, 3)}
-        self.L0 = torch.zeros(g.L0_nn, dtype=torch.uint8, device=self.dev)
+        self.L0 = torch.zeros(l0_words(g.L0_nodes), dtype=torch.int32, device=self.dev)  # bit-packed S1
         self.acc3 = torch.zeros(g.L[3].nn, **f)
         self.macc3 = torch.zeros(g.L[3].nn, **f)
         self.s2_prev_lo = None  # Level-0 start of the window last written (S2 snapshot)
         self._pending = None  # MovePlan made by plan_move and not yet applied
         self.use_graph = False  # run gm_subcycle as one CUDA graph per call
         self.use_pdl = True  # level steps as programmatic dependent launches
-        self.use_persist = True  # a Level-2 step's Level-3 steps as one persistent launch, where the window allows
+        # a Level-2 step's Level-3 steps as one persistent launch, where the window allows (opt-in: on the
+        # part-scale window it measures slower than one launch a step)
+        self.use_persist = False
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)  # GM_PERSIST_* bits of the device kernels
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
@@ -394,7 +428,7 @@ class Engine:
             a.n[d] = int(n[d])
             a.idx[d] = idx[d]
         a.l0_nx, a.l0_ny = self.geo.L0_nodes[0], self.geo.L0_nodes[1]
-        a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
+        a.l0_bits = self.L0.data_ptr()
         a.ph = C.cast(ph_out.data_ptr(), C.POINTER(C.c_uint8))
         if prev_ph is not None:
             a.prev_ph = C.cast(prev_ph.data_ptr(), C.POINTER(C.c_uint8))
@@ -411,7 +445,7 @@ class Engine:
             a.n[d] = g.L[3].nodes[d]
             a.idx[d] = idx[d]
         a.l0_nx, a.l0_ny = g.L0_nodes[0], g.L0_nodes[1]
-        a.l0_s1 = C.cast(self.L0.data_ptr(), C.POINTER(C.c_uint8))
+        a.l0_bits = self.L0.data_ptr()
         a.ph = C.cast(self.ph[3].data_ptr(), C.POINTER(C.c_uint8))
         N.call("gm_l0_scatter", C.byref(a), kern.stream_ptr(self.stream))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
@@ -579,6 +613,9 @@ class Engine:
                         torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev),
                         torch.empty(N2, L3.nn, dtype=self.dtype, device=self.dev))
         p = self._plan(rows, dtd, out_hist)
+        if getattr(self, "_batch_plan", False):  # subcycle_batched collects the plan instead
+            self._last_plan = p
+            return out_hist
         N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
                kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps), persist=bool(p.persist)))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
@@ -625,7 +662,7 @@ class Engine:
             p.rhs2_lo[d], p.rhs2_n[d] = c32.box_lo[d], c32.box_n[d]
             p.l0_idx3[d] = tb["l0_3"][d]
         p.c32, p.c31, p.c21 = c32.struct, c31.struct, c21.struct
-        p.L0 = pu(self.L0)
+        p.L0 = self.L0.data_ptr()
         p.L0_nx, p.L0_ny = g.L0_nodes[0], g.L0_nodes[1]
         p.rows, p.dts = rows, dtd
         p.T1p, p.T1c = self._buf("T1p", nn1).data_ptr(), self._buf("T1c", nn1).data_ptr()
@@ -810,13 +847,22 @@ class Engine:
         g.L0_overlap = [np.asarray(a).astype(np.int64) for a in L0["overlapNodes"]]
         g.L0_overlap_L2 = [np.asarray(a).astype(np.int64) for a in L0["overlapNodes_L2"]]
         g.L0_coords = [np.asarray(c, dtype=np.float64).copy() for c in L0["node_coords"]]
-        self.L0 = torch.as_tensor((np.asarray(L0["S1"], dtype=np.float64) > 0.499).astype(np.uint8),
-                                  device=self.dev).contiguous()
+        self.L0 = l0_pack(torch.as_tensor(np.asarray(L0["S1"], dtype=np.float64), device=self.dev), g.L0_nodes)
         s2 = np.asarray(L0["S2"]).astype(bool)
         self.s2_prev_lo = [int(g.L0_overlap[d][0]) for d in range(3)] if s2.any() else None
         self.acc3 = torch.zeros(g.L[3].nn, **f)
         self.macc3 = torch.zeros(g.L[3].nn, **f)
         self.build_tables()
+
+    def l0_s1(self):
+        """Level-0 S1 as one uint8 (0/1) per node."""
+        return l0_unpack(self.L0, self.geo.L0_nodes)
+
+    def l0_fill(self, first, last, value):
+        """Level-0 nodes [first, last) set to value (gm_l0_fill)."""
+        n = self.geo.L0_nodes
+        N.call("gm_l0_fill", self.L0.data_ptr(), int(n[0]), int(n[1]), int(n[2]), int(first), int(last),
+               int(value), kern.stream_ptr(self.stream))
 
     def fields_numpy(self):
         """Host copies of the state in the reference's field names."""
@@ -827,5 +873,41 @@ class Engine:
                         "S2": (ph & PH_S2) != 0}
             if lev > 1:
                 out[lev]["Tprime0"] = self.Tp[lev].double().cpu().numpy()
-        out[0] = {"S1": self.L0.cpu().numpy().astype(np.float64)}
+        out[0] = {"S1": self.l0_s1().cpu().numpy().astype(np.float64)}
         return out
+
+
+def subcycle_batched(engines, rows_list, rows_device=None, dts_device=None):
+    """subcycleGOMELT of many independent engines (scan instances) as ONE CUDA
+    graph (gm_subcycle_batched): each engine plans its call as Engine.subcycle
+    does, then all calls are issued as parallel branches of one graph on the
+    first engine's stream, which every engine must share.  The persistent
+    Level-3 kernel is not used here (its cooperative launches are not
+    co-scheduled across concurrent branches).  rows_list[i]: host rows of
+    engine i (or None with rows_device[i] / dts_device[i])."""
+    st = engines[0].stream
+    if st is None or any(e.stream is not st for e in engines):
+        raise N.GomeltError("batched engines must share one (non-default) stream")
+    plans = (N.gm_subcycle_plan * len(engines))()
+    props = (N.gm_props * len(engines))()
+    kernels = 0
+    for i, e in enumerate(engines):
+        e._batch_plan = True
+        keep = e.use_persist
+        e.use_persist = False
+        try:
+            e.subcycle(rows_list[i] if rows_list is not None else None,
+                       rows_device=None if rows_device is None else rows_device[i],
+                       dts_device=None if dts_device is None else dts_device[i])
+        finally:
+            e._batch_plan = False
+            e.use_persist = keep
+        plans[i] = e._last_plan
+        props[i] = e.ps
+        kernels += N.subcycle_kernel_count(e.N2, e.N3, N.props_constant(e.ps))
+    N.call("gm_subcycle_batched", plans, len(engines), props, kern.stream_ptr(st), kernels=kernels)
+    for e in engines:
+        g = e.geo
+        e.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
+        e._last_plan = None
+

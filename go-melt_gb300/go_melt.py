@@ -52,10 +52,12 @@ class AccumStore:
         self.max_accum = torch.zeros(n, dtype=engine.dtype, device=engine.dev)
 
     def idx(self):
+        """Level-0 node ids of the Level-3 window (Levels[0]["idx"]), formed on
+        the device from the three per-axis index arrays."""
         g = self.e.geo
-        x, y, z = (np.asarray(a) for a in g.L0_overlap)
-        i = (x[None, None, :] + y[None, :, None] * g.L0_nodes[0] + z[:, None, None] * g.L0_nodes[0] * g.L0_nodes[1])
-        return torch.as_tensor(i.reshape(-1), device=self.e.dev)
+        x, y, z = (torch.as_tensor(np.asarray(a, dtype=np.int64), device=self.e.dev) for a in g.L0_overlap)
+        nx, nxy = int(g.L0_nodes[0]), int(g.L0_nodes[0]) * int(g.L0_nodes[1])
+        return (x[None, None, :] + y[None, :, None] * nx + z[:, None, None] * nxy).reshape(-1)
 
 
 def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
@@ -153,7 +155,7 @@ def go_melt(solver_input: dict, dtype=torch.float32, device="cuda"):
                         move_vert = False
                         substrate = getSubstrateNodes(Levels)
                         eng.substrate = substrate
-                        eng.L0[: substrate[0]] = 1
+                        eng.l0_fill(0, substrate[0], 1)
                 if wait_inc <= Nonmesh["wait_time"]:
                     Levels, reset = stepGOMELT(Levels, ne_nn, tmp_ne_nn, None, None, lp, Properties, lp[5], lp[6],
                                                substrate)
@@ -236,9 +238,13 @@ def shift_level1(eng, z_new, sidx, s1_storage):
     eng._interp([(m, eng.T[1], 1.0)], L1.nodes, out)
     eng._clamp(out)
     eng.T[1].copy_(out)
+    # the reference indexes its JAX S1_storage: an update at a row outside the
+    # store is dropped, a read outside it takes the nearest row
+    rows = s1_storage.shape[0]
     s1 = (eng.ph[1] & 1)
-    s1_storage[sidx - 1].copy_(s1)
-    eng.ph[1].copy_((eng.ph[1] & 2) | s1_storage[sidx])
+    if -rows <= sidx - 1 < rows:
+        s1_storage[sidx - 1].copy_(s1)
+    eng.ph[1].copy_((eng.ph[1] & 2) | s1_storage[min(max(sidx, 0), rows - 1)])
     L1.coords = [L1.coords[0], L1.coords[1], np.asarray(z_new, dtype=float)]
 
 
@@ -249,8 +255,10 @@ def shift_level0(eng, acc, laser_z):
     nxy = g.L0_nodes[0] * g.L0_nodes[1]
     n1 = nxy * g.layer_idx_delta
     n2 = nxy * (g.L0_nodes[2] - g.layer_idx_delta)
-    eng.L0[:n2] = eng.L0[n1:].clone()
-    eng.L0[n2:] = 0
+    wpl = ((g.L0_nodes[0] + 31) // 32) * g.L0_nodes[1]  # words of one Level-0 plane in the bit store
+    w1, w2 = wpl * g.layer_idx_delta, wpl * (g.L0_nodes[2] - g.layer_idx_delta)
+    eng.L0[:w2] = eng.L0[w1:].clone()
+    eng.L0[w2:] = 0
     g.L0_coords[2] = g.L0_orig_coords[2] + laser_z - g.L0_orig_coords[2][-1]
     acc.max_accum.zero_()
     acc.accum[:n2] = acc.accum[n1:].clone()
@@ -258,10 +266,11 @@ def shift_level0(eng, acc, laser_z):
 
 
 def save_accum(acc, Nonmesh):
+    """The layer's melt-time record (go_melt.py:246-256), in the engine's precision."""
     a = torch.maximum(acc.accum, acc.max_accum)
     acc.accum.copy_(a)
     np.savez(os.path.join(Nonmesh["save_path"], "accum_time" + str(Nonmesh["layer_num"]).zfill(4)),
-             accum_time=a.double().cpu().numpy())
+             accum_time=a.cpu().numpy())
 
 
 def snapshot_state(eng, acc, time_inc, record_inc, s1_storage):

@@ -74,6 +74,32 @@ def part_scale_raster():
     }
 
 
+def part_scale_layers(layers=3, ntracks=40, length=4.0, l1_xy=20.0):
+    """The part-scale raster over several layers of 50 um: Level 1 extended to
+    z = 0.3 mm above the part top (53 element planes; the elements above the
+    current layer are inactive), serpentine layers at z = 0.05, 0.10, ... mm.
+    The Level-2 window keeps its 2 x 2 x 0.3 mm extent with 12 element planes
+    (25 um) instead of 15 (20 um): a new layer moves the windows up by one
+    layer height in whole Level-2 cells (the driver's integer ratio
+    round(layer_height / h2z), go_melt.py:42-44), which 20 um cells (2.5 a
+    layer) cannot do, and the Level-3 overlap would leave Level 2.
+    ``l1_xy`` < 20 crops Level 1 (and with it Level 0) to a square of that size
+    around the windows, for tests."""
+    import createPath
+
+    c = part_scale_raster()
+    c["Level2"]["elements"] = [100, 100, 12]
+    lo = 10.0 - l1_xy / 2
+    ne = int(round(l1_xy / 0.1))
+    c["Level1"] = {"elements": [ne, ne, 53], "bounds": {"x": [lo, lo + l1_xy], "y": [lo, lo + l1_xy], "z": [-5.0, 0.3]},
+                   "conditions": _cond()}
+    x0 = 10.0 - length / 2
+    y0 = 10.0 - (ntracks - 1) * 0.05
+    c["raster"] = {"x0": x0, "y0": y0, "length": length, "hatch": 0.1, "ntracks": ntracks, "layers": layers}
+    c["gcode"] = createPath.serpentine_gcode(x0, y0, length, 0.1, ntracks, z=0.05, layers=layers, layer_height=0.05)
+    return c
+
+
 def precision_window():
     """Precision study: the part-scale raster with a fine Level-3 window of 0.5 x 0.5 x 0.1 mm
     at 2.5 um (200 x 200 x 40 elements; Level-2 to Level-3 ratio 8), placed on

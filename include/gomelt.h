@@ -208,7 +208,11 @@ typedef struct gm_restrict_s1_args {
 
 int gm_restrict_s1(const gm_restrict_s1_args* a, void* stream);
 
-/* Level-0 phase store (one byte per Level-0 node: 1 = S1).
+/* Level-0 phase store: S1 of every Level-0 node as one bit (the reference
+ * keeps a float S1 and a bool S2 per node, computeFunctions.py:206-246; every
+ * use of its S1 is S1 > 0.499).  Words of 32 bits, each (y, z) row of l0_nx
+ * nodes padded to whole words: node (x, y, z) is bit x % 32 of word
+ * (z * l0_ny + y) * ceil(l0_nx / 32) + x / 32 (gm_l0_words words in all).
  * gather: ph[t] = S1 from Level 0 at (idx[0][i], idx[1][j], idx[2][k]) plus
  *   the S2 bit of prev_ph where the previous window (Level-0 start prev_lo,
  *   size prev_n) covers the node (moveEverything :2500-2502; Level 0 keeps S2
@@ -218,7 +222,7 @@ typedef struct gm_l0_args {
   int n[3];
   const int* idx[3];
   long long l0_nx, l0_ny;
-  uint8_t* l0_s1;
+  uint32_t* l0_bits;
   uint8_t* ph;
   const uint8_t* prev_ph; /* gather only; NULL: no S2 anywhere */
   int prev_lo[3], prev_n[3];
@@ -309,6 +313,13 @@ int gm_clamp_min(int dtype, void* T, long long n, double lo, void* stream);
 
 int gm_l0_gather(const gm_l0_args* a, void* stream);
 int gm_l0_scatter(const gm_l0_args* a, void* stream);
+/* Words of the Level-0 store of an nx x ny x nz node grid (-1 if empty). */
+long long gm_l0_words(long long nx, long long ny, long long nz);
+/* Level-0 nodes [first, last) (node ids ix + iy nx + iz nx ny) set to value
+ * (0 or 1): the substrate planes of a new layer (go_melt.py:198-314 via
+ * getSubstrateNodes) and the planes freed by the layer shift (:258-296). */
+int gm_l0_fill(uint32_t* l0_bits, long long nx, long long ny, long long nz, long long first, long long last, int value,
+               void* stream);
 
 /* Per-axis geometry of a fine level inside a coarse level, for the terms that
  * the reference evaluates through computeCoarseFineShapeFunctions
@@ -455,7 +466,7 @@ typedef struct gm_subcycle_plan {
   const double* xq31[3];
   int rhs1_lo[3], rhs1_n[3]; /* Level-1 node box of the coupling terms (c21) */
   int rhs2_lo[3], rhs2_n[3]; /* Level-2 node box of the coupling terms (c32) */
-  uint8_t* L0;               /* Level-0 S1 store */
+  uint32_t* L0;              /* Level-0 S1 store, one bit a node (layout of gm_l0_args) */
   long long L0_nx, L0_ny;
   const int* l0_idx3[3];     /* Level-0 node index of the Level-3 window, per axis */
   const double* rows;        /* device: N2*N3 rows (x, y, z, jump, dwell, dt, P) */
@@ -502,6 +513,18 @@ typedef struct gm_subcycle_plan {
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
 int gm_subcycle(const gm_subcycle_plan* p, const gm_props* props, void* stream);
+
+/* nb independent subcycleGOMELT calls (scan instances of uneven mesh sizes,
+ * plans[i] with props[i]) as ONE CUDA graph launched on `stream` (not the
+ * legacy default stream): instance i is issued on a branch stream forked from
+ * `stream` and joined back, so the instances run concurrently.  The graph of
+ * a stream and batch size is updated in place from call to call (same
+ * topology while the instances keep their feature sets); the first call of a
+ * batch issues the branches directly.  Plans must not ask for the persistent
+ * Level-3 kernel (concurrent cooperative launches are not co-scheduled).
+ * Results are those of nb gm_subcycle calls.  No counterpart in the reference
+ * (which runs one instance a process). */
+int gm_subcycle_batched(const gm_subcycle_plan* plans, int nb, const gm_props* props, void* stream);
 
 /* ------------------------------------------------------------------------
  * The N3 Level-3 fine steps of one Level-2 step in ONE launch (persistent
@@ -689,6 +712,20 @@ typedef struct gm_conv_args {
  * (mirror 0), or the data gradient dx[u][ci] = sum_tap dy[u - d(tap)] .
  * w[tap][.][ci] with w passed as [27][Cin][Cout] (mirror 1). */
 int gm_unet_conv3(const gm_conv_args* a, void* stream);
+
+/* The two forms gm_unet_conv3 chooses between.  _tc: tcgen05.mma (BF16 in,
+ * FP32 accumulators in tensor memory), operand tiles by TMA
+ * (cp.async.bulk.tensor, zero fill at the sample borders); needs cin and cout
+ * multiples of 16 with cout <= 256, and 16-byte aligned bases and slices
+ * (in/out/mask offsets and strides multiples of 8); GM_ERR_UNSUPPORTED
+ * otherwise.  _mma: the warp-level mma.sync.m16n8k16 form (any even slice).
+ * gm_unet_conv3 takes _tc when gm_unet_conv3_tc_eligible(a) returns 1. */
+int gm_unet_conv3_tc(const gm_conv_args* a, void* stream);
+int gm_unet_conv3_mma(const gm_conv_args* a, void* stream);
+int gm_unet_conv3_tc_eligible(const gm_conv_args* a);
+/* Waits of the tensor-core convolutions that ran out since the last call
+ * (bit 0), -1 on a CUDA error; clears the word; synchronises the device. */
+int gm_unet_tc_status(void);
 
 typedef struct gm_wgrad_args {
   int grid[4];
