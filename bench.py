@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--cpu-steps", type=int, default=8, help="oracle fine steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--surrogate-steps", type=int, default=300,
+                    help="training steps of the surrogate block of the headline line (0: no surrogate block)")
     ap.add_argument("--l3-shape", default="",
                     help="--kernel-only: launch shape instead of the autotuned one, 'separable,ROWS,THREAD_ROWS,ZCHUNK' "
                          "or 'tiles,TILE_X,ZCHUNK'")
@@ -618,6 +620,8 @@ def run_ours(args):
                               "L1_max_K": chk["L1_max_K"], "L2_max_K": chk["L2_max_K"],
                               "L3_peak_K": chk["L3_peak_K"],
                               "what": "same steps from the same start in FP32 and FP64 on this GPU"}
+    if args.surrogate_steps > 0 and ws == 1:
+        line["surrogate"] = surrogate_block(args, cfg, dev, t_ms / args.steps / N2)
     if not args.no_cpu_baseline and ws == 1:
         v, secs, n, cores = oracle_parallel(args.cpu_steps, 1)
         line["cpu_baseline"] = {"value": v, "unit": "mm/s", "cores": cores, "kind": "port",
@@ -629,6 +633,61 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def surrogate_block(args, cfg, dev, plain_ms_per_l2):
+    """The Level-3 surrogate beside the plain path (the headline metric names
+    both): snapshots of batched single-track instances, a short BF16 training
+    on the device, then on the part-scale raster per Level-2 step the
+    prediction against the plain result (max / RMS error, energy-balance
+    residual with the 1 % acceptance test) and the time of one prediction on
+    the 160 x 160 x 40 grid against the plain path's time per Level-2 step of
+    this run."""
+    import numpy as np
+    import torch
+
+    import surrogate
+    import surrogate_run as SR
+    import workloads
+
+    t0 = time.perf_counter()
+    inst = workloads.batched_instances(n=16)
+    snaps, t_gen = SR.generate(inst, dev, cap=4000)
+    net = surrogate.UNet(dev, seed=0)
+    losses, t_train = SR.train(net, snaps, [81, 81, 21], (80, 80, 20), args.surrogate_steps, 4, 1e-3, dev)
+    st = SR.evaluate(net, cfg, dev, nsteps=2)
+    X, Y, Z = 160, 160, 40
+    x = torch.zeros(X * Y * Z, 16, dtype=torch.bfloat16, device=dev)
+    for _ in range(3):
+        net.forward(x, (1, X, Y, Z))
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(10):
+        net.forward(x, (1, X, Y, Z))
+    e.record()
+    torch.cuda.synchronize()
+    t_inf = s.elapsed_time(e) / 10
+    fl = net.flops((1, X, Y, Z))
+    try:
+        with open(PEAKS_FILE) as f:
+            pk = float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        pk = 1900.0
+    med = lambda v: float(np.median(v)) if len(v) else None  # noqa: E731
+    return {
+        "what": "Level-3 surrogate per Level-2 step on the part-scale raster (plain subcycle as fallback)",
+        "train": {"snapshots": snaps.n, "instances": len(inst), "steps": args.surrogate_steps, "batch": 4,
+                  "seconds": t_train, "loss_last": losses[-1][1] if losses else None},
+        "eval_level2_steps": st["total"], "accepted_frac": st["accepted"] / max(st["total"], 1),
+        "max_err_K_median": med(st["max_err"]), "rms_err_K_median": med(st["rms_err"]),
+        "energy_residual_median": med(st["residual"]),
+        "prediction_ms": t_inf, "plain_ms_per_level2_step": plain_ms_per_l2,
+        "speed_vs_plain": plain_ms_per_l2 / t_inf,
+        "inference_tflops": fl / (t_inf * 1e-3) / 1e12, "bf16_peak_tflops": pk,
+        "inference_frac_of_peak": fl / (t_inf * 1e-3) / 1e12 / pk,
+        "conv_kernel": "tcgen05.mma + TMA (gm_unet_conv3_tc)", "block_seconds": time.perf_counter() - t0,
+    }
 
 
 def parity_sample(cfg, P, nm, rows, nsteps, Tref, dev, dtype):
