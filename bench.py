@@ -276,13 +276,28 @@ def oracle_sample(cfg, rows, nsteps, warm=1, keep=False):
     return mm / dt, dt, nsteps
 
 
+def sample_rows(cfg, rows, start):
+    """Toolpath rows from `start` translated in x, y so that the first one is
+    at the centre of the set-up Level-3 window (the CPU samples and the parity
+    check step the window from its set-up position: the laser must be inside
+    it for the sample to heat anything)."""
+    import numpy as np
+
+    r = np.array(rows[start:], dtype=np.float64)
+    c = np.asarray(cfg["properties"]["laser_center"], dtype=np.float64)
+    r[:, 0] += c[0] - r[0, 0]
+    r[:, 1] += c[1] - r[0, 1]
+    return r
+
+
 def _oracle_worker(job):
     start, nsteps, warm = job
     cfg, P, nm, rows = workload()
+    rs = sample_rows(cfg, rows, start)
     if start == 0:  # the first worker's field is kept for the parity check
-        v, secs, n, T = oracle_sample(cfg, rows[start:], nsteps, warm=warm, keep=True)
+        v, secs, n, T = oracle_sample(cfg, rs, nsteps, warm=warm, keep=True)
         return v * secs, secs, n, T
-    v, secs, n = oracle_sample(cfg, rows[start:], nsteps, warm=warm)
+    v, secs, n = oracle_sample(cfg, rs, nsteps, warm=warm)
     return v * secs, secs, n, None
 
 
@@ -708,7 +723,7 @@ def parity_sample(cfg, P, nm, rows, nsteps, Tref, dev, dtype):
         ring = eng._ring(3, eng.T[2], eng.T[2])
         Ta, Tb = eng.T[3].clone(), torch.empty_like(eng.T[3])
         pa, pb = eng.ph[3].clone(), torch.empty_like(eng.ph[3])
-        rd = torch.as_tensor(rows[:nsteps], device=dev)
+        rd = torch.as_tensor(sample_rows(cfg, rows, 0)[:nsteps], device=dev)
         for i in range(nsteps):
             eng._level(3, Ta, Tb, rd[i, 5:6], pa, pb, laser=rd[i], ring=ring, alpha=1.0)
             Ta, Tb, pa, pb = Tb, Ta, pb, pa
@@ -716,7 +731,8 @@ def parity_sample(cfg, P, nm, rows, nsteps, Tref, dev, dtype):
     got = Ta.double().cpu().numpy()
     ref = np.asarray(Tref, dtype=float)
     err = float(np.max(np.abs(got - ref)))
-    return {"what": f"part-scale Level-3 window, {nsteps} fine steps from rest along the raster: GPU "
+    return {"what": f"part-scale Level-3 window, {nsteps} fine steps from rest, laser from the window centre along "
+                    f"the raster: GPU "
                     f"{'FP32' if dtype == torch.float32 else 'FP64'} against the NumPy FP64 oracle",
             "max_abs_K": err, "max_rel": err / float(np.max(np.abs(ref))), "oracle_peak_K": float(np.max(ref)),
             "bar": 1e-4}
