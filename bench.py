@@ -44,6 +44,7 @@ WORKLOAD_NAME = ("part-scale raster, L1 200x200x50 @100um, L2 100x100x15 @20um, 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_FILE = os.path.join(ROOT, "profiles", "level_sep_l3_part_scale.txt")
 PERSIST_PROFILE = os.path.join(ROOT, "profiles", "level3_persist_part_scale.txt")
+STEPS_PROFILE = os.path.join(ROOT, "profiles", "level3_steps_part_scale.txt")
 
 
 def parse_args():
@@ -76,8 +77,9 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
-    ap.add_argument("--persist", action="store_true",
-                    help="the persistent Level-3 kernel (N3 fine steps a launch) instead of one launch a fine step")
+    ap.add_argument("--persist", type=int, default=None, choices=[0, 1, 2],
+                    help="a Level-2 step's Level-3 steps as one launch: 0 one launch a step, 1 window in shared "
+                         "memory, 2 one-step body with grid barriers (default: the engine's default)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the library's untuned launch shapes (for ncu launch lists: timings under ncu would "
                          "steer the autotuner)")
@@ -398,6 +400,56 @@ def persist_launcher(eng, chunk_rows, accum=False, nsteps=None):
     return launch, N3
 
 
+def steps_launcher(eng, chunk_rows, nlaunch, accum=False, nsteps=None):
+    """The N3 Level-3 steps of a Level-2 step as one cooperative launch of
+    the one-step kernel's body with grid barriers (gm_level3_steps), on the
+    engine's window as the subcycle launches it.  Launch i uses its own
+    zeroed barrier counter (nlaunch of them).  Returns launch(i) -> None and
+    the number of fine steps a launch runs; writes only scratch outputs."""
+    import ctypes as C
+
+    import torch
+
+    import _native as N
+    import kern
+
+    L3 = eng.geo.L[3]
+    N3 = nsteps or eng.N3
+    nn = L3.nn
+    dev = eng.dev
+    rows_d = torch.as_tensor(chunk_rows[:N3], device=dev).contiguous()
+    Lw = int(sum(L3.nodes))
+    tab = torch.empty(N3 * Lw, dtype=eng.dtype, device=dev)
+    N.call("gm_fine_source_tables", kern.dtype_code(tab), (C.c_int * 3)(*L3.nodes), (C.c_double * 3)(*L3.origin()),
+           (C.c_double * 3)(*L3.spacing()), rows_d.data_ptr(), N3, C.byref(eng.ps), tab.data_ptr(),
+           kern.stream_ptr(eng.stream))
+    ring = eng._ring(3, eng.T[2], eng.T[2])
+    keep = dict(rows=rows_d, tab=tab, ring=ring, ctr=torch.zeros(nlaunch, dtype=torch.int32, device=dev),
+                tb=[torch.empty(nn, dtype=eng.dtype, device=dev) for _ in range(2)],
+                Tout=torch.empty_like(eng.T[3]), pout=torch.empty_like(eng.ph[3]),
+                acc=torch.zeros(nn, dtype=eng.dtype, device=dev), macc=torch.zeros(nn, dtype=eng.dtype, device=dev),
+                status=torch.zeros(1, dtype=torch.int32, device=dev))
+    kw = eng.level_kwargs(3, eng.T[3], keep["Tout"], rows_d[0, 5:6], eng.ph[3], keep["pout"], laser=rows_d[0],
+                          ring=ring, alpha=1.0 / N3)
+    if accum:
+        kw.update(accum=keep["acc"], max_accum=keep["macc"])
+    kw["src_tab"] = tab  # launch shape: the autotuned one-step shape of this window
+    a = N.gm_steps_args()
+    a.level = kern.level_args(**kw)
+    a.nsteps, a.nsub = N3, N3
+    a.rows, a.src_tab = rows_d.data_ptr(), tab.data_ptr()
+    a.tbuf[0], a.tbuf[1] = keep["tb"][0].data_ptr(), keep["tb"][1].data_ptr()
+    a.status = keep["status"].data_ptr()
+    ctr = keep["ctr"].data_ptr()
+
+    def launch(i):
+        a.counter, a.base = ctr + 4 * i, 0
+        N.call("gm_level3_steps", C.byref(a), C.byref(eng.ps), kern.stream_ptr(eng.stream))
+
+    launch.keep = keep
+    return launch, N3
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -433,8 +485,9 @@ def run_ours(args):
         eng.move(rows[0], vstart)
         tuned = {} if args.no_autotune else eng.autotune(rows[0])  # launch shapes, measured (set-up, untimed)
         eng.use_graph = not args.no_graph  # each subcycle call as one CUDA graph
-        eng.use_persist = args.persist
-        persist = eng.use_persist and eng.persist_shape() is not None
+        if args.persist is not None:
+            eng.use_persist = args.persist
+        persist = int(eng.use_persist) if (int(eng.use_persist) != 1 or eng.persist_shape() is not None) else 0
         # toolpath rows generated on the device (FP64 accumulation) from the run table
         tp = engine.DeviceToolpath(runs, dev, stream)
         rows_buf = torch.empty(n23 * 7, dtype=torch.float64, device=dev)
@@ -562,28 +615,37 @@ def run_ours(args):
             t = s.elapsed_time(e) / reps
             k1_ms = t if k1_ms is None else min(k1_ms, t)
         del graph
-        # persistent kernel: N3 fine steps a launch, launches back to back
-        kp_ms = None
-        if eng.persist_shape() is not None:
-            launch, nper = persist_launcher(eng, last_chunk)
+        # the two multi-step Level-3 launches, N3 fine steps a launch, launches back to back
+        preps = 10
+
+        def time_launches(launch, status, first):
             for b in range(3):
-                launch(b * nper)
-            base = 3 * nper
+                launch(first + b)
             torch.cuda.synchronize()
-            preps = 10
+            i, best = first + 3, None
             for _ in range(3):
                 flush.zero_()
                 s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 s.record(stream)
                 for _ in range(preps):
-                    launch(base)
-                    base += nper
+                    launch(i)
+                    i += 1
                 e.record(stream)
                 torch.cuda.synchronize()
                 t = s.elapsed_time(e) / preps
-                kp_ms = t if kp_ms is None else min(kp_ms, t)
-            if int(launch.keep["status"].item()) != 0:
-                raise SystemExit("persistent Level-3 kernel reported a failure")
+                best = t if best is None else min(best, t)
+            if int(status.item()) != 0:
+                raise SystemExit("multi-step Level-3 kernel reported a failure")
+            return best
+
+        kp_ms = ks_ms = None
+        if eng.persist_shape() is not None:
+            launch, nper = persist_launcher(eng, last_chunk)
+            kp_ms = time_launches(lambda i: launch(i * nper), launch.keep["status"], 0)
+            del launch
+        launch, nper = steps_launcher(eng, last_chunk, 3 + 3 * preps)
+        ks_ms = time_launches(launch, launch.keep["status"], 0)
+        del launch
 
     t_ms, e2e_ms, mm, mm_e2e = combine_ranks(t_ms, e2e_ms, mm, mm_e2e, dev)
     if rank != 0:
@@ -591,12 +653,18 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     peak, peak_kind = measured_peak()
-    if persist:
+    if persist == 1:
         alg_bytes = 10.0 * L3.nn * N3
         k_ms = kp_ms
         kname = f"level3_persist_kernel (Level 3, {N3} fine steps a launch, window in shared memory)"
         traffic = profile_traffic(PERSIST_PROFILE)
         tsrc = "profiles/level3_persist_part_scale.txt (ncu capture of this workload, not of this run)"
+    elif persist == 2:
+        alg_bytes = 10.0 * L3.nn * N3
+        k_ms = ks_ms
+        kname = f"level_sep_steps_kernel (Level 3, {N3} fine steps a launch, grid barriers)"
+        traffic = profile_traffic(STEPS_PROFILE)
+        tsrc = "profiles/level3_steps_part_scale.txt (ncu capture of this workload, not of this run)"
     else:
         alg_bytes = 10.0 * L3.nn
         k_ms = k1_ms
@@ -621,7 +689,10 @@ def run_ours(args):
                                          "frac": 10.0 * L3.nn / (k1_ms * 1e-3) / 1e9 / peak},
                      "persistent_kernel": None if kp_ms is None else {
                          "kernel": f"level3_persist_kernel ({N3} fine steps a launch)", "ms_per_launch": kp_ms,
-                         "ms_per_fine_step": kp_ms / N3, "frac": 10.0 * L3.nn * N3 / (kp_ms * 1e-3) / 1e9 / peak}},
+                         "ms_per_fine_step": kp_ms / N3, "frac": 10.0 * L3.nn * N3 / (kp_ms * 1e-3) / 1e9 / peak},
+                     "grid_steps_kernel": {
+                         "kernel": f"level_sep_steps_kernel ({N3} fine steps a launch)", "ms_per_launch": ks_ms,
+                         "ms_per_fine_step": ks_ms / N3, "frac": 10.0 * L3.nn * N3 / (ks_ms * 1e-3) / 1e9 / peak}},
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
         "level3_persistent": persist,
@@ -1066,13 +1137,18 @@ def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
     nsteps = lambda e: 2 * e.N2 * e.N3 * e.geo.L[3].nn + 2 * e.N2 * e.geo.L[2].nn + 2 * e.geo.L[1].nn  # noqa: E731
     node_steps = sum(nsteps(e) for e in engs)
     for e in engs:
-        e.use_persist = False
+        e.use_persist = 0
         e.use_graph = True
     out = {"instances": len(engs), "steps": K, "node_steps_per_step": node_steps}
-    k = first_chunk
+    nchunk = min(len(r) // 100 for r in rows)  # the shortest toolpath: later steps start over from first_chunk
+    if nchunk <= first_chunk:
+        raise SystemExit(f"toolpath too short for the batched subcycles: {nchunk} Level-1 steps")
+    i = 0
     for mode in ("per_instance", "batched", "per_instance", "batched"):  # the first pair warms up
         t_gpu, t_wall, dist = 0.0, 0.0, 0.0
         for _ in range(K):
+            k = first_chunk + i % (nchunk - first_chunk)
+            i += 1
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             with torch.cuda.stream(stream):
@@ -1090,7 +1166,6 @@ def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
             t_wall += time.perf_counter() - t0
             t_gpu += s.elapsed_time(e_) * 1e-3
             dist += mm(k)
-            k += 1
         out[mode] = {"subcycle_gpu_ms_per_step": 1e3 * t_gpu / K, "wall_ms_per_step": 1e3 * t_wall / K,
                      "scan_mm_per_s_wall": dist / t_wall, "scan_mm_per_s_subcycle_gpu": dist / t_gpu,
                      "gnode_steps_per_s_subcycle_gpu": node_steps * K / t_gpu / 1e9}
@@ -1160,23 +1235,31 @@ def run_kernel_only(args):
     for k in range(args.warmup):
         eng.move(rows[k * n23], vstart)
         eng.subcycle(rows[k * n23:(k + 1) * n23])
-    if args.persist_only:  # the persistent Level-3 kernel: --steps launches of N3 fine steps
+    if args.persist_only:  # a multi-step Level-3 kernel (--persist 1 or 2): --steps launches of N3 fine steps
         eng.autotune(rows[0])
-        launch, nper = persist_launcher(eng, rows[(args.warmup - 1) * n23:args.warmup * n23], accum=args.l3_accum,
-                                        nsteps=args.persist_steps or None)
+        chunk = rows[(args.warmup - 1) * n23:args.warmup * n23]
+        if args.persist == 2:
+            launch, nper = steps_launcher(eng, chunk, args.steps, accum=args.l3_accum,
+                                          nsteps=args.persist_steps or None)
+            name, shape = "level_sep_steps_kernel", None
+        else:
+            pl, nper = persist_launcher(eng, chunk, accum=args.l3_accum, nsteps=args.persist_steps or None)
+            launch = lambda i: pl(i * nper)  # noqa: E731
+            launch.keep = pl.keep
+            name, shape = "level3_persist_kernel", eng.persist_shape()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(eng.stream)
         for i in range(args.steps):
-            launch(i * nper)
+            launch(i)
         e1.record(eng.stream)
         torch.cuda.synchronize()
         st = int(launch.keep["status"].item())
-        print(json.dumps({"kernel_only": "level3_persist_kernel", "launches": args.steps, "fine_steps": nper,
-                          "nodes": eng.geo.L[3].nn, "shape": eng.persist_shape(), "status": st,
+        print(json.dumps({"kernel_only": name, "launches": args.steps, "fine_steps": nper,
+                          "nodes": eng.geo.L[3].nn, "shape": shape, "status": st,
                           "us_per_launch": 1000 * e0.elapsed_time(e1) / args.steps}))
         if st:
-            raise SystemExit("persistent kernel status %d" % st)
+            raise SystemExit("multi-step kernel status %d" % st)
         return
     if args.l3_shape:  # e.g. "separable,4,2,6" (rows, thread rows, z-chunk) or "tiles,32,14"
         f = args.l3_shape.split(",")

@@ -199,6 +199,11 @@ class gm_persist_args(C.Structure):
 GM_PERSIST_TIMEOUT, GM_PERSIST_BAD_T = 1, 2
 
 
+class gm_steps_args(C.Structure):
+    _fields_ = [("level", gm_level_args), ("nsteps", C.c_int), ("nsub", C.c_int), ("rows", vp), ("src_tab", vp),
+                ("tbuf", vp * 2), ("counter", vp), ("base", C.c_uint), ("status", vp)]
+
+
 class gm_toolpath_state(C.Structure):
     _fields_ = [("run", C.c_longlong), ("k", C.c_longlong), ("row", C.c_longlong), ("x", C.c_double),
                 ("y", C.c_double), ("t", C.c_double)]
@@ -264,6 +269,7 @@ def lib():
 SIGNATURES = {
     "gm_level_step": [C.POINTER(gm_level_args), C.POINTER(gm_props), vp],
     "gm_level3_persist": [C.POINTER(gm_persist_args), C.POINTER(gm_props), vp],
+    "gm_level3_steps": [C.POINTER(gm_steps_args), C.POINTER(gm_props), vp],
     "gm_toolpath_rows": [vp, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp],
     "gm_l0_fill": [vp, C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong, C.c_longlong, C.c_int, vp],
     "gm_level3_persist_shape": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)],

@@ -18,6 +18,20 @@ namespace gm {
 constexpr uint8_t PH_S1 = 1;
 constexpr uint8_t PH_S2 = 2;
 
+// Arithmetic whose rounding is fixed by the source: the compiler neither
+// fuses these products and sums into multiply-adds nor splits the explicit
+// multiply-adds, whichever kernel inlines them.  Kernels that must give the
+// same bits as one another (the one-step, batched and multi-step Level-3
+// kernels) write their stencil with these.
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 template <typename real>
 struct Props {
   real k_powder, k_bulk_a0, k_bulk_a1, k_fluid;  // W/(mm K)  (already /1000)
@@ -152,12 +166,12 @@ __device__ __forceinline__ real src_factor(int i, int n, real rel, real h, real 
   real s = 0;
   for (int e = i - 1; e <= i; ++e) {
     if (e < 0 || e >= n - 1) continue;
-    const real d0 = rel + h * ((real)e + g0);
-    const real d1 = rel + h * ((real)e + g1);
-    const real q0 = exp((real)-3 * d0 * d0 * inv_r2);
-    const real q1 = exp((real)-3 * d1 * d1 * inv_r2);
+    const real d0 = rfma(h, radd((real)e, g0), rel);
+    const real d1 = rfma(h, radd((real)e, g1), rel);
+    const real q0 = exp(rmul(rmul((real)-3 * d0, d0), inv_r2));
+    const real q1 = exp(rmul(rmul((real)-3 * d1, d1), inv_r2));
     // node i is local node 0 of element e when i == e: weights (1-xi)/2 = g1 at xi=-1/sqrt3, g0 at +1/sqrt3
-    s += (i == e) ? (g1 * q0 + g0 * q1) : (g0 * q0 + g1 * q1);
+    s = radd(s, (i == e) ? rfma(g1, q0, rmul(g0, q1)) : rfma(g0, q0, rmul(g1, q1)));
   }
   return s;
 }
@@ -166,17 +180,18 @@ __device__ __forceinline__ real src_factor(int i, int n, real rel, real h, real 
 // (computeConvRadBC, go_melt/computeFunctions.py:2263-2290).
 template <typename real>
 __device__ __forceinline__ real surface_flux(const Props<real>& p, real Tq) {
-  Tq = fmin(Tq, p.T_boiling + (real)1000);
-  const real T2 = Tq * Tq;
-  real q = p.h_conv * (p.T_amb - Tq) + p.sig_eps * (p.Ta4 - T2 * T2);
+  Tq = fmin(Tq, radd(p.T_boiling, (real)1000));
+  const real T2 = rmul(Tq, Tq);
+  real q = rfma(p.h_conv, rsub(p.T_amb, Tq), rmul(p.sig_eps, rfma(-T2, T2, p.Ta4)));
   if (p.evc != (real)0) {
     const real invT = (real)1 / Tq;
-    const real E_pv = p.Lev + p.cp_fluid * (Tq - p.T_amb);
-    const real MolMot = sqrt(p.CM * invT);
-    const real S = p.evc * p.CP * exp(-p.CT * (invT - (real)1 / p.T_boiling)) * MolMot * E_pv;
-    q -= S;
+    const real E_pv = rfma(p.cp_fluid, rsub(Tq, p.T_amb), p.Lev);
+    const real MolMot = sqrt(rmul(p.CM, invT));
+    const real S = rmul(rmul(rmul(rmul(p.evc, p.CP), exp(rmul(-p.CT, rsub(invT, (real)1 / p.T_boiling)))), MolMot),
+                        E_pv);
+    q = rsub(q, S);
   }
-  return q * (real)1e-6;
+  return rmul(q, (real)1e-6);
 }
 
 // Per-axis interpolation map: target index t -> source element e[t] with the

@@ -31,8 +31,9 @@ struct Ctx {
   void* st;
   size_t esz;
   int rc = GM_OK;
-  bool persist = false;   // Level-3 steps of a Level-2 step as one persistent launch
-  unsigned pbase = 0;     // flag value at the next persistent launch
+  int persist = 0;        // Level-3 steps of a Level-2 step as one launch: 1 tiles in shared memory, 2 grid steps
+  unsigned pbase = 0;     // flag value at the next persistent launch (mode 1)
+  int plaunch = 0;        // persistent launches issued in this call (mode 2: counter index)
 };
 
 inline char* at(void* base, long long elems, size_t esz) { return (char*)base + elems * (long long)esz; }
@@ -46,10 +47,10 @@ inline long long nn(const gm_window& w) { return (long long)w.nodes[0] * w.nodes
     }                            \
   } while (0)
 
-void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tout, const double* dt,
-           const uint8_t* phin, uint8_t* phout, const void* rhs, const int lo[3], const int n[3],
-           const double* laser, int bc_mode, const gm_map3* map, const void* bnew, const void* bold, double alpha,
-           void* acc, void* macc, const void* src_tab = nullptr) {
+gm_level_args level_args(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tout, const double* dt,
+                         const uint8_t* phin, uint8_t* phout, const void* rhs, const int lo[3], const int n[3],
+                         const double* laser, int bc_mode, const gm_map3* map, const void* bnew, const void* bold,
+                         double alpha, void* acc, void* macc, const void* src_tab) {
   const gm_subcycle_plan& p = *c.p;
   gm_level_args a;
   memset(&a, 0, sizeof(a));
@@ -94,6 +95,15 @@ void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tou
   a.zchunk = p.zchunk;
   a.pdl = p.pdl;  // dt, the laser row and its factor table are never written by the kernels before it
   a.src_tab = src_tab;
+  return a;
+}
+
+void level(Ctx& c, const gm_window& w, int ne_planes, const void* Tin, void* Tout, const double* dt,
+           const uint8_t* phin, uint8_t* phout, const void* rhs, const int lo[3], const int n[3],
+           const double* laser, int bc_mode, const gm_map3* map, const void* bnew, const void* bold, double alpha,
+           void* acc, void* macc, const void* src_tab = nullptr) {
+  const gm_level_args a = level_args(c, w, ne_planes, Tin, Tout, dt, phin, phout, rhs, lo, n, laser, bc_mode, map,
+                                     bnew, bold, alpha, acc, macc, src_tab);
   GM_TRY(gm_level_step(&a, c.pr, c.st));
 }
 
@@ -250,7 +260,29 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
     level(c, p.L2, p.L2.nodes[2] - 1, T2c, T2n, dt2, ph2c, ph2n, p.rhs2, p.rhs2_lo, p.rhs2_n, nullptr, 3, nullptr,
           p.ring2[0], p.ring2[1], (l2 + 1) / (double)N2, nullptr, nullptr);
     ring(c, p.L3, p.bc23, T2n, T2c, p.ring3[0], p.ring3[1]);
-    if (c.persist) {  // all N3 fine steps in one launch
+    if (c.persist == 2) {  // all N3 fine steps in one launch of the one-step kernel's body, grid barriers
+      const int i0 = l2 * N3;
+      const long long L3n = (long long)p.L3.nodes[0] + p.L3.nodes[1] + p.L3.nodes[2];
+      gm_steps_args sa;
+      memset(&sa, 0, sizeof(sa));
+      sa.level = level_args(c, p.L3, p.L3.nodes[2] - 1, T3c, p.T3w[l2 % 2], p.rows + (long long)i0 * 7 + 5, ph3c,
+                            p.ph3w[l2 % 2], nullptr, nullptr, nullptr, p.rows + (long long)i0 * 7, 3, nullptr,
+                            p.ring3[0], p.ring3[1], 1.0 / N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr,
+                            at(p.src3tab, i0 * L3n, c.esz));
+      sa.level.pdl = 0;
+      sa.nsteps = N3;
+      sa.nsub = N3;
+      sa.rows = p.rows + (long long)i0 * 7;
+      sa.src_tab = at(p.src3tab, i0 * L3n, c.esz);
+      sa.tbuf[0] = p.xch3[0];
+      sa.tbuf[1] = p.xch3[1];
+      sa.counter = p.pflags + c.plaunch++;
+      sa.base = 0;
+      sa.status = p.pstatus;
+      GM_TRY(gm_level3_steps(&sa, c.pr, c.st));
+      T3c = sa.level.T_out;
+      ph3c = sa.level.ph_out;
+    } else if (c.persist == 1) {  // all N3 fine steps in one launch
       const int i0 = l2 * N3;
       const long long L3n = (long long)p.L3.nodes[0] + p.L3.nodes[1] + p.L3.nodes[2];
       gm_persist_args a;
@@ -284,7 +316,7 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
       T3c = a.T_out;
       ph3c = a.ph_out;
     }
-    for (int l3 = 0; l3 < (c.persist ? 0 : N3); ++l3) {
+    for (int l3 = 0; l3 < (c.persist ? 0 : N3); ++l3) {  // one launch a fine step
       const int i = l2 * N3 + l3;
       void* Tn = p.T3w[i % 2];
       uint8_t* phn = p.ph3w[i % 2];
@@ -347,13 +379,19 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   // persistent Level-3 steps: needs the factor table, the work buffers and a
   // constant-property material; the window must have a persistent shape
   if (p->persist && p->src3tab && p->xch3[0] && p->xch3[1] && p->pflags && p->pstatus) {
-    int shp[4];
-    const long long nf = gm_level3_persist_flags(p->L3.nodes);
-    c.persist = nf > 0 && nf <= p->pflags_cap && gm_level3_persist_shape(p->dtype, p->L3.nodes, shp) == GM_OK &&
-                props->k_powder == props->k_bulk_a0 && props->k_fluid == props->k_bulk_a0 &&
-                props->k_bulk_a1 == 0.0 && props->cp_solid_a1 == 0.0 && props->cp_mushy == props->cp_solid_a0 &&
-                props->cp_fluid == props->cp_solid_a0;
-    if (c.persist && cudaMemsetAsync(p->pflags, 0, sizeof(unsigned) * nf, (cudaStream_t)stream) != cudaSuccess)
+    const bool kconst = props->k_powder == props->k_bulk_a0 && props->k_fluid == props->k_bulk_a0 &&
+                        props->k_bulk_a1 == 0.0 && props->cp_solid_a1 == 0.0 &&
+                        props->cp_mushy == props->cp_solid_a0 && props->cp_fluid == props->cp_solid_a0;
+    if (p->persist == 1) {
+      int shp[4];
+      const long long nf = gm_level3_persist_flags(p->L3.nodes);
+      c.persist = (nf > 0 && nf <= p->pflags_cap && gm_level3_persist_shape(p->dtype, p->L3.nodes, shp) == GM_OK &&
+                   kconst) ? 1 : 0;
+    } else if (p->persist == 2) {
+      c.persist = (kconst && p->pflags_cap >= 2LL * p->N2) ? 2 : 0;  // a barrier counter per launch
+    }
+    if (c.persist &&
+        cudaMemsetAsync(p->pflags, 0, sizeof(unsigned) * p->pflags_cap, (cudaStream_t)stream) != cudaSuccess)
       return GM_ERR_CUDA;
   }
   // every later kernel of the call launches as a programmatic dependent of the one before it

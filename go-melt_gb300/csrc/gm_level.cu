@@ -602,7 +602,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
         const bool prev2 = (ph & PH_S2) != 0;
         const real racc = prev2 ? (real)0 : cAcc;
         a.max_accum[id] = fmax(racc, cMacc);
-        a.accum[id] = (cAcc + dt) - racc;
+        a.accum[id] = rsub(radd(cAcc, dt), racc);
       }
     }
   };
@@ -653,7 +653,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
           if (rx == nx - 1) Tn = a.face[1];
         }
       } else {
-        Tn = a.bc_alpha * a.bc_new[id] + a.bc_beta * a.bc_old[id];
+        Tn = rfma(a.bc_alpha, a.bc_new[id], rmul(a.bc_beta, a.bc_old[id]));
       }
       const real Told = needPh ? a.T_in[id] : (real)0;
       const bool liq = hAcc && Told >= P.T_liquidus;
@@ -680,16 +680,16 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     const real sx = xin ? tb[x] : (real)0;
     const real syl = (lane < BYT && y0 + lane < ny) ? tb[nx + y0 + lane] : (real)0;
 #pragma unroll
-    for (int r = 0; r < BYT; ++r) sxy[r] = sx * __shfl_sync(FULL, syl, r);
+    for (int r = 0; r < BYT; ++r) sxy[r] = rmul(sx, __shfl_sync(FULL, syl, r));
     if (Z0 + lane < Z1) szl = tb[nx + ny + Z0 + lane];
   } else if (hLaser) {
     const real rx = s_in[1], ry = s_in[2], rz = s_in[3], srcP = s_in[4];
-    const real sx = xin ? srcP * src_factor<real>(x, nx, rx, a.rh[0], a.rir2) : (real)0;
+    const real sx = xin ? rmul(srcP, src_factor<real>(x, nx, rx, a.rh[0], a.rir2)) : (real)0;
     // lane r < BYT evaluates the y factor of row y0 + r for the whole warp
     const real syl =
         (lane < BYT && y0 + lane < ny) ? src_factor<real>(y0 + lane, ny, ry, a.rh[1], a.rir2) : (real)0;
 #pragma unroll
-    for (int r = 0; r < BYT; ++r) sxy[r] = sx * __shfl_sync(FULL, syl, r);
+    for (int r = 0; r < BYT; ++r) sxy[r] = rmul(sx, __shfl_sync(FULL, syl, r));
     if (Z0 + lane < Z1) szl = src_factor<real>(Z0 + lane, nz, rz, a.rh[2], a.rid2);
   }
   // every read and write of a field comes after the preceding grid completed
@@ -799,33 +799,33 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
 #pragma unroll
     for (int i = 0; i < RY; ++i) {
       if (TOP) {
-        Zm[i] = Tm.v[i] + (real)2 * T0.v[i];
-        Zk[i] = T0.v[i] - Tm.v[i];
+        Zm[i] = rfma((real)2, T0.v[i], Tm.v[i]);
+        Zk[i] = rsub(T0.v[i], Tm.v[i]);
       } else {
-        const real s = Tm.v[i] + Tp.v[i];
-        Zm[i] = s + (real)4 * T0.v[i];
-        Zk[i] = (real)2 * T0.v[i] - s;
+        const real s = radd(Tm.v[i], Tp.v[i]);
+        Zm[i] = rfma((real)4, T0.v[i], s);
+        Zk[i] = rfma((real)2, T0.v[i], -s);
       }
     }
     const real mi = TOP ? (real)2 * minv : minv;
 #pragma unroll
     for (int r = 0; r < BYT; ++r) {
       const int i = r + 1;
-      const real u = Zm[i - 1] + Zm[i + 1];
-      const real w = Zk[i - 1] + Zk[i + 1];
-      const real A = a1 * (u + (real)4 * Zm[i]);
-      const real B = b1 * ((real)2 * Zm[i] - u) + b2 * (w + (real)4 * Zk[i]);
+      const real u = radd(Zm[i - 1], Zm[i + 1]);
+      const real w = radd(Zk[i - 1], Zk[i + 1]);
+      const real A = rmul(a1, rfma((real)4, Zm[i], u));
+      const real B = rfma(b1, rfma((real)2, Zm[i], -u), rmul(b2, rfma((real)4, Zk[i], w)));
       // x stencil: (2A - A(x-1) - A(x+1)) + (B(x-1) + 4B + B(x+1)) = 2A + 4B + D(x-1) + D(x+1), D = B - A
-      const real D = B - A;
+      const real D = rsub(B, A);
       const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
       if (!row_out[r] || (!TOP && hInact && p == ntop)) continue;
-      const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
+      const real KT = radd(rfma((real)2, A, rmul((real)4, B)), radd(Dl, Dr));
       const real Told = T0.v[i];
       real Rt = -KT;
-      if (hLaser) Rt += sxy[r] * sz;
-      if (hBox) Rt += rhs.v[r];
-      if (TOP && hSurf) Rt += surf.v[r];
-      real Tn = Told + Rt * mi;
+      if (hLaser) Rt = rfma(sxy[r], sz, Rt);
+      if (hBox) Rt = radd(Rt, rhs.v[r]);
+      if (TOP && hSurf) Rt = radd(Rt, surf.v[r]);
+      real Tn = rfma(Rt, mi, Told);
       if (!TOP && hInact && p > ntop) Tn = P.T_amb;
       finish(x + (y0 + r) * nx + p * nxy, Tn, Told, ph.v[r], acc.v[r], mac.v[r]);
     }
@@ -1616,6 +1616,173 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
   return GM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The N3 Level-3 steps of one Level-2 step in one cooperative launch, each
+// step the separable one-step kernel's body over its tiles (so results are
+// the one-step kernel's, bit for bit), the fields in L2 between steps, a grid
+// barrier between steps.  It removes the launch ramp and drain of N3 - 1
+// launches; the barrier costs one L2 round trip per CTA and step.
+// ---------------------------------------------------------------------------
+namespace gm {
+
+struct StepsK {
+  int nsteps, nsub, tiles, gx, gy;
+  const double* rows;
+  const void* src_tab;
+  int src_stride;
+  const void* T_in;
+  void* T_out;
+  void* tb0;
+  void* tb1;
+  const uint8_t* ph_in;
+  uint8_t* ph_out;
+  unsigned* counter;
+  unsigned base;
+  int* status;
+};
+
+constexpr long long STEPS_WAIT_CYCLES = 2000000000LL;
+
+template <typename real, int BYT, int FL>
+__global__ void __launch_bounds__(256, sep_min_blocks<real, BYT>()) level_sep_steps_kernel(const LevelK<real> a0, const StepsK k) {
+  __shared__ LevelK<real> a;
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) {
+    a = a0;
+    s_abort = 0;
+  }
+  const int gz = k.tiles / (k.gx * k.gy);
+  for (int s = 0; s < k.nsteps; ++s) {
+    __syncthreads();
+    if (threadIdx.x == 0) {  // this step's inputs and outputs
+      a.T_in = (const real*)(s == 0 ? k.T_in : ((s & 1) ? k.tb0 : k.tb1));
+      a.T_out = (real*)(s == k.nsteps - 1 ? k.T_out : ((s & 1) ? k.tb1 : k.tb0));
+      a.ph_in = s == 0 ? k.ph_in : k.ph_out;  // a node's phase is read and written by its own thread only
+      a.ph_out = k.ph_out;
+      a.dt = k.rows + 7LL * s + 5;
+      a.laser = k.rows + 7LL * s;
+      a.src_tab = (const real*)k.src_tab + (long long)s * k.src_stride;
+      const double al = (double)(s + 1) / (double)k.nsub;
+      a.bc_alpha = (real)al;
+      a.bc_beta = (real)(1.0 - al);
+    }
+    __syncthreads();
+    for (int t = blockIdx.x; t < k.tiles; t += gridDim.x) {
+      const int bx = t % k.gx, by = (t / k.gx) % k.gy, bz = t / (k.gx * k.gy);
+      sep_body<real, BYT, FL>(a, bx, by, bz, k.gx, k.gy, gz - 1);
+    }
+    if (s == k.nsteps - 1) break;
+    // grid barrier: every tile of step s is written before any CTA reads it
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned target = k.base + (unsigned)((s + 1) * gridDim.x);
+      asm volatile("fence.acq_rel.gpu;\n red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(k.counter) : "memory");
+      const long long t0 = clock64();
+      unsigned v;
+      for (;;) {
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(k.counter) : "memory");
+        if ((int)(v - target) >= 0) break;
+        if (clock64() - t0 > STEPS_WAIT_CYCLES) {
+          s_abort = 1;
+          atomicOr(k.status, GM_PERSIST_TIMEOUT);
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    if (s_abort) return;
+  }
+}
+
+template <typename real, int BYT, int FL>
+static int launch_steps_t(const LevelK<real>& a, StepsK k, int warps, cudaStream_t st) {
+  auto kern = level_sep_steps_kernel<real, BYT, FL>;
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 152;
+  }
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * warps, 0) != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    return GM_ERR_UNSUPPORTED;
+  }
+  const int grid = k.tiles < occ * sms ? k.tiles : occ * sms;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(32 * warps);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // every CTA resident: the grid barrier cannot starve
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, a, k) == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+template <typename real>
+static int launch_steps(const gm_steps_args* g, const gm_props* pr, cudaStream_t st) {
+  const gm_level_args* la = &g->level;
+  const int fl = level_flags(la, pr);
+  if (!sep_eligible(la, fl) || (fl != (LF_L3 | LF_CONST) && fl != (LF_L3ACC | LF_CONST))) return GM_ERR_UNSUPPORTED;
+  TuneVal v;
+  if (la->zchunk > 0 || !tuned_shape(TuneKey{la->dtype, fl, la->nx, la->ny, la->nz}, &v) || v.kernel != 1)
+    v = sep_default<real>(la, false);
+  if (la->zchunk > 0) v.zchunk = la->zchunk;
+  if ((v.rows != 1 && v.rows != 2 && v.rows != 4) || v.wys < 1 || v.wys > 8 || v.zchunk < 1 || v.zchunk > SEP_ZMAX)
+    return GM_ERR_ARG;
+  LevelK<real> a = make_levelk<real>(la, pr);
+  a.zchunk = v.zchunk;
+  StepsK k;
+  k.nsteps = g->nsteps;
+  k.nsub = g->nsub;
+  k.gx = cdiv(la->nx, SEP_TILE);
+  k.gy = cdiv(la->ny, v.wys * v.rows);
+  const long long tiles =
+      (long long)k.gx * k.gy * (sep_march_chunks(la->nz, la->ne_planes, false, v.zchunk) + 2);
+  if (tiles >= (1LL << 31)) return GM_ERR_TOO_LARGE;
+  k.tiles = (int)tiles;
+  k.rows = g->rows;
+  k.src_tab = g->src_tab;
+  k.src_stride = la->nx + la->ny + la->nz;
+  k.T_in = la->T_in;
+  k.T_out = la->T_out;
+  k.tb0 = g->tbuf[0];
+  k.tb1 = g->tbuf[1];
+  k.ph_in = la->ph_in;
+  k.ph_out = la->ph_out;
+  k.counter = g->counter;
+  k.base = g->base;
+  k.status = g->status;
+  const int fa = LF_L3 | LF_CONST, fb = LF_L3ACC | LF_CONST;
+  if (v.rows == 1)
+    return fl == fa ? launch_steps_t<real, 1, fa>(a, k, v.wys, st) : launch_steps_t<real, 1, fb>(a, k, v.wys, st);
+  if (v.rows == 2)
+    return fl == fa ? launch_steps_t<real, 2, fa>(a, k, v.wys, st) : launch_steps_t<real, 2, fb>(a, k, v.wys, st);
+  return fl == fa ? launch_steps_t<real, 4, fa>(a, k, v.wys, st) : launch_steps_t<real, 4, fb>(a, k, v.wys, st);
+}
+
+}  // namespace gm
+
+extern "C" int gm_level3_steps(const gm_steps_args* g, const gm_props* p, void* stream) {
+  if (!g || !p || g->nsteps < 1 || g->nsub < 1 || !g->rows || !g->src_tab || !g->tbuf[0] || !g->tbuf[1] ||
+      !g->counter || !g->status)
+    return GM_ERR_ARG;
+  const gm_level_args* la = &g->level;
+  const int rc = gm::check_level_args(la);
+  if (rc != GM_OK) return rc;
+  if (!la->ph_in || !la->ph_out || la->bc_mode != 3 || !la->laser) return GM_ERR_ARG;
+  const void* bufs[4] = {la->T_in, la->T_out, g->tbuf[0], g->tbuf[1]};
+  for (int i = 0; i < 4; ++i)
+    for (int j = i + 1; j < 4; ++j)
+      if (bufs[i] == bufs[j]) return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (la->dtype == GM_F32) return gm::launch_steps<float>(g, p, st);
+  return gm::launch_steps<double>(g, p, st);
+}
+
 extern "C" const char* gm_version(void) { return "gomelt-gb300 0.1 (sm_103a)"; }
 
 // ---------------------------------------------------------------------------
@@ -1665,7 +1832,7 @@ __global__ void fine_source_tables_kernel(int nx, int ny, int nz, double ox, dou
     real v;
     if (j < nx) {
       const real rx = (real)(ox - laser[0]), srcP = (real)(src_c * laser[6]);
-      v = srcP * src_factor<real>(j, nx, rx, hx, ir2);
+      v = rmul(srcP, src_factor<real>(j, nx, rx, hx, ir2));
     } else if (j < nx + ny) {
       v = src_factor<real>(j - nx, ny, (real)(oy - laser[1]), hy, ir2);
     } else {

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
     const real alpha = (real)al, beta = (real)(1.0 - al);
     const real* tb = a.src_tab + (size_t)s * L;
     const real sx = xin ? tb[x] : (real)0;
-    const real sxy = sx * ((y < ny) ? tb[nx + y] : (real)0);
+    const real sxy = rmul(sx, (y < ny) ? tb[nx + y] : (real)0);
 
     // step s+1 lives in exchange field (s+1) & 1; the last step publishes nothing
     real* const xbn = s == a.nsteps - 1 ? nullptr : ((s & 1) ? a.xb0 : a.xb1);
@@ -164,12 +164,12 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
         const bool prev2 = (ph & PH_S2) != 0;
         const real racc = prev2 ? (real)0 : cAcc;
         a.max_accum[id] = fmax(racc, cMacc);
-        a.accum[id] = (cAcc + dt) - racc;
+        a.accum[id] = rsub(radd(cAcc, dt), racc);
       }
     };
     auto ring_value = [&](int p) {
       const int id = col + p * nxy;
-      return alpha * a.ringA[id] + beta * a.ringB[id];
+      return rfma(alpha, a.ringA[id], rmul(beta, a.ringB[id]));
     };
     auto at = [&](const real* b, int p, int i) { return b[(p * RYH + i) * 32 + lane]; };
 
@@ -185,14 +185,14 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
       for (int p = za; p < zb; ++p) {
         c += plane;
         const real Tp0 = c[0], Tp1 = c[32], Tp2 = c[64];
-        const real s0 = Tm0 + Tp0, s1 = Tm1 + Tp1, s2 = Tm2 + Tp2;
-        const real Zm0 = s0 + (real)4 * T00, Zm1 = s1 + (real)4 * T01, Zm2 = s2 + (real)4 * T02;
-        const real Zk0 = (real)2 * T00 - s0, Zk1 = (real)2 * T01 - s1, Zk2 = (real)2 * T02 - s2;
-        const real u = Zm0 + Zm2;
-        const real w = Zk0 + Zk2;
-        const real A = a1 * (u + (real)4 * Zm1);
-        const real B = b1 * ((real)2 * Zm1 - u) + b2 * (w + (real)4 * Zk1);
-        const real D = B - A;
+        const real s0 = radd(Tm0, Tp0), s1 = radd(Tm1, Tp1), s2 = radd(Tm2, Tp2);
+        const real Zm0 = rfma((real)4, T00, s0), Zm1 = rfma((real)4, T01, s1), Zm2 = rfma((real)4, T02, s2);
+        const real Zk0 = rfma((real)2, T00, -s0), Zk1 = rfma((real)2, T01, -s1), Zk2 = rfma((real)2, T02, -s2);
+        const real u = radd(Zm0, Zm2);
+        const real w = radd(Zk0, Zk2);
+        const real A = rmul(a1, rfma((real)4, Zm1, u));
+        const real B = rfma(b1, rfma((real)2, Zm1, -u), rmul(b2, rfma((real)4, Zk1, w)));
+        const real D = rsub(B, A);
         const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
         const real sz = __shfl_sync(FULL, szl, p - za);
         if (own) {
@@ -201,10 +201,9 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
           if (dir) {
             Tn = ring_value(p);
           } else {
-            const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
-            real Rt = -KT;
-            Rt += sxy * sz;
-            Tn = Told + Rt * minv;
+            const real KT = radd(rfma((real)2, A, rmul((real)4, B)), radd(Dl, Dr));
+            const real Rt = rfma(sxy, sz, -KT);
+            Tn = rfma(Rt, minv, Told);
           }
           finish(p, Tn, Told);
         }
@@ -230,14 +229,14 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
       real Zm[3], Zk[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        Zm[i] = Tm[i] + (real)2 * t0c.v[i];
-        Zk[i] = t0c.v[i] - Tm[i];
+        Zm[i] = rfma((real)2, t0c.v[i], Tm[i]);
+        Zk[i] = rsub(t0c.v[i], Tm[i]);
       }
-      const real u = Zm[0] + Zm[2];
-      const real w = Zk[0] + Zk[2];
-      const real A = a1 * (u + (real)4 * Zm[1]);
-      const real B = b1 * ((real)2 * Zm[1] - u) + b2 * (w + (real)4 * Zk[1]);
-      const real D = B - A;
+      const real u = radd(Zm[0], Zm[2]);
+      const real w = radd(Zk[0], Zk[2]);
+      const real A = rmul(a1, rfma((real)4, Zm[1], u));
+      const real B = rfma(b1, rfma((real)2, Zm[1], -u), rmul(b2, rfma((real)4, Zk[1], w)));
+      const real D = rsub(B, A);
       const real Dl = __shfl_up_sync(FULL, D, 1), Dr = __shfl_down_sync(FULL, D, 1);
       if (own) {
         const real Told = t0c.v[1];
@@ -245,11 +244,9 @@ __global__ void __launch_bounds__(PERSIST_MAX_THREADS, 1) level3_persist_kernel(
         if (dir) {
           Tn = ring_value(ntop);
         } else {
-          const real KT = ((real)2 * A + (real)4 * B) + (Dl + Dr);
-          real Rt = -KT;
-          Rt += sxy * szt;
-          Rt += sf.v[0];
-          Tn = Told + Rt * ((real)2 * minv);
+          const real KT = radd(rfma((real)2, A, rmul((real)4, B)), radd(Dl, Dr));
+          const real Rt = radd(rfma(sxy, szt, -KT), sf.v[0]);
+          Tn = rfma(Rt, (real)2 * minv, Told);
         }
         finish(ntop, Tn, Told);
       }

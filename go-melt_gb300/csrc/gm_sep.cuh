@@ -37,18 +37,20 @@ __device__ __noinline__ RegCol<real, BYT> sep_surface(const Props<real> P, real 
         for (int qx = 0; qx < 2; ++qx) {
           const real px0 = qx ? MQ : PQ, px1 = qx ? PQ : MQ;
           const real py0 = qy ? MQ : PQ, py1 = qy ? PQ : MQ;
-          const real Tq4 = px0 * py0 * t00 + px1 * py0 * t10 + px0 * py1 * t01 + px1 * py1 * t11;
-          const real q = surface_flux(P, Tq4) * w2;
-          c00[i] += px0 * py0 * q;
-          c10[i] += px1 * py0 * q;
-          c01[i] += px0 * py1 * q;
-          c11[i] += px1 * py1 * q;
+          const real w00 = rmul(px0, py0), w10 = rmul(px1, py0), w01 = rmul(px0, py1), w11 = rmul(px1, py1);
+          const real Tq4 = rfma(w11, t11, rfma(w01, t01, rfma(w10, t10, rmul(w00, t00))));
+          const real q = rmul(surface_flux(P, Tq4), w2);
+          c00[i] = rfma(w00, q, c00[i]);
+          c10[i] = rfma(w10, q, c10[i]);
+          c01[i] = rfma(w01, q, c01[i]);
+          c11[i] = rfma(w11, q, c11[i]);
         }
     }
   }
   // node row r: elements i = r (upper-y corners) and i = r + 1 (lower-y corners)
 #pragma unroll
-  for (int r = 0; r < BYT; ++r) surf[r] = c01[r] + c00[r + 1] + __shfl_up_sync(FULL, c11[r] + c10[r + 1], 1);
+  for (int r = 0; r < BYT; ++r)
+    surf[r] = radd(radd(c01[r], c00[r + 1]), __shfl_up_sync(FULL, radd(c11[r], c10[r + 1]), 1));
   return out;
 }
 

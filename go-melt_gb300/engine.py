@@ -229,9 +229,10 @@ class Engine:
         self._pending = None  # MovePlan made by plan_move and not yet applied
         self.use_graph = False  # run gm_subcycle as one CUDA graph per call
         self.use_pdl = True  # level steps as programmatic dependent launches
-        # a Level-2 step's Level-3 steps as one persistent launch, where the window allows (opt-in: on the
-        # part-scale window it measures slower than one launch a step)
-        self.use_persist = False
+        # a Level-2 step's N3 Level-3 steps as one launch: 0 one launch a step, 1 the window in shared memory
+        # (gm_level3_persist, where the window has a shape), 2 the one-step kernel's body with grid barriers
+        # (gm_level3_steps); constant-property materials only
+        self.use_persist = 0
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)  # GM_PERSIST_* bits of the device kernels
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
@@ -690,9 +691,14 @@ class Engine:
         p.pdl = 1 if self.use_pdl else 0
         if N.props_constant(self.ps):  # the separable Level-3 step reads tabulated laser factors
             p.src3tab = self._buf("src3tab", N2 * N3 * int(sum(L3.nodes))).data_ptr()
-            if self.use_persist and self.persist_shape() is not None:
+            mode = int(self.use_persist)
+            nf = 0
+            if mode == 1 and self.persist_shape() is not None:
                 nf = int(N.lib().gm_level3_persist_flags((C.c_int * 3)(*L3.nodes)))
-                p.persist = 1
+            elif mode == 2:
+                nf = 2 * N2  # a grid-barrier counter per launch
+            if nf > 0:
+                p.persist = mode
                 p.xch3[0], p.xch3[1] = self._buf("xch3a", nn3).data_ptr(), self._buf("xch3b", nn3).data_ptr()
                 p.pflags, p.pflags_cap = self._buf("pflags", nf, torch.int32).data_ptr(), nf
                 p.pstatus = self.status.data_ptr()
@@ -894,7 +900,7 @@ def subcycle_batched(engines, rows_list, rows_device=None, dts_device=None):
     for i, e in enumerate(engines):
         e._batch_plan = True
         keep = e.use_persist
-        e.use_persist = False
+        e.use_persist = 0
         try:
             e.subcycle(rows_list[i] if rows_list is not None else None,
                        rows_device=None if rows_device is None else rows_device[i],

@@ -501,11 +501,14 @@ typedef struct gm_subcycle_plan {
                                 that one drains and wait for it before touching any field) */
   void* src3tab;             /* optional work (N2*N3 * (nx+ny+nz) of Level 3): the Level-3 laser factors
                                 of the call, tabulated at its start */
-  int persist;               /* 1: the N3 Level-3 steps of each Level-2 step run as one gm_level3_persist
-                                launch (constant-property materials with src3tab and the work below; a
-                                window without a persistent shape falls back to one launch a step) */
+  int persist;               /* the N3 Level-3 steps of each Level-2 step as one launch (constant-property
+                                materials with src3tab and the work below): 1 gm_level3_persist (window
+                                in shared memory; a window without a persistent shape falls back to one
+                                launch a step), 2 gm_level3_steps (grid barriers; pflags_cap >= 2 N2);
+                                0: one launch a step */
   void* xch3[2];             /* work of persist: two nn3 fields (halo exchange) */
-  unsigned* pflags;          /* work of persist: gm_level3_persist_flags(L3 nodes) counters, zeroed by the call */
+  unsigned* pflags;          /* work of persist: counters, zeroed by the call (mode 1: gm_level3_persist_flags(L3
+                                nodes), mode 2: 2 N2) */
   long long pflags_cap;
   int* pstatus;              /* device word of persist: GM_PERSIST_* bits are or-ed into it (never cleared
                                 by the call) */
@@ -612,6 +615,34 @@ typedef struct gm_toolpath_state {
 
 int gm_toolpath_rows(const double* runs, int nruns, gm_toolpath_state* state, int nrows, int ngroups, double* rows,
                      double* dts, void* stream);
+
+/* The N3 Level-3 steps of one Level-2 step in ONE cooperative launch, every
+ * step the separable one-step kernel's arithmetic over its tiles (results are
+ * gm_level_step's, bit for bit: the same inner lax.scan of subcycleGOMELT,
+ * computeFunctions.py:3404-3430, :3586-3622, as gm_level3_persist), the
+ * fields staying in L2 between steps and a grid barrier on `counter` between
+ * them.  `level` is one step's gm_level_args (bc_mode 3 ring arrays, phase
+ * in and out, optional melt time, laser set); T_in is the first step's input
+ * and T_out the last step's output; step s reads rows + 7 s (dt at [5]) and
+ * laser factor row s of src_tab and blends the ring with alpha = (s+1)/nsub.
+ * tbuf: two work fields aliasing neither T_in nor T_out.  `counter` must
+ * equal `base` when the launch starts (the launch leaves it at base +
+ * (nsteps - 1) x its grid size: give every launch its own zeroed counter).
+ * Barrier waits are bounded (about one second, GM_PERSIST_TIMEOUT in
+ * *status).  Constant-property materials; GM_ERR_UNSUPPORTED otherwise.  No
+ * counterpart in the reference. */
+typedef struct gm_steps_args {
+  gm_level_args level;
+  int nsteps, nsub;
+  const double* rows;
+  const void* src_tab;
+  void* tbuf[2];
+  unsigned* counter;
+  unsigned base;
+  int* status;
+} gm_steps_args;
+
+int gm_level3_steps(const gm_steps_args* a, const gm_props* p, void* stream);
 
 /* Library identification: returns a static string; never fails. */
 const char* gm_version(void);

@@ -233,11 +233,14 @@ def test_persist_rejects_bad_arguments():
     assert N.lib().gm_level3_persist(None, C.byref(eng.ps), None) == N.GM_ERR_ARG
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("graph", [False, True])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
-def test_subcycle_persist_on_off(graph, dtype):
-    """Two move + subcycle calls of the single-track workload with the
-    persistent Level-3 steps and with one launch a step: identical fields."""
+def test_subcycle_persist_on_off(graph, dtype, mode):
+    """Three move + subcycle calls of the single-track workload with the
+    N3 Level-3 steps of a Level-2 step as one launch (mode 1: window in shared
+    memory, mode 2: one-step body with grid barriers) and with one launch a
+    step: identical fields."""
     import copy
 
     import workloads
@@ -250,7 +253,7 @@ def test_subcycle_persist_on_off(graph, dtype):
     P = setup_properties(cfg["properties"])
     vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
     out = {}
-    for persist_on in (False, True):
+    for persist_on in (0, mode):
         stream = torch.cuda.Stream()
         with torch.cuda.stream(stream):
             eng = Engine(copy.deepcopy(cfg), P, 10, 10, dtype=dtype, stream=stream)
@@ -264,8 +267,8 @@ def test_subcycle_persist_on_off(graph, dtype):
             stream.synchronize()
         eng.check_status()
         out[persist_on] = eng
-    a, b = out[False], out[True]
-    assert b.persist_shape() is not None
+    a, b = out[0], out[mode]
+    assert mode == 2 or b.persist_shape() is not None
     for lev in (1, 2, 3):
         torch.testing.assert_close(b.T[lev], a.T[lev], rtol=0, atol=0)
         assert torch.equal(b.ph[lev], a.ph[lev])
@@ -274,3 +277,56 @@ def test_subcycle_persist_on_off(graph, dtype):
     torch.testing.assert_close(b.acc3, a.acc3, rtol=0, atol=0)
     torch.testing.assert_close(b.macc3, a.macc3, rtol=0, atol=0)
     assert float(a.T[3].max()) > 2000.0
+
+
+def steps_launch(eng, ringA, ringB, rows_d, tab, acc, macc, N3, base=0, counter=None):
+    """gm_level3_steps: the N3 steps in one launch with grid barriers."""
+    import _native as N
+    import kern
+
+    L3 = eng.geo.L[3]
+    nn = L3.nn
+    Tout = torch.full((nn,), -1.0, dtype=eng.dtype, device="cuda")
+    pout = torch.full((nn,), 255, dtype=torch.uint8, device="cuda")
+    tb = [torch.full((nn,), float("nan"), dtype=eng.dtype, device="cuda") for _ in range(2)]
+    kw = eng.level_kwargs(3, eng.T[3], Tout, rows_d[0, 5:6], eng.ph[3], pout, laser=rows_d[0], ring=(ringA, ringB),
+                          alpha=1.0 / N3)
+    if acc is not None:
+        kw.update(accum=acc, max_accum=macc)
+    kw["src_tab"] = tab
+    a = N.gm_steps_args()
+    a.level = kern.level_args(**kw)
+    a.nsteps, a.nsub = N3, N3
+    a.rows, a.src_tab = rows_d.data_ptr(), tab.data_ptr()
+    a.tbuf[0], a.tbuf[1] = tb[0].data_ptr(), tb[1].data_ptr()
+    if counter is None:
+        counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    a.counter, a.base = counter.data_ptr(), base
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    a.status = status.data_ptr()
+    rc = N.lib().gm_level3_steps(C.byref(a), C.byref(eng.ps), None)
+    torch.cuda.synchronize()
+    return rc, Tout, pout, int(status.item())
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("accum", [False, True])
+@pytest.mark.parametrize("window,N3", [("single_track", 10), ("part_scale", 10), ("odd", 7), ("odd", 1)])
+def test_grid_steps_equal_per_step(window, N3, dtype, accum):
+    """gm_level3_steps runs the one-step kernel's body: the same bits as N3
+    launches of the one-step kernel with the same launch shape."""
+    import _native as N
+
+    eng, rA, rB, rows_d, tab, acc, macc = _case(window, dtype, N3)
+    acc2, macc2 = (acc.clone(), macc.clone()) if accum else (None, None)
+    Tref, pref = per_step(eng, rA, rB, rows_d, tab, acc2, macc2, N3, (2, 4, 6))
+    acc1, macc1 = (acc.clone(), macc.clone()) if accum else (None, None)
+    rc, Tout, pout, status = steps_launch(eng, rA, rB, rows_d, tab, acc1, macc1, N3)
+    assert rc == N.GM_OK and status == 0
+    assert float(Tref.max()) > 1900.0
+    torch.testing.assert_close(Tout, Tref, rtol=0, atol=0)
+    assert torch.equal(pout, pref)
+    if accum:
+        torch.testing.assert_close(acc1, acc2, rtol=0, atol=0)
+        torch.testing.assert_close(macc1, macc2, rtol=0, atol=0)
+
