@@ -49,6 +49,7 @@ class gm_level_args(C.Structure):
         ("face", C.c_double * 5), ("inactive_amb", C.c_int), ("bc_new", vp), ("bc_old", vp),
         ("bc_alpha", C.c_double), ("bc_beta", C.c_double), ("bc_map", gm_map3), ("clamp", C.c_int),
         ("accum", vp), ("max_accum", vp), ("zchunk", C.c_int), ("pdl", C.c_int), ("src_tab", vp),
+        ("status", vp),
     ]
 
 
@@ -124,6 +125,12 @@ class gm_restrict_args(C.Structure):
                 ("cnx", C.c_int), ("cny", C.c_int), ("fine", vp), ("coarse", vp)]
 
 
+class gm_tprime_args(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("cmap", gm_map3), ("cf0", C.POINTER(C.c_int) * 3),
+                ("cf1", C.POINTER(C.c_int) * 3), ("c_of_f", C.POINTER(C.c_int) * 3), ("cnx", C.c_int),
+                ("cny", C.c_int), ("fine", vp), ("coarse", vp), ("out", vp)]
+
+
 class gm_restrict_s1_args(C.Structure):
     _fields_ = [("dtype", C.c_int), ("n", C.c_int * 3), ("map", gm_map3), ("cidx", C.POINTER(C.c_int) * 3),
                 ("cnx", C.c_int), ("cny", C.c_int), ("fine_ph", C.POINTER(C.c_uint8)),
@@ -185,7 +192,8 @@ class gm_subcycle_plan(C.Structure):
         ("src_scratch", vp), ("src_cap", C.c_longlong), ("src2", vp), ("L2all", vp), ("L3all", vp), ("L3pall", vp),
         ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int),
         ("pdl", C.c_int), ("src3tab", vp), ("persist", C.c_int), ("xch3", vp * 2), ("pflags", vp),
-        ("pflags_cap", C.c_longlong), ("pstatus", vp)]
+        ("pflags_cap", C.c_longlong), ("pstatus", vp), ("inj32", C.POINTER(C.c_int) * 9),
+        ("inj21", C.POINTER(C.c_int) * 9)]
 
 
 class gm_persist_args(C.Structure):
@@ -197,6 +205,7 @@ class gm_persist_args(C.Structure):
 
 
 GM_PERSIST_TIMEOUT, GM_PERSIST_BAD_T = 1, 2
+GM_STATUS_BAD_T = GM_PERSIST_BAD_T
 
 
 class gm_steps_args(C.Structure):
@@ -209,7 +218,8 @@ class gm_toolpath_state(C.Structure):
                 ("y", C.c_double), ("t", C.c_double)]
 
 
-def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bool = False) -> int:
+def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bool = False,
+                          inject32: bool = False, inject21: bool = False) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
     steps (coupling 2 onto the step's source, Level-2 solve, Level-3 ring, N3
@@ -217,8 +227,11 @@ def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bo
     (3).  For a constant-property material (separable kernels) each of the
     4 + 2 N2 coupling calls is one kernel more and the Level-3 laser factors
     are tabulated once (one kernel).  With persistent Level-3 steps the N3
-    solves of a Level-2 step are one kernel."""
+    solves of a Level-2 step are one kernel.  Where a restriction is an
+    injection its restriction and T' are one kernel (inject32: the 2 N2
+    Level-3 ones, inject21: the two Level-2 ones)."""
     n = 20 + 2 * (1 + N2 * (6 + (1 if persist else N3)))
+    n -= (2 * N2 if inject32 else 0) + (2 if inject21 else 0)
     return n + (4 + 2 * N2 + 1 if separable else 0)
 
 
@@ -283,6 +296,7 @@ SIGNATURES = {
     "gm_interp_matrix": [C.c_int, C.POINTER(gm_map3), vp, vp, vp],
     "gm_interp_w_matrix": [C.c_int, vp, vp, vp, vp, C.c_longlong, vp],
     "gm_restrict": [C.POINTER(gm_restrict_args), vp],
+    "gm_tprime_inject": [C.POINTER(gm_tprime_args), vp],
     "gm_restrict_s1": [C.POINTER(gm_restrict_s1_args), vp],
     "gm_l0_gather": [C.POINTER(gm_l0_args), vp],
     "gm_l0_scatter": [C.POINTER(gm_l0_args), vp],

@@ -95,6 +95,7 @@ gm_level_args level_args(Ctx& c, const gm_window& w, int ne_planes, const void* 
   a.zchunk = p.zchunk;
   a.pdl = p.pdl;  // dt, the laser row and its factor table are never written by the kernels before it
   a.src_tab = src_tab;
+  a.status = p.pstatus;  // non-finite or out-of-range results of any level step
   return a;
 }
 
@@ -172,8 +173,27 @@ void source(Ctx& c, const gm_couple_geom& g, const double* const xq[3], const do
 // getNewTprime (:2060-2099): restrict the fine field into coarse_T, then
 // T' = T_f - I(T_c).
 void new_tprime(Ctx& c, const gm_map3& rmap, const int* const idx[3], const gm_window& coarse, const gm_map3& cmap,
-                const gm_window& fine, const void* fineT, void* coarseT, void* outTp) {
+                const gm_window& fine, const void* fineT, void* coarseT, void* outTp, const int* const inj[9]) {
   const gm_subcycle_plan& p = *c.p;
+  if (inj[0]) {  // the restriction is an injection: one pass
+    gm_tprime_args t;
+    memset(&t, 0, sizeof(t));
+    t.dtype = p.dtype;
+    for (int d = 0; d < 3; ++d) {
+      t.n[d] = fine.nodes[d];
+      t.cf0[d] = inj[d];
+      t.cf1[d] = inj[3 + d];
+      t.c_of_f[d] = inj[6 + d];
+    }
+    t.cmap = cmap;
+    t.cnx = coarse.nodes[0];
+    t.cny = coarse.nodes[1];
+    t.fine = fineT;
+    t.coarse = coarseT;
+    t.out = outTp;
+    GM_TRY(gm_tprime_inject(&t, c.st));
+    return;
+  }
   gm_restrict_args r;
   memset(&r, 0, sizeof(r));
   r.dtype = p.dtype;
@@ -329,7 +349,7 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
       ph3c = phn;
     }
     void* Tp3n = part2 ? p.tp3w[l2 % 2] : hist_l2;
-    new_tprime(c, p.r32, p.r32_idx, p.L2, p.bc23, p.L3, T3c, T2n, Tp3n);
+    new_tprime(c, p.r32, p.r32_idx, p.L2, p.bc23, p.L3, T3c, T2n, Tp3n, p.inj32);
     if (part2 && p.L2all) {
       copy(c, at(p.L2all, (long long)l2 * nn(p.L2), c.esz), T2n, nn(p.L2) * c.esz);
       copy(c, at(p.L3all, l2 * n3, c.esz), T3c, n3 * c.esz);
@@ -428,7 +448,7 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
 
   // pass 1 (predictor)
   PassOut o = l2_pass(c, p->T1p, false);
-  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, o.T2, p->T1p, p->Tp2w);
+  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, o.T2, p->T1p, p->Tp2w, p->inj21);
   couple(c, p->c31, p->L3, p->rhs1, p->rhs1_lo, p->rhs1_n, nullptr, o.Tp3, p->L3.Tp, p->dts);
   couple(c, p->c21, p->L2, p->rhs1, p->rhs1_lo, p->rhs1_n, nullptr, p->Tp2w, p->L2.Tp, p->dts);
   level(c, p->L1, p->L1_ne_planes, p->L1.T, p->T1c, p->dts, p->L1.ph, nullptr, p->rhs1, p->rhs1_lo, p->rhs1_n,
@@ -441,7 +461,7 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
   copy(c, p->L3.Tp, o.Tp3, n3 * c.esz);
   copy(c, p->L2.T, o.T2, n2 * c.esz);
   copy(c, p->L2.ph, o.ph2, n2);
-  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, p->L2.T, p->T1c, p->L2.Tp);
+  new_tprime(c, p->r21, p->r21_idx, p->L1, p->bc12, p->L2, p->L2.T, p->T1c, p->L2.Tp, p->inj21);
   copy(c, p->L1.T, p->T1c, n1 * c.esz);
 
   // Level-0 S1 store at the Level-3 window

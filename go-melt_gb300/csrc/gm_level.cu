@@ -57,6 +57,7 @@ struct LevelK {
   Map3<real> bc_map;
   real* accum;
   real* max_accum;
+  int* status;  // optional: GM_STATUS_BAD_T when a new value is non-finite or above 1e5 K
   real lam[8];  // Hadamard-mode eigenvalues of K_ref, divided by 8
   real wvol;    // hx*hy*hz/8
   real w2;      // hx*hy/4
@@ -438,6 +439,7 @@ __device__ __forceinline__ void level_body(const LevelK<real>& a, int bx, int by
         }
         Tn = v;
       }
+      if (a.status && !(Tn <= (real)1e5)) atomicOr(a.status, GM_STATUS_BAD_T);
       if (hClamp) Tn = fmax(Tn, P.T_amb);
       a.T_out[id] = Tn;
       if (hPhout) a.ph_out[id] = (uint8_t)(phn & 3u);
@@ -591,7 +593,12 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
   // byte ph).  The melt-time update (acc + dt S2 - reset acc, max(reset acc,
   // macc)) leaves a node that is not liquid unchanged (macc >= 0), so the
   // accumulators are read (cAcc, cMacc) and written at liquid nodes only.
+  bool bad = false;  // a new value non-finite or above 1e5 K (before the clamp)
+  auto report = [&]() {
+    if (bad && a.status) atomicOr(a.status, GM_STATUS_BAD_T);
+  };
   auto finish = [&](int id, real Tn, real Told, uint32_t ph, real cAcc, real cMacc) {
+    bad = bad || !(Tn <= (real)1e5);
     if (hClamp) Tn = fmax(Tn, P.T_amb);
     a.T_out[id] = Tn;
     if (needPh) {
@@ -660,6 +667,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
       finish(id, Tn, Told, needPh ? (uint32_t)a.ph_in[id] : 0u, liq ? a.accum[id] : (real)0,
              liq ? a.max_accum[id] : (real)0);
     }
+    report();
     return;
   }
 
@@ -850,6 +858,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     const real sz = hLaser ? __shfl_sync(FULL, szl, 0) : (real)0;
     plane_out(std::true_type(), ntop, strip_of(Tm), strip_of(T0), strip_of(T0), node_of(surf), sz, phase_of(nph[0]),
               node_of(nrhs[0]), node_of(nacc[0]), node_of(nmac[0]));
+    report();
     return;
   }
 
@@ -886,6 +895,7 @@ __device__ __forceinline__ void sep_body(const LevelK<real>& a, int bx, int by, 
     if (p + 4 < Z1) body(std::integral_constant<int, 4>(), p + 4);
     if (p + 5 < Z1) body(std::integral_constant<int, 5>(), p + 5);
   }
+  report();
 }
 
 template <typename real, int BYT, int FL>
@@ -1200,6 +1210,7 @@ static LevelK<real> make_levelk(const gm_level_args* g, const gm_props* pr) {
   a.bc_map = make_map3<real>(g->bc_map);
   a.accum = (real*)g->accum;
   a.max_accum = (real*)g->max_accum;
+  a.status = g->status;
   a.p = make_props<real>(*pr);
   const double hx = g->h[0], hy = g->h[1], hz = g->h[2];
   for (int m = 0; m < 8; ++m) {

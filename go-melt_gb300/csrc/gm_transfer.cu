@@ -129,6 +129,93 @@ __global__ void restrict_kernel(int n0, int n1, int n2, const Map3<real> m, cons
   }
 }
 
+// Restriction and T' in one pass (gm_tprime_inject): the prolongation of
+// interp_kernel with the eight corner values taken from the fine field at
+// coarse overlap nodes (their restricted value when the restriction is an
+// injection), and the coarse overlap nodes written with those fine values.
+// Reads of the coarse field touch only nodes outside the overlap, which no
+// thread writes.  Per fine index and axis, cf0 / cf1 give the fine node
+// coinciding with the low / high corner of its coarse element (-1: not an
+// overlap index), so each corner value is one load after the tables.
+constexpr int TROWS = 2;  // fine rows a thread
+template <typename real>
+struct TprimeK {
+  int n[3];
+  Map3<real> cmap;
+  const int* cf0[3];
+  const int* cf1[3];
+  const int* c_of_f[3];
+  int cnx, cny;
+  const real* fine;
+  real* coarse;
+  real* out;
+};
+
+template <typename real>
+__global__ void tprime_inject_kernel(const TprimeK<real> a) {
+  pdl_begin();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
+  if (i >= a.n[0]) return;
+  const Map3<real>& m = a.cmap;
+  const int ex = m.ax[0].e[i], ez = m.ax[2].e[k];
+  const real x0 = m.ax[0].w[2 * i], x1 = m.ax[0].w[2 * i + 1];
+  const real z0 = m.ax[2].w[2 * k], z1 = m.ax[2].w[2 * k + 1];
+  const int fx[2] = {a.cf0[0][i], a.cf1[0][i]};
+  const int fz[2] = {a.cf0[2][k], a.cf1[2][k]};
+  const int cfx = a.c_of_f[0][i], cfz = a.c_of_f[2][k];
+  const long long fnxy = (long long)a.n[0] * a.n[1];
+  const long long cnxy = (long long)a.cnx * a.cny;
+  const int jb = blockIdx.y * TROWS;
+  // the rows' tables first (independent loads), then the corner values
+  int ey[TROWS], fy0[TROWS], fy1[TROWS], cfy[TROWS];
+  real y0[TROWS], y1[TROWS];
+#pragma unroll
+  for (int r = 0; r < TROWS; ++r) {
+    const int j = min(jb + r, a.n[1] - 1);
+    ey[r] = m.ax[1].e[j];
+    y0[r] = m.ax[1].w[2 * j];
+    y1[r] = m.ax[1].w[2 * j + 1];
+    fy0[r] = a.cf0[1][j];
+    fy1[r] = a.cf1[1][j];
+    cfy[r] = a.c_of_f[1][j];
+  }
+  constexpr int OX[8] = {0, 1, 1, 0, 0, 1, 1, 0}, OY[8] = {0, 0, 1, 1, 0, 0, 1, 1}, OZ[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+#pragma unroll
+  for (int r = 0; r < TROWS; ++r) {
+    const int j = jb + r;
+    if (j >= a.n[1]) break;
+    const long long t = i + (long long)a.n[0] * j + fnxy * k;
+    real w8[8];
+    w8[0] = x0 * y0[r] * z0;
+    w8[1] = x1 * y0[r] * z0;
+    w8[2] = x1 * y1[r] * z0;
+    w8[3] = x0 * y1[r] * z0;
+    w8[4] = x0 * y0[r] * z1;
+    w8[5] = x1 * y0[r] * z1;
+    w8[6] = x1 * y1[r] * z1;
+    w8[7] = x0 * y1[r] * z1;
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ok = ok && (w8[q] >= (real)-1e-2) && (w8[q] <= (real)(1 + 1e-2));
+#pragma unroll
+    for (int q = 0; q < 8; ++q) w8[q] = ok ? fmin(fmax(w8[q], (real)0), (real)1) : (real)0;
+    const int fy[2] = {fy0[r], fy1[r]};
+    real u[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int gx = fx[OX[q]], gy = fy[OY[q]], gz = fz[OZ[q]];
+      u[q] = (gx >= 0 && gy >= 0 && gz >= 0)
+                 ? a.fine[gx + (long long)a.n[0] * gy + fnxy * gz]
+                 : a.coarse[(ex + OX[q]) + (long long)a.cnx * (ey[r] + OY[q]) + cnxy * (ez + OZ[q])];
+    }
+    const real v = w8[0] * u[0] + w8[1] * u[1] + w8[2] * u[2] + w8[3] * u[3] + w8[4] * u[4] + w8[5] * u[5] +
+                   w8[6] * u[6] + w8[7] * u[7];
+    const real f = a.fine[t];
+    a.out[t] = f + (real)-1 * v;
+    if (cfx >= 0 && cfy[r] >= 0 && cfz >= 0) a.coarse[cfx + (long long)a.cnx * cfy[r] + cnxy * cfz] = f;
+  }
+}
+
 // Level-1 S1 from Level 2 (subcycleGOMELT :3272-3278, updateStateProperties
 // :2547-2556): interpolate the 0/1 S1 of Level 2 at the Level-1 overlap nodes;
 // the stored bit is the value's use in computeStateProperties (S1 > 0.499),
@@ -331,6 +418,38 @@ extern "C" int gm_restrict(const gm_restrict_args* g, void* stream) {
   else
     return GM_ERR_ARG;
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+template <typename real>
+static int do_tprime(const gm_tprime_args* g, cudaStream_t st) {
+  TprimeK<real> a;
+  for (int d = 0; d < 3; ++d) {
+    a.n[d] = g->n[d];
+    a.cf0[d] = g->cf0[d];
+    a.cf1[d] = g->cf1[d];
+    a.c_of_f[d] = g->c_of_f[d];
+  }
+  a.cmap = make_map3<real>(g->cmap);
+  a.cnx = g->cnx;
+  a.cny = g->cny;
+  a.fine = (const real*)g->fine;
+  a.coarse = (real*)g->coarse;
+  a.out = (real*)g->out;
+  const int bx = a.n[0] <= 256 ? 32 * cdiv(a.n[0], 32) : 256;
+  launch_k(tprime_inject_kernel<real>, dim3(cdiv(a.n[0], bx), cdiv(a.n[1], TROWS), a.n[2]), dim3(bx), 0, st, a);
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+extern "C" int gm_tprime_inject(const gm_tprime_args* g, void* stream) {
+  if (!g || !g->fine || !g->coarse || !g->out || g->out == g->fine || !map_ok(g->cmap, g->n) ||
+      g->cnx != g->cmap.src_nx || g->cny != g->cmap.src_ny)
+    return GM_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (g->n[d] < 1 || g->n[d] > 65535 || !g->cf0[d] || !g->cf1[d] || !g->c_of_f[d]) return GM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (g->dtype == GM_F32) return do_tprime<float>(g, st);
+  if (g->dtype == GM_F64) return do_tprime<double>(g, st);
+  return GM_ERR_ARG;
 }
 
 extern "C" int gm_restrict_s1(const gm_restrict_s1_args* g, void* stream) {

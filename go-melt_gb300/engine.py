@@ -277,6 +277,34 @@ class Engine:
         a.which_term = int(which)
         N.call("gm_interp", C.byref(a), kern.stream_ptr(self.stream))
 
+    def _inject(self, fine_coords, fine_nodes, overlap_coords, overlap_idx, coarse_coords):
+        """Tables of gm_tprime_inject (cf0[3], cf1[3], c_of_f[3]) when the
+        restriction of the fine level at the coarse overlap nodes is an
+        injection (each overlap coordinate coincides with a fine node: weights
+        0 / 1 within 1e-9), else None."""
+        cf0, cf1, cof = [], [], []
+        for d in range(3):
+            m = axis_map(fine_coords[d], overlap_coords[d])
+            e = np.asarray(m.elem, dtype=np.int64)
+            w = np.asarray(m.w)
+            at0, at1 = np.abs(w[:, 1]) <= 1e-9, np.abs(w[:, 0]) <= 1e-9
+            if not np.all(at0 | at1):
+                return None
+            f = np.where(at0, e, e + 1)
+            ci = np.asarray(overlap_idx[d], dtype=np.int64)
+            nc = len(coarse_coords[d])
+            if f.min() < 0 or f.max() >= fine_nodes[d] or ci.min() < 0 or ci.max() >= nc:
+                return None
+            foc = np.full(nc, -1, dtype=np.int64)  # coarse index -> coinciding fine index
+            foc[ci] = f
+            b = np.full(int(fine_nodes[d]), -1, dtype=np.int32)
+            b[f] = ci
+            ce = np.asarray(axis_map(coarse_coords[d], fine_coords[d]).elem, dtype=np.int64)  # as cmap
+            cf0.append(foc[ce].astype(np.int32))
+            cf1.append(foc[ce + 1].astype(np.int32))
+            cof.append(b)
+        return [C.cast(self.arena.put(x, np.int32), C.POINTER(C.c_int)) for x in cf0 + cf1 + cof]
+
     def _idx_tensor(self, arrs, nodes, what):
         """Stage per-axis node-index arrays (device int pointers) after checking
         they address the grid."""
@@ -303,6 +331,8 @@ class Engine:
         t["r21"] = self._map(L2.coords, L2.nodes, L2.overlap_coords)  # Level 2 at Level-1 overlap nodes
         t["r32_idx"] = self._idx_tensor(L3.overlap_nodes, L2.nodes, "Level-3 overlap in Level 2")
         t["r21_idx"] = self._idx_tensor(L2.overlap_nodes, L1.nodes, "Level-2 overlap in Level 1")
+        t["inj32"] = self._inject(L3.coords, L3.nodes, L3.overlap_coords, L3.overlap_nodes, L2.coords)
+        t["inj21"] = self._inject(L2.coords, L2.nodes, L2.overlap_coords, L2.overlap_nodes, L1.coords)
         t["c32"] = CoupleGeom(L3.coords, L2.coords, self.np_dtype, self.arena)
         t["c31"] = CoupleGeom(L3.coords, L1.coords, self.np_dtype, self.arena)
         t["c21"] = CoupleGeom(L2.coords, L1.coords, self.np_dtype, self.arena)
@@ -552,13 +582,28 @@ class Engine:
         a.coarse = kern.ptr(coarse_T)
         N.call("gm_restrict", C.byref(a), kern.stream_ptr(self.stream))
 
-    def _new_tprime(self, fine_lev, fine_T, coarse_T, out_Tp):
-        """getNewTprime (:2060-2099): restrict into coarse_T, then T' = T_f - I(T_c)."""
+    def _new_tprime(self, fine_lev, fine_T, coarse_T, out_Tp, fused=True):
+        """getNewTprime (:2060-2099): restrict into coarse_T, then T' = T_f - I(T_c)
+        (one gm_tprime_inject launch where the restriction is an injection,
+        unless fused is False)."""
         g = self.geo
         if fine_lev == 3:
             rmap, idx, cmap, cn = self.tables["r32"], self.tables["r32_idx"], self.tables["bc23"], g.L[2].nodes
+            inj = self.tables.get("inj32")
         else:
             rmap, idx, cmap, cn = self.tables["r21"], self.tables["r21_idx"], self.tables["bc12"], g.L[1].nodes
+            inj = self.tables.get("inj21")
+        if fused and inj is not None:
+            a = N.gm_tprime_args()
+            a.dtype = kern.dtype_code(fine_T)
+            for d in range(3):
+                a.n[d] = int(g.L[fine_lev].nodes[d])
+                a.cf0[d], a.cf1[d], a.c_of_f[d] = inj[d], inj[3 + d], inj[6 + d]
+            a.cmap = cmap.struct
+            a.cnx, a.cny = int(cn[0]), int(cn[1])
+            a.fine, a.coarse, a.out = kern.ptr(fine_T), kern.ptr(coarse_T), kern.ptr(out_Tp)
+            N.call("gm_tprime_inject", C.byref(a), kern.stream_ptr(self.stream))
+            return
         self._restrict(rmap, idx, cn, fine_T, coarse_T)
         self._interp([(cmap, coarse_T, -1.0)], g.L[fine_lev].nodes, out_Tp, base=fine_T)
 
@@ -618,7 +663,8 @@ class Engine:
             self._last_plan = p
             return out_hist
         N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
-               kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps), persist=bool(p.persist)))
+               kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps), persist=bool(p.persist),
+                                              inject32=bool(p.inj32[0]), inject21=bool(p.inj21[0])))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         return out_hist
 
@@ -654,6 +700,11 @@ class Engine:
             p.face[i] = float(v)
         p.acc3, p.macc3 = self.acc3.data_ptr(), self.macc3.data_ptr()
         p.bc12, p.bc23, p.r32, p.r21 = tb["bc12"].struct, tb["bc23"].struct, tb["r32"].struct, tb["r21"].struct
+        for q in range(9):
+            if tb.get("inj32") is not None:
+                p.inj32[q] = tb["inj32"][q]
+            if tb.get("inj21") is not None:
+                p.inj21[q] = tb["inj21"][q]
         for d in range(3):
             p.r32_idx[d] = tb["r32_idx"][d]
             p.r21_idx[d] = tb["r21_idx"][d]
@@ -701,7 +752,7 @@ class Engine:
                 p.persist = mode
                 p.xch3[0], p.xch3[1] = self._buf("xch3a", nn3).data_ptr(), self._buf("xch3b", nn3).data_ptr()
                 p.pflags, p.pflags_cap = self._buf("pflags", nf, torch.int32).data_ptr(), nf
-                p.pstatus = self.status.data_ptr()
+        p.pstatus = self.status.data_ptr()  # every level step reports non-finite / out-of-range values here
         return p
 
     def persist_shape(self):
@@ -722,8 +773,8 @@ class Engine:
             what = []
             if v & N.GM_PERSIST_TIMEOUT:
                 what.append("a wait between Level-3 tiles ran out")
-            if v & N.GM_PERSIST_BAD_T:
-                what.append("non-finite or out-of-range Level-3 temperature")
+            if v & N.GM_STATUS_BAD_T:
+                what.append("non-finite or out-of-range temperature (above 1e5 K) from a level step")
             raise N.GomeltError("device status: " + ", ".join(what or [f"code {v}"]))
 
     # ------------------------------------------------------------------
@@ -910,10 +961,24 @@ def subcycle_batched(engines, rows_list, rows_device=None, dts_device=None):
             e.use_persist = keep
         plans[i] = e._last_plan
         props[i] = e.ps
-        kernels += N.subcycle_kernel_count(e.N2, e.N3, N.props_constant(e.ps))
+        kernels += N.subcycle_kernel_count(e.N2, e.N3, N.props_constant(e.ps), inject32=bool(plans[i].inj32[0]),
+                                           inject21=bool(plans[i].inj21[0]))
     N.call("gm_subcycle_batched", plans, len(engines), props, kern.stream_ptr(st), kernels=kernels)
     for e in engines:
         g = e.geo
         e.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         e._last_plan = None
 
+
+
+def failed_instances(engines):
+    """Indices of the engines whose device status word is set (a level step
+    produced a non-finite or out-of-range value, or a bounded wait ran out),
+    read with ONE device-to-host copy for all of them; the words are cleared.
+    The words are read on the first engine's stream."""
+    st = engines[0].stream or torch.cuda.current_stream()
+    with torch.cuda.stream(st):
+        words = torch.stack([e.status[0] for e in engines])
+        for e in engines:
+            e.status.zero_()
+    return [i for i, v in enumerate(words.cpu().tolist()) if v]

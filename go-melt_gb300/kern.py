@@ -92,7 +92,7 @@ def level_args(*, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_o
                substrate=0, k_arr=None, rc_arr=None, F_full=None, corr_full=None, rhs_box=None, box=None,
                laser=None, surface=0, bc_mode=0, face=None, inactive_amb=0, bc_new=None, bc_old=None,
                bc_alpha=0.0, bc_beta=0.0, bc_map: DeviceMap3 | None = None, clamp=0, accum=None, max_accum=None,
-               zchunk=0, pdl=0, src_tab=None):
+               zchunk=0, pdl=0, src_tab=None, status=None):
     a = N.gm_level_args()
     a.dtype = dtype_code(T_in)
     a.nx, a.ny, a.nz = (int(x) for x in nodes)
@@ -126,4 +126,5 @@ def level_args(*, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_o
     a.zchunk = int(zchunk)
     a.pdl = int(pdl)
     a.src_tab = ptr(src_tab)
+    a.status = ptr(status)
     return a

@@ -107,6 +107,9 @@ typedef struct gm_level_args {
   const void* src_tab;         /* optional: this step's laser factors from gm_fine_source_tables (one
                                   row); the separable kernel reads them instead of evaluating the
                                   Gaussians (with pdl, not written by the preceding kernels either) */
+  int* status;                 /* optional device status word: a new value that is non-finite or above
+                                  1e5 K (checked before the clamp; the bound of the reference's
+                                  printLevelMaxMin, computeFunctions.py:3648-3658) sets GM_STATUS_BAD_T */
 } gm_level_args;
 
 int gm_level_step(const gm_level_args* a, const gm_props* p, void* stream);
@@ -191,6 +194,33 @@ typedef struct gm_restrict_args {
 } gm_restrict_args;
 
 int gm_restrict(const gm_restrict_args* a, void* stream);
+
+/* getNewTprime (:2060-2099) in ONE pass where the restriction is an
+ * injection (every coarse overlap node coincides with a fine node, as on the
+ * aligned level hierarchies): the coarse overlap nodes take the fine values
+ * there, and T' = T_f - I(T_c) reads those values from the fine field, so
+ * neither part waits for the other.  Per axis d and fine index f (length:
+ * fine nodes along d): cf0[d][f] / cf1[d][f] = the fine index coinciding with
+ * the low / high coarse node of f's coarse element (cmap) when that coarse
+ * index is an overlap index, else -1; c_of_f[d][f] = the overlap coarse
+ * index coinciding with f, else -1.  cmap: fine nodes -> coarse grid (the
+ * prolongation map of gm_interp).  Equals gm_restrict + gm_interp with base =
+ * fine, coef = -1 when the restriction weights are exactly 0 / 1.  No
+ * counterpart in the reference (the two steps fused). */
+typedef struct gm_tprime_args {
+  int dtype;
+  int n[3];              /* fine nodes */
+  gm_map3 cmap;          /* fine nodes -> coarse grid */
+  const int* cf0[3];
+  const int* cf1[3];
+  const int* c_of_f[3];
+  int cnx, cny;          /* coarse node strides */
+  const void* fine;      /* fine T */
+  void* coarse;          /* coarse T: overlap nodes overwritten */
+  void* out;             /* T' (fine nodes) */
+} gm_tprime_args;
+
+int gm_tprime_inject(const gm_tprime_args* a, void* stream);
 
 /* Level-1 S1 from Level 2 (subcycleGOMELT :3272-3278, updateStateProperties
  * :2547-2556): S1 bit of coarse_ph at the overlap nodes := interpolated
@@ -510,8 +540,14 @@ typedef struct gm_subcycle_plan {
   unsigned* pflags;          /* work of persist: counters, zeroed by the call (mode 1: gm_level3_persist_flags(L3
                                 nodes), mode 2: 2 N2) */
   long long pflags_cap;
-  int* pstatus;              /* device word of persist: GM_PERSIST_* bits are or-ed into it (never cleared
-                                by the call) */
+  int* pstatus;              /* optional device status word: every level step of the call or-s
+                                GM_STATUS_BAD_T into it for a non-finite or out-of-range new value, and
+                                persist its GM_PERSIST_* bits (never cleared by the call; needed by
+                                persist) */
+  const int* inj32[9];       /* optional: cf0[3], cf1[3], c_of_f[3] of gm_tprime_inject for Level 3 ->
+                                Level 2 when that restriction is an injection (its T' then takes one
+                                launch) */
+  const int* inj21[9];       /* the same for Level 2 -> Level 1 */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
@@ -554,6 +590,7 @@ int gm_subcycle_batched(const gm_subcycle_plan* plans, int nb, const gm_props* p
  * ------------------------------------------------------------------------ */
 #define GM_PERSIST_TIMEOUT 1
 #define GM_PERSIST_BAD_T 2
+#define GM_STATUS_BAD_T GM_PERSIST_BAD_T /* level steps: gm_level_args.status */
 
 typedef struct gm_persist_args {
   int dtype;

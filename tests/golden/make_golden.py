@@ -1,7 +1,7 @@
 """Generate golden vectors by running the unmodified GO-MELT reference.
 
-Run in a container that has the reference sources (read-only) at
-``/root/reference`` (or pass ``--reference``).  JAX 0.4.16, which the
+Run with ``--reference <GO-MELT checkout>`` (or the environment variable
+GOMELT_REFERENCE naming it); the sources are only read.  JAX 0.4.16, which the
 reference pins, is not installed, so ``oracle/jaxshim.py`` supplies a NumPy
 (FP64) implementation of the JAX primitives the reference uses; the
 reference's own ``computeFunctions.py`` / ``go_melt.py`` run unchanged on top.
@@ -394,10 +394,13 @@ def unit_vectors(name, cf, cfg, props, store):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("GOMELT_REFERENCE"),
+                    help="a checkout of JLnorthwestern/GO-MELT (default: $GOMELT_REFERENCE)")
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--cases", default=",".join(CASES))
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("name the reference checkout with --reference or GOMELT_REFERENCE")
     jaxshim.install()
     sys.path.insert(0, os.path.join(args.reference, "go_melt"))
     for name in args.cases.split(","):
