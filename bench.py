@@ -45,6 +45,7 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_FILE = os.path.join(ROOT, "profiles", "level_sep_l3_part_scale.txt")
 PERSIST_PROFILE = os.path.join(ROOT, "profiles", "level3_persist_part_scale.txt")
 STEPS_PROFILE = os.path.join(ROOT, "profiles", "level3_steps_part_scale.txt")
+PAIR_PROFILE = os.path.join(ROOT, "profiles", "level_sep2_l3_part_scale.txt")
 
 
 def parse_args():
@@ -77,6 +78,10 @@ def parse_args():
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--no-graph", action="store_true", help="issue the subcycle's launches directly")
+    ap.add_argument("--pairs", type=int, default=None, choices=[0, 1],
+                    help="Level-3 steps two at a time in the subcycle (default: the autotuner's choice)")
+    ap.add_argument("--pair-only", action="store_true",
+                    help="--kernel-only: the two-step Level-3 kernel (gm_level_step2) instead of the one-step kernel")
     ap.add_argument("--persist", type=int, default=None, choices=[0, 1, 2],
                     help="a Level-2 step's Level-3 steps as one launch: 0 one launch a step, 1 window in shared "
                          "memory, 2 one-step body with grid barriers (default: the engine's default)")
@@ -226,6 +231,8 @@ def bench_config(ws):
 # ---------------------------------------------------------------------------
 def l3_kernel_name(v):
     """The Level-3 level-step kernel the bench runs (constant-property workload)."""
+    if v is not None and v.kernel == 2:
+        return "level_sep2_kernel (Level 3, two fine steps a launch, separable stencil)"
     if v is None or v.kernel == 1:
         return "level_sep_kernel (Level 3, separable stencil)"
     return "level_step_kernel (Level 3, element tiles)"
@@ -233,9 +240,9 @@ def l3_kernel_name(v):
 
 def shape_json(v):
     """A measured level-step launch shape (kern.TunedShape) for the JSON line."""
-    if v.kernel == 1:
-        return {"kernel": "separable", "cta": [v.tile_x, v.tile_y], "rows_per_thread": v.rows, "zchunk": v.zchunk,
-                "us": round(v.us, 2)}
+    if v.kernel in (1, 2):
+        return {"kernel": "separable" if v.kernel == 1 else "separable, two steps a launch", "cta": [v.tile_x, v.tile_y],
+                "rows_per_thread": v.rows, "zchunk": v.zchunk, "us": round(v.us, 2)}
     return {"kernel": "element_tiles", "tile": [v.tile_x, v.tile_y], "zchunk": v.zchunk, "us": round(v.us, 2)}
 
 
@@ -450,7 +457,48 @@ def steps_launcher(eng, chunk_rows, nlaunch, accum=False, nsteps=None):
     return launch, N3
 
 
+def pair_launcher(eng, chunk_rows, accum=False):
+    """The two-step Level-3 kernel (gm_level_step2) as the subcycle launches
+    it on the engine's window: fine steps 0 and 1 of the chunk (ring from the
+    precomputed prolongation arrays, laser factors from the steps' table,
+    programmatic dependent launch).  Returns launch() -> None; writes only
+    scratch outputs."""
+    import ctypes as C
+
+    import torch
+
+    import _native as N
+    import kern
+
+    L3 = eng.geo.L[3]
+    dev = eng.dev
+    rows_d = torch.as_tensor(chunk_rows[:2], device=dev).contiguous()
+    Lw = int(sum(L3.nodes))
+    tab = torch.empty(2 * Lw, dtype=eng.dtype, device=dev)
+    N.call("gm_fine_source_tables", kern.dtype_code(tab), (C.c_int * 3)(*L3.nodes), (C.c_double * 3)(*L3.origin()),
+           (C.c_double * 3)(*L3.spacing()), rows_d.data_ptr(), 2, C.byref(eng.ps), tab.data_ptr(),
+           kern.stream_ptr(eng.stream))
+    ring = eng._ring(3, eng.T[2], eng.T[2])
+    nn = L3.nn
+    keep = dict(rows=rows_d, tab=tab, ring=ring, Tout=torch.empty_like(eng.T[3]), pout=torch.empty_like(eng.ph[3]),
+                acc=torch.zeros(nn, dtype=eng.dtype, device=dev), macc=torch.zeros(nn, dtype=eng.dtype, device=dev))
+    kw = eng.level_kwargs(3, eng.T[3], keep["Tout"], rows_d[0, 5:6], eng.ph[3], keep["pout"], laser=rows_d[0],
+                          ring=ring, alpha=0.1)
+    if accum:
+        kw.update(accum=keep["acc"], max_accum=keep["macc"])
+    kw.update(src_tab=tab[:Lw], pdl=1)
+    a = kern.level2_args(dt2=rows_d[1, 5:6], src_tab2=tab[Lw:], bc_alpha2=0.2, bc_beta2=0.8, **kw)
+
+    def launch():
+        N.call("gm_level_step2", C.byref(a), C.byref(eng.ps), kern.stream_ptr(eng.stream))
+
+    launch.keep = keep
+    return launch
+
+
 def run_ours(args):
+    import ctypes as C
+
     import numpy as np
     import torch
 
@@ -488,6 +536,9 @@ def run_ours(args):
         if args.persist is not None:
             eng.use_persist = args.persist
         persist = int(eng.use_persist) if (int(eng.use_persist) != 1 or eng.persist_shape() is not None) else 0
+        if args.pairs is not None:
+            eng.use_pairs = bool(args.pairs)
+        pairs = bool(eng.use_pairs) and persist == 0 and N.props_constant(eng.ps)
         # toolpath rows generated on the device (FP64 accumulation) from the run table
         tp = engine.DeviceToolpath(runs, dev, stream)
         rows_buf = torch.empty(n23 * 7, dtype=torch.float64, device=dev)
@@ -592,6 +643,13 @@ def run_ours(args):
         last = torch.as_tensor(last_chunk[-1], device=dev)
         ring = eng._ring(3, eng.T[2], eng.T[2])
         l3kw = eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5)
+        if N.props_constant(eng.ps):  # the laser factors from a table, as the subcycle passes them
+            Lw = int(sum(L3.nodes))
+            l3tab = torch.empty(Lw, dtype=eng.dtype, device=dev)
+            N.call("gm_fine_source_tables", kern.dtype_code(l3tab), (C.c_int * 3)(*L3.nodes),
+                   (C.c_double * 3)(*L3.origin()), (C.c_double * 3)(*L3.spacing()), last.data_ptr(), 1,
+                   C.byref(eng.ps), l3tab.data_ptr(), kern.stream_ptr(stream))
+            l3kw["src_tab"] = l3tab
 
         def l3():
             kern.level_step(eng.ps, stream=stream, pdl=1, **l3kw)
@@ -615,6 +673,28 @@ def run_ours(args):
             t = s.elapsed_time(e) / reps
             k1_ms = t if k1_ms is None else min(k1_ms, t)
         del graph
+        # the two-step kernel as the subcycle runs it (paired fine steps), graph-replayed the same way
+        k2_ms = None
+        if N.props_constant(eng.ps):
+            l3pair = pair_launcher(eng, last_chunk)
+            for _ in range(5):
+                l3pair()
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=stream):
+                for _ in range(reps):
+                    l3pair()
+            torch.cuda.synchronize()
+            for _ in range(3):
+                flush.zero_()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                graph.replay()
+                e.record(stream)
+                torch.cuda.synchronize()
+                t = s.elapsed_time(e) / reps
+                k2_ms = t if k2_ms is None else min(k2_ms, t)
+            del graph, l3pair
         # the two multi-step Level-3 launches, N3 fine steps a launch, launches back to back
         preps = 10
 
@@ -665,6 +745,12 @@ def run_ours(args):
         kname = f"level_sep_steps_kernel (Level 3, {N3} fine steps a launch, grid barriers)"
         traffic = profile_traffic(STEPS_PROFILE)
         tsrc = "profiles/level3_steps_part_scale.txt (ncu capture of this workload, not of this run)"
+    elif pairs and k2_ms is not None:
+        alg_bytes = 20.0 * L3.nn
+        k_ms = k2_ms
+        kname = l3_kernel_name(tuned.get("3pair"))
+        traffic = profile_traffic(PAIR_PROFILE)
+        tsrc = "profiles/level_sep2_l3_part_scale.txt (ncu capture of this workload, not of this run)"
     else:
         alg_bytes = 10.0 * L3.nn
         k_ms = k1_ms
@@ -687,6 +773,9 @@ def run_ours(args):
                      "phase byte read + write)", "peak_kind": peak_kind,
                      "one_step_kernel": {"kernel": l3_kernel_name(tuned.get(3)), "ms": k1_ms,
                                          "frac": 10.0 * L3.nn / (k1_ms * 1e-3) / 1e9 / peak},
+                     "two_step_kernel": None if k2_ms is None else {
+                         "kernel": "level_sep2_kernel (two fine steps a launch)", "ms_per_launch": k2_ms,
+                         "ms_per_fine_step": k2_ms / 2, "frac": 20.0 * L3.nn / (k2_ms * 1e-3) / 1e9 / peak},
                      "persistent_kernel": None if kp_ms is None else {
                          "kernel": f"level3_persist_kernel ({N3} fine steps a launch)", "ms_per_launch": kp_ms,
                          "ms_per_fine_step": kp_ms / N3, "frac": 10.0 * L3.nn * N3 / (kp_ms * 1e-3) / 1e9 / peak},
@@ -696,6 +785,7 @@ def run_ours(args):
         "clocks": clk,
         "subcycle_as_cuda_graph": not args.no_graph,
         "level3_persistent": persist,
+        "level3_paired_steps": pairs,
         "autotuned": {f"L{lev}": shape_json(v) for lev, v in tuned.items()},  # L3acc: the corrector's step
     }
     if args.fp64_steps > 0:
@@ -1220,9 +1310,12 @@ def run_unet_only(args):
 def run_kernel_only(args):
     """The dominant kernel alone on the workload's Level-3 window after
     --warmup subcycle calls (the case the ncu summaries under profiles/ use)."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
+    import _native as N
     import engine
     import kern
 
@@ -1235,6 +1328,25 @@ def run_kernel_only(args):
     for k in range(args.warmup):
         eng.move(rows[k * n23], vstart)
         eng.subcycle(rows[k * n23:(k + 1) * n23])
+    if args.pair_only:  # the two-step Level-3 kernel: --steps launches of two fine steps
+        tuned = eng.autotune(rows[0])
+        chunk = rows[(args.warmup - 1) * n23:args.warmup * n23]
+        launch = pair_launcher(eng, chunk, accum=args.l3_accum)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("level3_steps")  # ncu --nvtx --nvtx-include level3_steps/
+        with torch.cuda.stream(eng.stream):
+            e0.record(eng.stream)
+            for _ in range(args.steps):
+                launch()
+            e1.record(eng.stream)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        key = "3pair_acc" if args.l3_accum else "3pair"
+        print(json.dumps({"kernel_only": "level_sep2_kernel (two fine steps a launch)", "launches": args.steps,
+                          "nodes": eng.geo.L[3].nn, "us_per_launch_host_issued": 1000 * e0.elapsed_time(e1) / args.steps,
+                          "shape": shape_json(tuned[key]) if key in tuned else None}))
+        return
     if args.persist_only:  # a multi-step Level-3 kernel (--persist 1 or 2): --steps launches of N3 fine steps
         eng.autotune(rows[0])
         chunk = rows[(args.warmup - 1) * n23:args.warmup * n23]
@@ -1271,6 +1383,14 @@ def run_kernel_only(args):
     Tout = torch.empty_like(eng.T[3])
     phout = torch.empty_like(eng.ph[3])
     ring = eng._ring(3, eng.T[2], eng.T[2])
+    kw = eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5,
+                          accum=args.l3_accum)
+    if N.props_constant(eng.ps):  # laser factors from a table, as the subcycle passes them
+        L3 = eng.geo.L[3]
+        kw["src_tab"] = torch.empty(int(sum(L3.nodes)), dtype=eng.dtype, device=eng.dev)
+        N.call("gm_fine_source_tables", kern.dtype_code(kw["src_tab"]), (C.c_int * 3)(*L3.nodes),
+               (C.c_double * 3)(*L3.origin()), (C.c_double * 3)(*L3.spacing()), last.data_ptr(), 1, C.byref(eng.ps),
+               kw["src_tab"].data_ptr(), kern.stream_ptr(eng.stream))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("level3_steps")  # ncu --nvtx --nvtx-include level3_steps/
@@ -1278,12 +1398,9 @@ def run_kernel_only(args):
         e0.record(eng.stream)
         for _ in range(args.steps):
             if args.l3_shape:
-                kern.level_step_shape(eng.ps, stream=eng.stream, **shape,
-                                      **eng.level_kwargs(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last,
-                                                         ring=ring, alpha=0.5, accum=args.l3_accum))
+                kern.level_step_shape(eng.ps, stream=eng.stream, **shape, **kw)
             else:
-                eng._level(3, eng.T[3], Tout, last[5:6], eng.ph[3], phout, laser=last, ring=ring, alpha=0.5,
-                           accum=args.l3_accum)
+                kern.level_step(eng.ps, stream=eng.stream, **kw)
         e1.record(eng.stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()

@@ -193,7 +193,7 @@ class gm_subcycle_plan(C.Structure):
         ("zchunk", C.c_int), ("ring2", vp * 2), ("ring3", vp * 2), ("graph", C.c_int),
         ("pdl", C.c_int), ("src3tab", vp), ("persist", C.c_int), ("xch3", vp * 2), ("pflags", vp),
         ("pflags_cap", C.c_longlong), ("pstatus", vp), ("inj32", C.POINTER(C.c_int) * 9),
-        ("inj21", C.POINTER(C.c_int) * 9)]
+        ("inj21", C.POINTER(C.c_int) * 9), ("l3_pairs", C.c_int)]
 
 
 class gm_persist_args(C.Structure):
@@ -213,13 +213,18 @@ class gm_steps_args(C.Structure):
                 ("tbuf", vp * 2), ("counter", vp), ("base", C.c_uint), ("status", vp)]
 
 
+class gm_level2_args(C.Structure):
+    _fields_ = [("level", gm_level_args), ("dt2", vp), ("src_tab2", vp), ("bc_alpha2", C.c_double),
+                ("bc_beta2", C.c_double)]
+
+
 class gm_toolpath_state(C.Structure):
     _fields_ = [("run", C.c_longlong), ("k", C.c_longlong), ("row", C.c_longlong), ("x", C.c_double),
                 ("y", C.c_double), ("t", C.c_double)]
 
 
 def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bool = False,
-                          inject32: bool = False, inject21: bool = False) -> int:
+                          inject32: bool = False, inject21: bool = False, pairs: bool = False) -> int:
     """Kernels gm_subcycle launches: the N2 Level-2 sources (2), set-up and
     Level 1 (8), two passes of a Level-2 ring prolongation plus N2 Level-2
     steps (coupling 2 onto the step's source, Level-2 solve, Level-3 ring, N3
@@ -227,10 +232,12 @@ def subcycle_kernel_count(N2: int, N3: int, separable: bool = False, persist: bo
     (3).  For a constant-property material (separable kernels) each of the
     4 + 2 N2 coupling calls is one kernel more and the Level-3 laser factors
     are tabulated once (one kernel).  With persistent Level-3 steps the N3
-    solves of a Level-2 step are one kernel.  Where a restriction is an
+    solves of a Level-2 step are one kernel; with paired Level-3 steps
+    (gm_level_step2) they are N3 // 2 + N3 % 2.  Where a restriction is an
     injection its restriction and T' are one kernel (inject32: the 2 N2
     Level-3 ones, inject21: the two Level-2 ones)."""
-    n = 20 + 2 * (1 + N2 * (6 + (1 if persist else N3)))
+    n3 = 1 if persist else (N3 // 2 + N3 % 2 if pairs else N3)
+    n = 20 + 2 * (1 + N2 * (6 + n3))
     n -= (2 * N2 if inject32 else 0) + (2 if inject21 else 0)
     return n + (4 + 2 * N2 + 1 if separable else 0)
 
@@ -310,6 +317,10 @@ SIGNATURES = {
     "gm_level_batched_launch": [vp, C.POINTER(gm_batch_info), vp],
     "gm_level_autotune": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.c_int, C.POINTER(gm_tune_result), vp],
     "gm_level_step_shape": [C.POINTER(gm_level_args), C.POINTER(gm_props), C.POINTER(gm_level_shape), vp],
+    "gm_level_step2": [C.POINTER(gm_level2_args), C.POINTER(gm_props), vp],
+    "gm_level_step2_shape": [C.POINTER(gm_level2_args), C.POINTER(gm_props), C.POINTER(gm_level_shape), vp],
+    "gm_level_autotune2": [C.POINTER(gm_level2_args), C.POINTER(gm_props), C.c_int, C.POINTER(gm_tune_result),
+                           vp],
     "gm_fine_source_tables": [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), vp,
                               C.c_int, C.POINTER(gm_props), vp, vp],
     "gm_energy_balance": [C.POINTER(gm_energy_args), C.POINTER(gm_props), vp],

@@ -34,6 +34,7 @@ struct Ctx {
   int persist = 0;        // Level-3 steps of a Level-2 step as one launch: 1 tiles in shared memory, 2 grid steps
   unsigned pbase = 0;     // flag value at the next persistent launch (mode 1)
   int plaunch = 0;        // persistent launches issued in this call (mode 2: counter index)
+  int pairs = 0;          // Level-3 fine steps two at a time (gm_level_step2)
 };
 
 inline char* at(void* base, long long elems, size_t esz) { return (char*)base + elems * (long long)esz; }
@@ -336,15 +337,30 @@ PassOut l2_pass(Ctx& c, const void* T1new, bool part2) {
       T3c = a.T_out;
       ph3c = a.ph_out;
     }
-    for (int l3 = 0; l3 < (c.persist ? 0 : N3); ++l3) {  // one launch a fine step
+    for (int l3 = 0; l3 < (c.persist ? 0 : N3);) {  // one launch a fine step, or one a pair of them
       const int i = l2 * N3 + l3;
-      void* Tn = p.T3w[i % 2];
-      uint8_t* phn = p.ph3w[i % 2];
+      void* Tn = T3c == p.T3w[0] ? p.T3w[1] : p.T3w[0];
+      uint8_t* phn = ph3c == p.ph3w[0] ? p.ph3w[1] : p.ph3w[0];
       const double* row = p.rows + (long long)i * 7;
       const long long L3n = (long long)p.L3.nodes[0] + p.L3.nodes[1] + p.L3.nodes[2];
-      level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 3, nullptr,
-            p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr,
-            p.src3tab ? at(p.src3tab, i * L3n, c.esz) : nullptr);
+      if (c.pairs && l3 + 1 < N3) {  // steps l3 and l3 + 1 in one launch
+        gm_level2_args a2;
+        memset(&a2, 0, sizeof(a2));
+        a2.level = level_args(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row,
+                              3, nullptr, p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr,
+                              part2 ? p.macc3 : nullptr, at(p.src3tab, i * L3n, c.esz));
+        a2.dt2 = row + 7 + 5;
+        a2.src_tab2 = at(p.src3tab, (i + 1) * L3n, c.esz);
+        a2.bc_alpha2 = (l3 + 2) / (double)N3;
+        a2.bc_beta2 = 1.0 - a2.bc_alpha2;
+        GM_TRY(gm_level_step2(&a2, c.pr, c.st));
+        l3 += 2;
+      } else {
+        level(c, p.L3, p.L3.nodes[2] - 1, T3c, Tn, row + 5, ph3c, phn, nullptr, nullptr, nullptr, row, 3, nullptr,
+              p.ring3[0], p.ring3[1], (l3 + 1) / (double)N3, part2 ? p.acc3 : nullptr, part2 ? p.macc3 : nullptr,
+              p.src3tab ? at(p.src3tab, i * L3n, c.esz) : nullptr);
+        l3 += 1;
+      }
       T3c = Tn;
       ph3c = phn;
     }
@@ -398,10 +414,10 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
                                  p->src3tab, stream));
   // persistent Level-3 steps: needs the factor table, the work buffers and a
   // constant-property material; the window must have a persistent shape
+  const bool kconst = props->k_powder == props->k_bulk_a0 && props->k_fluid == props->k_bulk_a0 &&
+                      props->k_bulk_a1 == 0.0 && props->cp_solid_a1 == 0.0 && props->cp_mushy == props->cp_solid_a0 &&
+                      props->cp_fluid == props->cp_solid_a0;
   if (p->persist && p->src3tab && p->xch3[0] && p->xch3[1] && p->pflags && p->pstatus) {
-    const bool kconst = props->k_powder == props->k_bulk_a0 && props->k_fluid == props->k_bulk_a0 &&
-                        props->k_bulk_a1 == 0.0 && props->cp_solid_a1 == 0.0 &&
-                        props->cp_mushy == props->cp_solid_a0 && props->cp_fluid == props->cp_solid_a0;
     if (p->persist == 1) {
       int shp[4];
       const long long nf = gm_level3_persist_flags(p->L3.nodes);
@@ -414,6 +430,8 @@ int subcycle_issue(const gm_subcycle_plan* p, const gm_props* props, void* strea
         cudaMemsetAsync(p->pflags, 0, sizeof(unsigned) * p->pflags_cap, (cudaStream_t)stream) != cudaSuccess)
       return GM_ERR_CUDA;
   }
+  // Level-3 fine steps two at a time: constant-property materials with the factor table
+  c.pairs = (p->l3_pairs && !c.persist && p->src3tab && kconst && p->L3.nodes[2] >= 3) ? 1 : 0;
   // every later kernel of the call launches as a programmatic dependent of the one before it
   const gm::PdlScope pdl(p->pdl != 0);
 

@@ -1518,51 +1518,26 @@ extern "C" int gm_level_step_shape(const gm_level_args* a, const gm_props* p, co
   return gm::launch_level<double>(a, p, st, v);
 }
 
-extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out,
-                                 void* stream) {
-  if (!p || reps < 1) return GM_ERR_ARG;
-  const int rc = gm::check_level_args(a);
-  if (rc != GM_OK) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
+namespace gm {
+
+// Times each candidate shape as a CUDA graph of R back-to-back launches of
+// `launch(v)` (programmatic dependents of one another, as gm_subcycle issues
+// level steps), so that neither host launch overhead nor the launch gaps of
+// stream order enter the comparison; on a stream that cannot be captured (the
+// legacy default stream) the launches are timed as issued.  One untimed launch
+// precedes each candidate.  Returns the fastest in *best / *best_us.
+template <typename Launch>
+static int time_shapes(const std::vector<TuneVal>& cand, int R, cudaStream_t st, Launch launch, TuneVal* best,
+                       float* best_us) {
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess) return GM_ERR_CUDA;
   if (cudaEventCreate(&e1) != cudaSuccess) {
     cudaEventDestroy(e0);
     return GM_ERR_CUDA;
   }
-  // candidates: element tiles 32 x 8 and 16 x 16, and (where eligible) the
-  // separable kernel with 2 or 4 rows a thread and 1, 2 or 4 thread rows,
-  // each over the distinct z-chunks of 2..64 planes
-  std::vector<gm::TuneVal> cand;
-  std::vector<int> zcs;
-  for (int nch = gm::cdiv(a->nz, gm::ZMAX), last = -1; nch <= a->nz; ++nch) {
-    const int zc = gm::cdiv(a->nz, nch);
-    if (zc == last || zc < 2) continue;
-    last = zc;
-    zcs.push_back(zc);
-  }
-  for (int tx : {gm::LT_X, 16})
-    for (int zc : zcs) cand.push_back(gm::TuneVal{0, tx, 0, 0, zc});
-  if (gm::sep_eligible(a, gm::level_flags(a, p)))
-    for (int rows : {1, 2, 4})
-      for (int warps : {2, 4, 8})
-        for (int zc : zcs)
-          if (zc <= gm::SEP_ZMAX) cand.push_back(gm::TuneVal{1, gm::SEP_TILE, warps, rows, zc});
-  // Each candidate is timed as a CUDA graph of 4*reps back-to-back launches,
-  // programmatic dependents of one another (as gm_subcycle issues level
-  // steps), so that neither host launch overhead nor the launch gaps of
-  // stream order enter the comparison; on a stream that cannot be captured
-  // (the legacy default stream) the launches are timed as issued.
-  gm_level_args b = *a;
-  b.pdl = 1;  // the timed launches read the same dt, laser and factors throughout
-  auto launch = [&](const gm::TuneVal& v) {
-    return b.dtype == GM_F32 ? gm::launch_level<float>(&b, p, st, v) : gm::launch_level<double>(&b, p, st, v);
-  };
-  const int R = 4 * reps;
-  gm::TuneVal best{0, gm::LT_X, 0, 0, 0};
-  float best_us = -1.f;
+  *best_us = -1.f;
   int status = GM_OK;
-  for (const gm::TuneVal& v : cand) {
+  for (const TuneVal& v : cand) {
     status = launch(v);  // untimed first launch
     if (status != GM_OK) break;
     cudaGraphExec_t exec = nullptr;
@@ -1598,13 +1573,50 @@ extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int 
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     const float us = 1000.f * ms / R;
-    if (best_us < 0 || us < best_us) {
-      best_us = us;
-      best = v;
+    if (*best_us < 0 || us < *best_us) {
+      *best_us = us;
+      *best = v;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return status;
+}
+
+}  // namespace gm
+
+extern "C" int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out,
+                                 void* stream) {
+  if (!p || reps < 1) return GM_ERR_ARG;
+  const int rc = gm::check_level_args(a);
+  if (rc != GM_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // candidates: element tiles 32 x 8 and 16 x 16, and (where eligible) the
+  // separable kernel with 2 or 4 rows a thread and 1, 2 or 4 thread rows,
+  // each over the distinct z-chunks of 2..64 planes
+  std::vector<gm::TuneVal> cand;
+  std::vector<int> zcs;
+  for (int nch = gm::cdiv(a->nz, gm::ZMAX), last = -1; nch <= a->nz; ++nch) {
+    const int zc = gm::cdiv(a->nz, nch);
+    if (zc == last || zc < 2) continue;
+    last = zc;
+    zcs.push_back(zc);
+  }
+  for (int tx : {gm::LT_X, 16})
+    for (int zc : zcs) cand.push_back(gm::TuneVal{0, tx, 0, 0, zc});
+  if (gm::sep_eligible(a, gm::level_flags(a, p)))
+    for (int rows : {1, 2, 4})
+      for (int warps : {2, 4, 8})
+        for (int zc : zcs)
+          if (zc <= gm::SEP_ZMAX) cand.push_back(gm::TuneVal{1, gm::SEP_TILE, warps, rows, zc});
+  gm_level_args b = *a;
+  b.pdl = 1;  // the timed launches read the same dt, laser and factors throughout
+  auto launch = [&](const gm::TuneVal& v) {
+    return b.dtype == GM_F32 ? gm::launch_level<float>(&b, p, st, v) : gm::launch_level<double>(&b, p, st, v);
+  };
+  gm::TuneVal best{0, gm::LT_X, 0, 0, 0};
+  float best_us = -1.f;
+  const int status = gm::time_shapes(cand, 4 * reps, st, launch, &best, &best_us);
   if (status != GM_OK) return status;
   {
     std::lock_guard<std::mutex> lock(gm::g_tuned_mutex);
@@ -1792,6 +1804,196 @@ extern "C" int gm_level3_steps(const gm_steps_args* g, const gm_props* p, void* 
   cudaStream_t st = (cudaStream_t)stream;
   if (la->dtype == GM_F32) return gm::launch_steps<float>(g, p, st);
   return gm::launch_steps<double>(g, p, st);
+}
+
+// ---------------------------------------------------------------------------
+// Two Level-3 fine steps in one launch (gm_sep2.cuh).
+// ---------------------------------------------------------------------------
+#include "gm_sep2.cuh"
+
+namespace gm {
+
+constexpr int LF_TWO = 1 << 14;  // tune-key bit: the two-step kernel's shape
+
+template <typename real, int FL, int BYT>
+static void launch_sep2_t(const LevelK<real>& a, const Step2<real>& b, int warps, int zc, bool pdl, cudaStream_t st) {
+  LevelK<real> c = a;
+  c.zchunk = zc;
+  // z-slices: the marching chunks, the two top planes, the Dirichlet nodes
+  const dim3 grid(cdiv(a.nx, SEP2_TILE), cdiv(a.ny, warps * BYT), sep2_march_chunks(a.ne_planes, zc) + 2);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(32 * warps);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, level_sep2_kernel<real, BYT, FL>, c, b);
+}
+
+// The two-step kernel serves constant-property Level-3 calls (laser factors
+// from tables for both steps, surface flux, clamp, ring arrays, phase in and
+// out, optional melt time) whose nodes are all at or below the top plane.
+static bool sep2_eligible(const gm_level2_args* g, int fl) {
+  const gm_level_args& a = g->level;
+  return (fl == (LF_L3 | LF_CONST) || fl == (LF_L3ACC | LF_CONST)) && a.ne_planes == a.nz - 1 && a.nz >= 3 &&
+         a.src_tab && g->src_tab2 && g->dt2;
+}
+
+template <typename real>
+static int launch_sep2(const gm_level2_args* g, const gm_props* pr, const TuneVal& v, cudaStream_t st) {
+  const gm_level_args* la = &g->level;
+  const int fl = level_flags(la, pr);
+  if (!sep2_eligible(g, fl)) return GM_ERR_UNSUPPORTED;
+  if ((v.rows != 1 && v.rows != 2 && v.rows != 4) || v.wys < 1 || v.wys > 8 || v.zchunk < 1 ||
+      v.zchunk > SEP2_ZMAX)
+    return GM_ERR_ARG;
+  const LevelK<real> a = make_levelk<real>(la, pr);
+  Step2<real> b;
+  b.dt = g->dt2;
+  b.src_tab = (const real*)g->src_tab2;
+  b.bc_alpha = (real)g->bc_alpha2;
+  b.bc_beta = (real)g->bc_beta2;
+  const bool pdl = la->pdl != 0;
+  constexpr int fa = LF_L3 | LF_CONST, fb = LF_L3ACC | LF_CONST;
+  if (v.rows == 1) {
+    if (fl == fa)
+      launch_sep2_t<real, fa, 1>(a, b, v.wys, v.zchunk, pdl, st);
+    else
+      launch_sep2_t<real, fb, 1>(a, b, v.wys, v.zchunk, pdl, st);
+  } else if (v.rows == 2) {
+    if (fl == fa)
+      launch_sep2_t<real, fa, 2>(a, b, v.wys, v.zchunk, pdl, st);
+    else
+      launch_sep2_t<real, fb, 2>(a, b, v.wys, v.zchunk, pdl, st);
+  } else {
+    if (fl == fa)
+      launch_sep2_t<real, fa, 4>(a, b, v.wys, v.zchunk, pdl, st);
+    else
+      launch_sep2_t<real, fb, 4>(a, b, v.wys, v.zchunk, pdl, st);
+  }
+  return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+}
+
+// Untuned two-step shape: 2 rows a thread, 4-warp CTAs, and the z-chunk whose
+// CTA count best fills the SMs (busiest SM's CTAs x (planes + 4 halo planes)).
+static TuneVal sep2_default(const gm_level_args* g) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms = n > 0 ? n : 152;
+  }
+  TuneVal v{2, SEP2_TILE, 4, 2, 1};
+  const int res = g->dtype == GM_F32 ? 4 : 2;  // resident 4-warp CTAs per SM
+  const long long gxy = (long long)cdiv(g->nx, SEP2_TILE) * cdiv(g->ny, v.wys * v.rows);
+  const int nplanes = g->ne_planes - 2;
+  double best = -1;
+  for (int zc = 1; zc <= min(max(nplanes, 1), SEP2_ZMAX); ++zc) {
+    const long long ctas = gxy * (sep2_march_chunks(g->ne_planes, zc) + 1);
+    const long long waves = (ctas + (long long)sms * res - 1) / ((long long)sms * res);
+    const double cost = (double)waves * (zc + 4);
+    if (best < 0 || cost < best - 1e-9) {
+      best = cost;
+      v.zchunk = zc;
+    }
+  }
+  return v;
+}
+
+static int check_level2_args(const gm_level2_args* g, const gm_props* p) {
+  if (!g || !p) return GM_ERR_ARG;
+  const int rc = check_level_args(&g->level);
+  if (rc != GM_OK) return rc;
+  const gm_level_args& a = g->level;
+  if (!g->dt2 || !a.ph_in || !a.ph_out || a.ph_in == a.ph_out || a.bc_mode != 3 || !a.laser) return GM_ERR_ARG;
+  if (!sep2_eligible(g, level_flags(&a, p))) return GM_ERR_UNSUPPORTED;
+  return GM_OK;
+}
+
+template <typename real>
+static int launch_level2(const gm_level2_args* g, const gm_props* p, cudaStream_t st, TuneVal sh) {
+  if (sh.kernel < 0) {
+    const gm_level_args* la = &g->level;
+    TuneVal v;
+    if (la->zchunk <= 0 && tuned_shape(TuneKey{la->dtype, level_flags(la, p) | LF_TWO, la->nx, la->ny, la->nz}, &v))
+      sh = v;
+    else
+      sh = sep2_default(la);
+    if (la->zchunk > 0) sh.zchunk = la->zchunk;
+  }
+  return launch_sep2<real>(g, p, sh, st);
+}
+
+}  // namespace gm
+
+extern "C" int gm_level_step2(const gm_level2_args* a, const gm_props* p, void* stream) {
+  const int rc = gm::check_level2_args(a, p);
+  if (rc != GM_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const gm::TuneVal none{-1, 0, 0, 0, 0};
+  if (a->level.dtype == GM_F32) return gm::launch_level2<float>(a, p, st, none);
+  return gm::launch_level2<double>(a, p, st, none);
+}
+
+extern "C" int gm_level_step2_shape(const gm_level2_args* a, const gm_props* p, const gm_level_shape* shape,
+                                    void* stream) {
+  if (!shape) return GM_ERR_ARG;
+  const int rc = gm::check_level2_args(a, p);
+  if (rc != GM_OK) return rc;
+  if (shape->kernel != 2) return GM_ERR_ARG;
+  const gm::TuneVal v{2, gm::SEP2_TILE, shape->tile_y, shape->rows, shape->zchunk};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a->level.dtype == GM_F32) return gm::launch_level2<float>(a, p, st, v);
+  return gm::launch_level2<double>(a, p, st, v);
+}
+
+extern "C" int gm_level_autotune2(const gm_level2_args* a, const gm_props* p, int reps, gm_tune_result* out,
+                                  void* stream) {
+  if (reps < 1) return GM_ERR_ARG;
+  const int rc = gm::check_level2_args(a, p);
+  if (rc != GM_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nplanes = a->level.ne_planes - 2;
+  std::vector<int> zcs;
+  for (int nch = gm::cdiv(nplanes > 0 ? nplanes : 1, gm::SEP2_ZMAX), last = -1; nch <= (nplanes > 0 ? nplanes : 1);
+       ++nch) {
+    const int zc = gm::cdiv(nplanes > 0 ? nplanes : 1, nch);
+    if (zc == last) continue;
+    last = zc;
+    zcs.push_back(zc);
+  }
+  std::vector<gm::TuneVal> cand;
+  for (int rows : {1, 2, 4})
+    for (int warps : {2, 4, 8})
+      for (int zc : zcs) cand.push_back(gm::TuneVal{2, gm::SEP2_TILE, warps, rows, zc});
+  gm_level2_args b = *a;
+  b.level.pdl = 1;
+  auto launch = [&](const gm::TuneVal& v) {
+    return b.level.dtype == GM_F32 ? gm::launch_level2<float>(&b, p, st, v) : gm::launch_level2<double>(&b, p, st, v);
+  };
+  gm::TuneVal best{2, gm::SEP2_TILE, 4, 2, 1};
+  float best_us = -1.f;
+  const int status = gm::time_shapes(cand, 4 * reps, st, launch, &best, &best_us);
+  if (status != GM_OK) return status;
+  {
+    std::lock_guard<std::mutex> lock(gm::g_tuned_mutex);
+    gm::g_tuned[gm::TuneKey{a->level.dtype, gm::level_flags(&a->level, p) | gm::LF_TWO, a->level.nx, a->level.ny,
+                            a->level.nz}] = best;
+  }
+  if (out) {
+    out->kernel = 2;
+    out->zchunk = best.zchunk;
+    out->us = best_us;
+    out->tile_x = gm::SEP2_TILE;
+    out->tile_y = best.wys;
+    out->rows = best.rows;
+  }
+  return GM_OK;
 }
 
 extern "C" const char* gm_version(void) { return "gomelt-gb300 0.1 (sm_103a)"; }

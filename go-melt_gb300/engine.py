@@ -233,6 +233,8 @@ class Engine:
         # (gm_level3_persist, where the window has a shape), 2 the one-step kernel's body with grid barriers
         # (gm_level3_steps); constant-property materials only
         self.use_persist = 0
+        # with one launch a step: the Level-3 steps two at a time (gm_level_step2; constant-property materials)
+        self.use_pairs = True
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)  # GM_PERSIST_* bits of the device kernels
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
@@ -420,7 +422,10 @@ class Engine:
         (gm_level_autotune); later level steps of the same shapes use the
         fastest.  Needs the tables of a move; writes only scratch outputs;
         synchronises the stream.  Returns {level: kern.TunedShape}, the
-        Level-3 step with the melt-time update under "3acc"."""
+        Level-3 step with the melt-time update under "3acc" and, for a
+        constant-property material, the two-step kernel (gm_level_step2)
+        under "3pair" / "3pair_acc"; the subcycle then takes its Level-3 steps
+        two at a time if that measured faster per step (use_pairs)."""
         g = self.geo
         t = self.tables
         if t is None:
@@ -434,6 +439,15 @@ class Engine:
             if lev == 3:
                 kw = self.level_kwargs(3, self.T[3], To, rowd[5:6], self.ph[3], Po, laser=rowd,
                                        ring=self._ring(3, self.T[2], self.T[2]), alpha=0.5)
+                tab = None
+                if N.props_constant(self.ps):  # the subcycle's Level-3 steps read tabulated laser factors
+                    nl = int(sum(L.nodes))
+                    tab = self._buf("tuneTab", 2 * nl)
+                    rows2 = torch.stack([rowd, rowd])
+                    N.call("gm_fine_source_tables", kern.dtype_code(self.T[3]), (C.c_int * 3)(*L.nodes),
+                           (C.c_double * 3)(*L.origin()), (C.c_double * 3)(*L.spacing()), rows2.data_ptr(), 2,
+                           C.byref(self.ps), tab.data_ptr(), kern.stream_ptr(self.stream))
+                    kw["src_tab"] = tab[:nl]
             else:
                 cg = t["c32"] if lev == 2 else t["c21"]
                 box = [v for d in range(3) for v in (cg.box_lo[d], cg.box_lo[d] + cg.box_n[d])]
@@ -451,6 +465,15 @@ class Engine:
                     macc.zero_()
                 kw.update(accum=acc, max_accum=macc)
                 out["3acc"] = kern.level_autotune(self.ps, reps=reps, stream=self.stream, **kw)
+                if tab is not None and L.nodes[2] >= 3:
+                    # the two-step kernel (the subcycle's paired steps), with and without melt time
+                    kw2 = dict(kw)
+                    two = dict(dt2=rowd[5:6], src_tab2=tab[nl:], bc_alpha2=0.6, bc_beta2=0.4)
+                    out["3pair_acc"] = kern.level_autotune2(self.ps, reps=reps, stream=self.stream, **two, **kw2)
+                    kw2.pop("accum")
+                    kw2.pop("max_accum")
+                    out["3pair"] = kern.level_autotune2(self.ps, reps=reps, stream=self.stream, **two, **kw2)
+                    self.use_pairs = out["3pair"].us + out["3pair_acc"].us < 2.0 * (out[3].us + out["3acc"].us)
         return out
 
     def _l0_gather(self, idx, n, ph_out, prev_ph, prev_lo, prev_n):
@@ -664,7 +687,8 @@ class Engine:
             return out_hist
         N.call("gm_subcycle", C.byref(p), C.byref(self.ps), kern.stream_ptr(self.stream),
                kernels=N.subcycle_kernel_count(N2, N3, N.props_constant(self.ps), persist=bool(p.persist),
-                                              inject32=bool(p.inj32[0]), inject21=bool(p.inj21[0])))
+                                              inject32=bool(p.inj32[0]), inject21=bool(p.inj21[0]),
+                                              pairs=self.pairs_active(p)))
         self.s2_prev_lo = [int(np.asarray(g.L0_overlap[d])[0]) for d in range(3)]
         return out_hist
 
@@ -752,8 +776,15 @@ class Engine:
                 p.persist = mode
                 p.xch3[0], p.xch3[1] = self._buf("xch3a", nn3).data_ptr(), self._buf("xch3b", nn3).data_ptr()
                 p.pflags, p.pflags_cap = self._buf("pflags", nf, torch.int32).data_ptr(), nf
+            p.l3_pairs = 1 if (self.use_pairs and not p.persist) else 0
         p.pstatus = self.status.data_ptr()  # every level step reports non-finite / out-of-range values here
         return p
+
+    def pairs_active(self, p) -> bool:
+        """Whether gm_subcycle takes the Level-3 steps of plan p two at a
+        time (its own condition: constant properties, the factor table, no
+        persistent steps, at least three node planes)."""
+        return bool(p.l3_pairs and not p.persist and p.src3tab and self.geo.L[3].nodes[2] >= 3)
 
     def persist_shape(self):
         """Tile shape of the persistent Level-3 kernel on this window ({tiles,
@@ -962,7 +993,7 @@ def subcycle_batched(engines, rows_list, rows_device=None, dts_device=None):
         plans[i] = e._last_plan
         props[i] = e.ps
         kernels += N.subcycle_kernel_count(e.N2, e.N3, N.props_constant(e.ps), inject32=bool(plans[i].inj32[0]),
-                                           inject21=bool(plans[i].inj21[0]))
+                                           inject21=bool(plans[i].inj21[0]), pairs=e.pairs_active(plans[i]))
     N.call("gm_subcycle_batched", plans, len(engines), props, kern.stream_ptr(st), kernels=kernels)
     for e in engines:
         g = e.geo

@@ -88,6 +88,37 @@ def level_step_shape(props: N.gm_props, *, kernel, zchunk, tile_x=32, tile_y=1, 
     N.call("gm_level_step_shape", C.byref(a), C.byref(props), C.byref(s), stream_ptr(stream))
 
 
+def level2_args(*, dt2, src_tab2, bc_alpha2, bc_beta2, **kw):
+    """gm_level2_args: the first step as level_args(**kw), then the second
+    step's dt, laser factor row and ring blend."""
+    a = N.gm_level2_args()
+    a.level = level_args(**kw)
+    a.dt2 = ptr(dt2)
+    a.src_tab2 = ptr(src_tab2)
+    a.bc_alpha2, a.bc_beta2 = float(bc_alpha2), float(bc_beta2)
+    return a
+
+
+def level_step2(props: N.gm_props, *, stream=None, shape=None, **kw):
+    """gm_level_step2 (two Level-3 fine steps in one launch) with the
+    arguments of level2_args; shape = (rows, tile_y, zchunk) forces a launch
+    shape (gm_level_step2_shape)."""
+    a = level2_args(**kw)
+    if shape is None:
+        N.call("gm_level_step2", C.byref(a), C.byref(props), stream_ptr(stream))
+    else:
+        s = N.gm_level_shape(2, 28, int(shape[1]), int(shape[0]), int(shape[2]))
+        N.call("gm_level_step2_shape", C.byref(a), C.byref(props), C.byref(s), stream_ptr(stream))
+
+
+def level_autotune2(props: N.gm_props, *, reps=5, stream=None, **kw) -> TunedShape:
+    """gm_level_autotune2 for the two-step call level2_args(**kw) describes."""
+    a = level2_args(**kw)
+    r = N.gm_tune_result()
+    N.call("gm_level_autotune2", C.byref(a), C.byref(props), int(reps), C.byref(r), stream_ptr(stream), kernels=0)
+    return TunedShape(r.tile_x, r.tile_y, r.zchunk, r.us, r.kernel, r.rows)
+
+
 def level_args(*, T_in, T_out, nodes, h, origin, ne_planes, dt, ph_in=None, ph_out=None,
                substrate=0, k_arr=None, rc_arr=None, F_full=None, corr_full=None, rhs_box=None, box=None,
                laser=None, surface=0, bc_mode=0, face=None, inactive_amb=0, bc_new=None, bc_old=None,

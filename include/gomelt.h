@@ -318,6 +318,42 @@ typedef struct gm_tune_result {
 
 int gm_level_autotune(const gm_level_args* a, const gm_props* p, int reps, gm_tune_result* out, void* stream);
 
+/* Two consecutive Level-3 fine steps in ONE launch: the N3 inner steps of
+ * computeSolutions_L3 within subcycleGOMELT's innermost lax.scan
+ * (computeFunctions.py:3015-3054, :3404-3430, :3586-3622) taken two at a
+ * time.  `level` is the first step (its dt, src_tab, bc_alpha / bc_beta)
+ * and carries everything both steps share; dt2, src_tab2 and bc_alpha2 /
+ * bc_beta2 are the second step's.  T_out, ph_out and the melt-time arrays
+ * receive the fields after both steps, equal bit for bit to gm_level_step of
+ * the first step followed by gm_level_step of the second on its output; the
+ * intermediate fields are never written (the first step's values stay in the
+ * kernel's registers).  Serves the constant-property Level-3 feature set:
+ * laser factors from tables for both steps (src_tab and src_tab2 of
+ * gm_fine_source_tables), surface flux, clamp, bc_mode 3 ring arrays, phase
+ * in and out, optional melt time, ne_planes = nz - 1, nz >= 3; anything else
+ * returns GM_ERR_UNSUPPORTED.  pdl as gm_level_step.  No counterpart in the
+ * reference (which takes the steps one at a time). */
+typedef struct gm_level2_args {
+  gm_level_args level;
+  const double* dt2;           /* device pointer: the second step's time step */
+  const void* src_tab2;        /* the second step's laser factors (one gm_fine_source_tables row) */
+  double bc_alpha2, bc_beta2;  /* the second step's ring blend */
+} gm_level2_args;
+
+int gm_level_step2(const gm_level2_args* a, const gm_props* p, void* stream);
+
+/* gm_level_step2 with an explicit launch shape: kernel 2, rows (1, 2 or 4)
+ * y rows a thread, tile_y (1..8) warps a CTA of 28 node columns each, zchunk
+ * (1..30) output planes a CTA marches. */
+int gm_level_step2_shape(const gm_level2_args* a, const gm_props* p, const gm_level_shape* shape, void* stream);
+
+/* Autotuner of gm_level_step2 (as gm_level_autotune: CUDA-graph timing of
+ * 4*reps back-to-back programmatic-dependent launches per candidate; writes
+ * T_out / ph_out / melt time; synchronises; not during stream capture): the
+ * fastest rows x warps x z-chunk is kept for later calls with the same dtype,
+ * features and grid that leave zchunk at 0.  Result kernel = 2. */
+int gm_level_autotune2(const gm_level2_args* a, const gm_props* p, int reps, gm_tune_result* out, void* stream);
+
 /* Prolongation of one or two coarse fields onto the Dirichlet ring of a fine
  * level (faces x0, x1, y0, y1 and the bottom plane), written at the ring
  * nodes' ids in full-size arrays: outA = I(srcA), outB = I(srcB) (the
@@ -548,6 +584,9 @@ typedef struct gm_subcycle_plan {
                                 Level 2 when that restriction is an injection (its T' then takes one
                                 launch) */
   const int* inj21[9];       /* the same for Level 2 -> Level 1 */
+  int l3_pairs;              /* 1: the N3 Level-3 steps of a Level-2 step two at a time (gm_level_step2;
+                                constant-property materials with src3tab, persist 0; an odd N3 ends
+                                with one single step); 0: one launch a step */
 } gm_subcycle_plan;
 
 /* The whole subcycleGOMELT call (:3224-3632) enqueued on `stream`. */
