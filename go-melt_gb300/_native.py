@@ -74,7 +74,7 @@ class gm_conv_args(C.Structure):
     _fields_ = [("grid", C.c_int * 4), ("cin", C.c_int), ("cout", C.c_int), ("in_", vp), ("in_stride", C.c_int),
                 ("in_off", C.c_int), ("w", vp), ("bias", vp), ("relu", C.c_int), ("mask", vp),
                 ("mask_stride", C.c_int), ("mask_off", C.c_int), ("mirror", C.c_int), ("out", vp),
-                ("out_stride", C.c_int), ("out_off", C.c_int)]
+                ("out_stride", C.c_int), ("out_off", C.c_int), ("wpack", vp)]
 
 
 class gm_wgrad_args(C.Structure):

@@ -382,6 +382,79 @@ __global__ void up2_kernel(Grid5 g, int C, const uint16_t* in, int is, int io, u
   }
 }
 
+// The same two kernels eight channels (16 bytes) a thread, for channel counts,
+// slice offsets and strides that are multiples of 8 and 16-byte aligned
+// bases (every tensor of the surrogate's U-Net); per channel the arithmetic
+// and its order are those of the element-wise forms (same bits).  Voxel ids
+// are 32-bit (grids below 2^31 voxels).
+__device__ __forceinline__ void bf8_to_f(const uint4 q, float (&f)[8]) {
+  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    f[2 * i] = __uint_as_float(w[i] << 16);
+    f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+__device__ __forceinline__ uint4 f_to_bf8(const float (&f)[8]) {
+  uint32_t w[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    w[i] = *reinterpret_cast<uint32_t*>(&v);
+  }
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// pool (mode 0) / up (mode 1), forward or backward, 8 channels a thread.
+// Fine-to-coarse sums (pool forward, up backward) add the 8 fine voxels in
+// the order k = 0..7 and scale by `scale` (0.125 or 1); coarse-to-fine copies
+// (up forward) or scaled copies (pool backward, scale 0.125) otherwise.
+__global__ void resample8_kernel(Grid5 g, int C8, const uint16_t* in, int is, int io, uint16_t* out, int os, int oo,
+                                 int gather, float scale, int copy) {
+  const unsigned Xc = g.X / 2, Yc = g.Y / 2, Zc = g.Z / 2;
+  if (gather) {  // out on the coarse grid, sum of 8 fine voxels
+    const unsigned n = (unsigned)g.B * Xc * Yc * Zc * C8;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const unsigned c8 = i % C8, v = i / C8;
+      const unsigned x = v % Xc, y = (v / Xc) % Yc, t = v / (Xc * Yc), z = t % Zc, b = t / Zc;
+      float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const unsigned f = ((b * g.Z + 2 * z + (k >> 2)) * g.Y + 2 * y + ((k >> 1) & 1)) * g.X + 2 * x + (k & 1);
+        float e[8];
+        bf8_to_f(__ldg(reinterpret_cast<const uint4*>(in + (size_t)f * is + io) + c8), e);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) s[q] += e[q];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s[q] = scale * s[q];
+      reinterpret_cast<uint4*>(out + (size_t)v * os + oo)[c8] = f_to_bf8(s);
+    }
+  } else {  // out on the fine grid from its coarse voxel
+    const unsigned n = (unsigned)g.B * g.X * g.Y * g.Z * C8;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      const unsigned c8 = i % C8, f = i / C8;
+      const unsigned x = f % g.X, y = (f / g.X) % g.Y, t = f / (g.X * g.Y), z = t % g.Z, b = t / g.Z;
+      const unsigned v = ((b * Zc + z / 2) * Yc + y / 2) * Xc + x / 2;
+      uint4 q = __ldg(reinterpret_cast<const uint4*>(in + (size_t)v * is + io) + c8);
+      if (!copy) {
+        float e[8];
+        bf8_to_f(q, e);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) e[k] = scale * e[k];
+        q = f_to_bf8(e);
+      }
+      reinterpret_cast<uint4*>(out + (size_t)f * os + oo)[c8] = q;
+    }
+  }
+}
+
+static bool vec8_ok(const int grid[4], int C, const void* in, int is, int io, const void* out, int os, int oo) {
+  const long long V = (long long)grid[0] * grid[1] * grid[2] * grid[3];
+  return C % 8 == 0 && is % 8 == 0 && io % 8 == 0 && os % 8 == 0 && oo % 8 == 0 &&
+         !(((uintptr_t)in | (uintptr_t)out) & 15) && V * (C / 8) < (1LL << 31) && V * (long long)(is > os ? is : os) < (1LL << 62);
+}
+
 // b += a (where mask > 0, if a mask is given): the gradient of a tensor used
 // twice, the second path's gradient passed through the ReLU of its producer.
 __global__ void add_slice_kernel(long long V, int C, const uint16_t* a, int as, int ao, uint16_t* b, int bs, int bo,
@@ -675,6 +748,11 @@ extern "C" int gm_unet_pool2(const int grid[4], int C, const void* in, int is, i
                              int backward, void* stream) {
   if (!grid || !in || !out || C < 1 || grid[1] % 2 || grid[2] % 2 || grid[3] % 2) return GM_ERR_ARG;
   const long long n = (long long)grid[0] * grid[1] * grid[2] * grid[3] * C;
+  if (vec8_ok(grid, C, in, is, io, out, os, oo)) {  // 8 channels a thread
+    resample8_kernel<<<ugrid(n / 8), 256, 0, (cudaStream_t)stream>>>(grid5(grid), C / 8, (const uint16_t*)in, is, io,
+                                                                     (uint16_t*)out, os, oo, !backward, 0.125f, 0);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+  }
   pool2_kernel<<<ugrid(n), 256, 0, (cudaStream_t)stream>>>(grid5(grid), C, (const uint16_t*)in, is, io,
                                                            (uint16_t*)out, os, oo, backward);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
@@ -684,6 +762,11 @@ extern "C" int gm_unet_up2(const int grid[4], int C, const void* in, int is, int
                            int backward, void* stream) {
   if (!grid || !in || !out || C < 1 || grid[1] % 2 || grid[2] % 2 || grid[3] % 2) return GM_ERR_ARG;
   const long long n = (long long)grid[0] * grid[1] * grid[2] * grid[3] * C;
+  if (vec8_ok(grid, C, in, is, io, out, os, oo)) {  // 8 channels a thread
+    resample8_kernel<<<ugrid(n / 8), 256, 0, (cudaStream_t)stream>>>(grid5(grid), C / 8, (const uint16_t*)in, is, io,
+                                                                     (uint16_t*)out, os, oo, backward, 1.f, !backward);
+    return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;
+  }
   up2_kernel<<<ugrid(n), 256, 0, (cudaStream_t)stream>>>(grid5(grid), C, (const uint16_t*)in, is, io,
                                                          (uint16_t*)out, os, oo, backward);
   return cudaGetLastError() == cudaSuccess ? GM_OK : GM_ERR_LAUNCH;

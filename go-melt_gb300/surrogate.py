@@ -89,7 +89,10 @@ class UNet:
             a.mask, a.mask_stride, a.mask_off = mask[0].data_ptr(), mask[1], mask[2]
         a.mirror = mirror
         a.out, a.out_stride, a.out_off = out[0].data_ptr(), out[1], out[2]
-        self._call("gm_unet_conv3", C.byref(a))
+        # work of the tensor-core form: the weights in its tile layout (one buffer, calls in stream order)
+        a.wpack = self._buf("wpack", (27 * cin * cout,), torch.bfloat16, grow=True).data_ptr()
+        kernels = 2 if N.lib().gm_unet_conv3_tc_eligible(C.byref(a)) else 1
+        self._call("gm_unet_conv3", C.byref(a), kernels=kernels)
 
     def _wgrad(self, grid, cin, cout, inp, dy, dw):
         need = int(N.lib().gm_unet_wgrad_scratch(_i4(grid), cin, cout))

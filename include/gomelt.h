@@ -813,6 +813,10 @@ typedef struct gm_conv_args {
   int mirror;            /* 1: tap offsets negated (data gradient with W^T) */
   void* out;             /* BF16 */
   int out_stride, out_off;
+  void* wpack;           /* optional work of the tensor-core form (27 cin cout BF16): the weights are
+                            repacked into it once per call in the layout of its shared-memory weight
+                            tiles, so each tile arrives as one contiguous bulk copy; NULL: the tiles are
+                            gathered from w by tensor copies of 16-byte rows */
 } gm_conv_args;
 
 /* y[v][co] = act(bias[co] + sum_tap sum_ci x[v + d(tap)][ci] w[tap][co][ci])

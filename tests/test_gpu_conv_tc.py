@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _conv(entry, B, X, Y, Z, cin, cout, xin, in_stride, in_off, Wb, bias, relu, out, out_stride, out_off,
-          mask=None, mask_stride=0, mask_off=0, mirror=0):
+          mask=None, mask_stride=0, mask_off=0, mirror=0, wpack=None):
     import _native as N
     import kern
 
@@ -30,6 +30,8 @@ def _conv(entry, B, X, Y, Z, cin, cout, xin, in_stride, in_off, Wb, bias, relu, 
     if mask is not None:
         a.mask, a.mask_stride, a.mask_off = mask.data_ptr(), mask_stride, mask_off
     a.out, a.out_stride, a.out_off = out.data_ptr(), out_stride, out_off
+    if wpack is not None:
+        a.wpack = wpack.data_ptr()
     rc = getattr(N.lib(), entry)(C.byref(a), kern.stream_ptr())
     torch.cuda.synchronize()
     return rc, a
@@ -51,12 +53,16 @@ def test_conv3_tc_forward(cin, cout, grid):
     Wb = W.to(torch.bfloat16).contiguous()
     V = B * X * Y * Z
     outs = {}
-    for entry in ("gm_unet_conv3_tc", "gm_unet_conv3_mma"):
+    wp = torch.full((27 * cin * cout,), float("nan"), dtype=torch.bfloat16, device="cuda")
+    for entry, wpack in (("gm_unet_conv3_tc", None), ("gm_unet_conv3_tc", wp), ("gm_unet_conv3_mma", None)):
         out = torch.full((V, cout), float("nan"), dtype=torch.bfloat16, device="cuda")
-        rc, a = _conv(entry, B, X, Y, Z, cin, cout, xin, cin, 0, Wb, b, 1, out, cout, 0)
+        rc, a = _conv(entry, B, X, Y, Z, cin, cout, xin, cin, 0, Wb, b, 1, out, cout, 0, wpack=wpack)
         assert rc == N.GM_OK, entry
-        outs[entry] = _from_cl(out, B, cout, Z, Y, X)
-        _close(outs[entry], ref, 1e-2)
+        key = entry + ("+wpack" if wpack is not None else "")
+        outs[key] = _from_cl(out, B, cout, Z, Y, X)
+        _close(outs[key], ref, 1e-2)
+    # the weight tiles by bulk copies of the prepacked layout or by tensor copies of 16-byte rows: same bits
+    assert torch.equal(outs["gm_unet_conv3_tc"], outs["gm_unet_conv3_tc+wpack"])
     assert N.lib().gm_unet_conv3_tc_eligible(C.byref(a)) == 1
     assert N.lib().gm_unet_tc_status() == 0
     # the two tensor-core forms sum in different orders: agreement to BF16 rounding
@@ -96,6 +102,11 @@ def test_conv3_tc_slices_mask_and_data_gradient():
     rc, _ = _conv("gm_unet_conv3_tc", B, X, Y, Z, cout, cin, _cl(dy), cout, 0, WT, None, 0, dx, cin, 0, mirror=1)
     assert rc == N.GM_OK
     _close(_from_cl(dx, B, cin, Z, Y, X), xr.grad, 1e-2)
+    dx2 = torch.empty_like(dx)
+    wp = torch.empty(27 * cin * cout, dtype=torch.bfloat16, device="cuda")
+    rc, _ = _conv("gm_unet_conv3_tc", B, X, Y, Z, cout, cin, _cl(dy), cout, 0, WT, None, 0, dx2, cin, 0, mirror=1,
+                  wpack=wp)
+    assert rc == N.GM_OK and torch.equal(dx, dx2)
     assert N.lib().gm_unet_tc_status() == 0
 
 

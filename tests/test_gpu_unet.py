@@ -200,3 +200,33 @@ def test_unet_training_reduces_loss():
         losses.append(net.backward(target, lmask, 1.0 / target.numel()).item())
         net.step(lr=3e-3)
     assert losses[-1] < 0.3 * losses[0], losses[::10]
+
+
+@pytest.mark.parametrize("backward", [0, 1])
+def test_pool_up_vector_and_element_forms_agree(backward):
+    """Pooling and up-sampling, forward and backward: the 8-channel vector
+    form (aligned slices) and the element-wise form (a slice offset that is not
+    a multiple of 8 channels) give the same bits."""
+    import _native as N
+    import kern
+
+    torch.manual_seed(5)
+    B, Cn, X, Y, Z = 2, 16, 10, 6, 4
+    fine = B * X * Y * Z
+    grid = (C.c_int * 4)(B, X, Y, Z)
+    for entry in ("gm_unet_pool2", "gm_unet_up2"):
+        # the input lives on the fine grid for pool forward / up backward, on the coarse grid otherwise
+        src_fine = (entry == "gm_unet_pool2") != bool(backward)
+        nin, nout = (fine, fine // 8) if src_fine else (fine // 8, fine)
+        src = torch.randn(nin, Cn, device="cuda").to(torch.bfloat16)
+        a_in = torch.zeros(nin, Cn + 8, dtype=torch.bfloat16, device="cuda")
+        a_in[:, 8:] = src
+        b_in = torch.zeros(nin, Cn + 2, dtype=torch.bfloat16, device="cuda")
+        b_in[:, 2:] = src
+        a_out = torch.zeros(nout, Cn + 8, dtype=torch.bfloat16, device="cuda")
+        b_out = torch.zeros(nout, Cn + 2, dtype=torch.bfloat16, device="cuda")
+        N.call(entry, grid, Cn, a_in.data_ptr(), Cn + 8, 8, a_out.data_ptr(), Cn + 8, 8, backward, kern.stream_ptr())
+        N.call(entry, grid, Cn, b_in.data_ptr(), Cn + 2, 2, b_out.data_ptr(), Cn + 2, 2, backward, kern.stream_ptr())
+        torch.cuda.synchronize()
+        assert torch.equal(a_out[:, 8:], b_out[:, 2:]), entry
+        assert torch.all(a_out[:, :8] == 0) and torch.all(b_out[:, :2] == 0)
