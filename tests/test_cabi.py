@@ -57,6 +57,18 @@ def test_argument_validation_without_gpu(lib):
     assert lib.gm_couple(C.byref(cg), C.byref(p), None) == N.GM_ERR_ARG
     assert lib.gm_clamp_min(7, None, 0, 0.0, None) == N.GM_ERR_ARG
     assert lib.gm_clamp_min(N.GM_F32, 16, -1, 0.0, None) == N.GM_ERR_ARG
+    # two Level-3 steps a launch: the first step's arguments are checked as gm_level_step's, then
+    # the second step's dt, the phase buffers and the ring arrays, before any launch
+    b = N.gm_level2_args()
+    assert lib.gm_level_step2(C.byref(b), C.byref(p), None) == N.GM_ERR_ARG  # null T
+    b.level.T_in, b.level.T_out, b.level.dt = 16, 32, 8
+    b.level.nx = b.level.ny = b.level.nz = 4
+    b.level.ne_planes = 3
+    assert lib.gm_level_step2(C.byref(b), C.byref(p), None) == N.GM_ERR_ARG  # no dt2, phases, ring
+    assert lib.gm_level_step2(None, C.byref(p), None) == N.GM_ERR_ARG
+    s2 = N.gm_level_shape(1, 30, 4, 2, 6)  # kernel 1 is the one-step kernel's shape
+    assert lib.gm_level_step2_shape(C.byref(b), C.byref(p), C.byref(s2), None) == N.GM_ERR_ARG
+    assert lib.gm_level_autotune2(C.byref(b), C.byref(p), 0, None, None) == N.GM_ERR_ARG
 
 
 def test_launch_shape_and_batch_validation_without_gpu(lib):
