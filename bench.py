@@ -522,7 +522,7 @@ def run_ours(args):
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
     stream = torch.cuda.Stream(device=dev)
     vstart = np.asarray(cfg["properties"]["laser_center"], dtype=float)
-    need = (args.warmup + 2 * args.steps + 3) * n23
+    need = (args.warmup + 2 * args.steps + 4) * n23  # + the chunk whose rows are made ahead
     if len(rows) < need:
         raise SystemExit(f"toolpath too short: {len(rows)} rows < {need}")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -539,21 +539,42 @@ def run_ours(args):
         if args.pairs is not None:
             eng.use_pairs = bool(args.pairs)
         pairs = bool(eng.use_pairs) and persist == 0 and N.props_constant(eng.ps)
-        # toolpath rows generated on the device (FP64 accumulation) from the run table
-        tp = engine.DeviceToolpath(runs, dev, stream)
-        rows_buf = torch.empty(n23 * 7, dtype=torch.float64, device=dev)
-        dts_buf = torch.empty(N2 + 1, dtype=torch.float64, device=dev)
+        # toolpath rows generated on the device (FP64 accumulation) from the run table, on a side stream:
+        # the rows of chunk k+1 are made while step k runs (two row buffers; a buffer is refilled once the
+        # subcycle that read it has completed)
+        tstream = torch.cuda.Stream(device=dev)
+        tp = engine.DeviceToolpath(runs, dev, tstream)
+        rows_buf = [torch.empty(n23 * 7, dtype=torch.float64, device=dev) for _ in range(2)]
+        dts_buf = [torch.empty(N2 + 1, dtype=torch.float64, device=dev) for _ in range(2)]
+        buf_free = [None, None]  # event after the subcycle that last read buffer b
+        rows_ready = {}  # chunk -> event on the side stream
 
         def chunk(k):
             return rows[k * n23:(k + 1) * n23]
 
-        def device_step(k, plan=None):
-            """moveEverything + subcycleGOMELT of chunk k with its rows made on the device."""
+        def make_rows(k):
             if tp.emitted != k * n23:
                 raise SystemExit(f"toolpath generator at row {tp.emitted}, chunk {k} starts at {k * n23}")
-            tp.next(n23, N2, rows_buf, dts_buf)
+            b = k % 2
+            if buf_free[b] is not None:
+                tstream.wait_event(buf_free[b])
+            tp.next(n23, N2, rows_buf[b], dts_buf[b])
+            ev = torch.cuda.Event()
+            ev.record(tstream)
+            rows_ready[k] = ev
+
+        def device_step(k, plan=None):
+            """moveEverything + subcycleGOMELT of chunk k with its rows made on the device."""
+            if k not in rows_ready:
+                make_rows(k)
+            stream.wait_event(rows_ready.pop(k))
+            b = k % 2
             eng.move(chunk(k)[0], vstart, plan)  # the host plans the window move from its mirror of the path
-            eng.subcycle(None, rows_device=rows_buf, dts_device=dts_buf)
+            eng.subcycle(None, rows_device=rows_buf[b], dts_device=dts_buf[b])
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            buf_free[b] = ev
+            make_rows(k + 1)  # the next chunk's rows, overlapping this step
 
         k = 0
         for _ in range(args.warmup):
