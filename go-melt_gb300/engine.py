@@ -233,8 +233,9 @@ class Engine:
         # (gm_level3_persist, where the window has a shape), 2 the one-step kernel's body with grid barriers
         # (gm_level3_steps); constant-property materials only
         self.use_persist = 0
-        # with one launch a step: the Level-3 steps two at a time (gm_level_step2; constant-property materials)
-        self.use_pairs = True
+        # with one launch a step: the Level-3 steps two at a time (gm_level_step2; constant-property
+        # materials); autotune() turns it on where the pair measures faster than two single steps
+        self.use_pairs = False
         self.status = torch.zeros(1, dtype=torch.int32, device=self.dev)  # GM_PERSIST_* bits of the device kernels
         self.last_table_bytes = 0  # bytes of the last move's table upload
         self.substrate = g.substrate()
