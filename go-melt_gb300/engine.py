@@ -23,7 +23,7 @@ import torch
 
 import _native as N
 import kern
-from geometry import axis_map, couple_axis
+from geometry import _Cache, axis_map, couple_axis
 from levels import Geometry
 
 PH_S1, PH_S2 = 1, 2
@@ -197,6 +197,42 @@ class DeviceToolpath:
         return int(raw[0]), int(raw[1]), int(raw[2]), float(f[3]), float(f[4]), float(f[5])
 
 
+_INJECT_AXES = _Cache()
+
+
+def _inject_axis(fine_c, fine_n, overlap_c, overlap_i, coarse_c):
+    """One axis of Engine._inject: (cf0, cf1, c_of_f) as int32 arrays, or
+    False when the overlap coordinates do not all coincide with fine nodes.
+    Memoised on the exact inputs (a raster move changes one axis); the cached
+    arrays are read-only."""
+    fc = np.asarray(fine_c, dtype=np.float64)
+    oc = np.asarray(overlap_c, dtype=np.float64)
+    ci = np.asarray(overlap_i, dtype=np.int64)
+    cc = np.asarray(coarse_c, dtype=np.float64)
+    key = (fc.tobytes(), oc.tobytes(), ci.tobytes(), cc.tobytes(), int(fine_n))
+    hit = _INJECT_AXES.get(key)
+    if hit is not None:
+        return hit
+    m = axis_map(fc, oc)
+    e = np.asarray(m.elem, dtype=np.int64)
+    w = np.asarray(m.w)
+    at0, at1 = np.abs(w[:, 1]) <= 1e-9, np.abs(w[:, 0]) <= 1e-9
+    nc = len(cc)
+    r = False
+    if np.all(at0 | at1):
+        f = np.where(at0, e, e + 1)
+        if not (f.min() < 0 or f.max() >= fine_n or ci.min() < 0 or ci.max() >= nc):
+            foc = np.full(nc, -1, dtype=np.int64)  # coarse index -> coinciding fine index
+            foc[ci] = f
+            b = np.full(int(fine_n), -1, dtype=np.int32)
+            b[f] = ci
+            ce = np.asarray(axis_map(cc, fc).elem, dtype=np.int64)  # as cmap
+            r = (foc[ce].astype(np.int32), foc[ce + 1].astype(np.int32), b)
+            for x in r:
+                x.setflags(write=False)
+    return _INJECT_AXES.put(key, r)
+
+
 class MovePlan:
     """Host half of one window move (see Engine.plan_move)."""
 
@@ -285,27 +321,11 @@ class Engine:
         restriction of the fine level at the coarse overlap nodes is an
         injection (each overlap coordinate coincides with a fine node: weights
         0 / 1 within 1e-9), else None."""
-        cf0, cf1, cof = [], [], []
-        for d in range(3):
-            m = axis_map(fine_coords[d], overlap_coords[d])
-            e = np.asarray(m.elem, dtype=np.int64)
-            w = np.asarray(m.w)
-            at0, at1 = np.abs(w[:, 1]) <= 1e-9, np.abs(w[:, 0]) <= 1e-9
-            if not np.all(at0 | at1):
-                return None
-            f = np.where(at0, e, e + 1)
-            ci = np.asarray(overlap_idx[d], dtype=np.int64)
-            nc = len(coarse_coords[d])
-            if f.min() < 0 or f.max() >= fine_nodes[d] or ci.min() < 0 or ci.max() >= nc:
-                return None
-            foc = np.full(nc, -1, dtype=np.int64)  # coarse index -> coinciding fine index
-            foc[ci] = f
-            b = np.full(int(fine_nodes[d]), -1, dtype=np.int32)
-            b[f] = ci
-            ce = np.asarray(axis_map(coarse_coords[d], fine_coords[d]).elem, dtype=np.int64)  # as cmap
-            cf0.append(foc[ce].astype(np.int32))
-            cf1.append(foc[ce + 1].astype(np.int32))
-            cof.append(b)
+        axes = [_inject_axis(fine_coords[d], fine_nodes[d], overlap_coords[d], overlap_idx[d], coarse_coords[d])
+                for d in range(3)]
+        if any(r is False for r in axes):
+            return None
+        cf0, cf1, cof = ([r[q] for r in axes] for q in range(3))
         return [C.cast(self.arena.put(x, np.int32), C.POINTER(C.c_int)) for x in cf0 + cf1 + cof]
 
     def _idx_tensor(self, arrs, nodes, what):
