@@ -1237,7 +1237,8 @@ def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
     subcycle calls issued one instance after another (each as its own CUDA
     graph) or as ONE graph of parallel branches (gm_subcycle_batched).  Scan
     throughput over all instances, GPU time of the subcycles alone and wall
-    time per step (host planning of the 64 window moves included)."""
+    time per step (host planning of the window moves included, overlapped
+    with the previous step's device work)."""
     import numpy as np
     import torch
 
@@ -1258,15 +1259,19 @@ def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
         raise SystemExit(f"toolpath too short for the batched subcycles: {nchunk} Level-1 steps")
     i = 0
     for mode in ("per_instance", "batched", "per_instance", "batched"):  # the first pair warms up
-        t_gpu, t_wall, dist = 0.0, 0.0, 0.0
-        for _ in range(K):
-            k = first_chunk + i % (nchunk - first_chunk)
-            i += 1
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            with torch.cuda.stream(stream):
-                for e, r, v in zip(engs, rows, vst):
-                    e.move(r[k * 100], v)
+        # step k's window moves are planned on the host while the device runs step k - 1 (as the e2e
+        # loop of the headline does); a plan is made only for a step that then runs
+        ks = [first_chunk + (i + q) % (nchunk - first_chunk) for q in range(K)]
+        i += K
+        dist = sum(mm(k) for k in ks)
+        ev = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            plans = [e.plan_move(r[ks[0] * 100], v) for e, r, v in zip(engs, rows, vst)]
+            for q, k in enumerate(ks):
+                for e, r, v, pl in zip(engs, rows, vst, plans):
+                    e.move(r[k * 100], v, pl)
                 s, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 s.record(stream)
                 if mode == "batched":
@@ -1275,10 +1280,12 @@ def batched_subcycles(engs, inst, stream, K=5, first_chunk=2):
                     for e, r in zip(engs, rows):
                         e.subcycle(r[k * 100:(k + 1) * 100])
                 e_.record(stream)
-            torch.cuda.synchronize()
-            t_wall += time.perf_counter() - t0
-            t_gpu += s.elapsed_time(e_) * 1e-3
-            dist += mm(k)
+                ev.append((s, e_))
+                if q + 1 < len(ks):
+                    plans = [e.plan_move(r[ks[q + 1] * 100], v) for e, r, v in zip(engs, rows, vst)]
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t0
+        t_gpu = sum(s.elapsed_time(e_) for s, e_ in ev) * 1e-3
         out[mode] = {"subcycle_gpu_ms_per_step": 1e3 * t_gpu / K, "wall_ms_per_step": 1e3 * t_wall / K,
                      "scan_mm_per_s_wall": dist / t_wall, "scan_mm_per_s_subcycle_gpu": dist / t_gpu,
                      "gnode_steps_per_s_subcycle_gpu": node_steps * K / t_gpu / 1e9}
