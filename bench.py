@@ -853,7 +853,8 @@ def surrogate_block(args, cfg, dev, plain_ms_per_l2):
     inst = workloads.batched_instances(n=16)
     snaps, t_gen = SR.generate(inst, dev, cap=4000)
     net = surrogate.UNet(dev, seed=0)
-    losses, t_train = SR.train(net, snaps, [81, 81, 21], (80, 80, 20), args.surrogate_steps, 4, 1e-3, dev)
+    losses, t_train = SR.train(net, snaps, [81, 81, 21], (80, 80, 20), args.surrogate_steps, 4, 1e-3, dev,
+                               log_every=args.surrogate_steps)
     st = SR.evaluate(net, cfg, dev, nsteps=2)
     X, Y, Z = 160, 160, 40
     x = torch.zeros(X * Y * Z, 16, dtype=torch.bfloat16, device=dev)
@@ -877,7 +878,8 @@ def surrogate_block(args, cfg, dev, plain_ms_per_l2):
     return {
         "what": "Level-3 surrogate per Level-2 step on the part-scale raster (plain subcycle as fallback)",
         "train": {"snapshots": snaps.n, "instances": len(inst), "steps": args.surrogate_steps, "batch": 4,
-                  "seconds": t_train, "loss_last": losses[-1][1] if losses else None},
+                  "seconds": t_train, "loss_first": losses[0][1] if losses else None,
+                  "loss_last": losses[-1][1] if losses else None},
         "eval_level2_steps": st["total"], "accepted_frac": st["accepted"] / max(st["total"], 1),
         "max_err_K_median": med(st["max_err"]), "rms_err_K_median": med(st["rms_err"]),
         "energy_residual_median": med(st["residual"]),
