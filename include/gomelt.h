@@ -29,7 +29,7 @@ enum gm_status_code {
   GM_ERR_ARG = 1,         /* invalid argument (null pointer, size, dtype) */
   GM_ERR_LAUNCH = 2,      /* kernel launch failed */
   GM_ERR_CUDA = 3,        /* other CUDA runtime error */
-  GM_ERR_UNSUPPORTED = 4, /* configuration outside what this build handles */
+  GM_ERR_UNSUPPORTED = 4, /* configuration the library does not handle */
   GM_ERR_TOO_LARGE = 5    /* request exceeds a fixed capacity */
 };
 

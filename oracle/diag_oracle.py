@@ -1,9 +1,9 @@
-"""CPU definitions of the diagnostics that the GB300 build reports beside its
+"""CPU definitions of the diagnostics that the GB300 implementation reports beside its
 results: energy balance of a level window over an interval, melt-pool extent
 at an isotherm, max / RMS field difference.
 
 TEST INFRASTRUCTURE (like ``gomelt_oracle``): used by ``tests/`` only, as the
-checker of the device reductions in ``go-melt_gb300/csrc/gm_diag.cu``.  The
+expected values of the device reductions in ``go-melt_gb300/csrc/gm_diag.cu``.  The
 reference has no counterpart of these quantities; they are assembled here
 from the oracle's restatements of the reference's own operators
 (``solveMatrixFreeFE`` lumped mass and stiffness, ``computeSourcesL3``,

@@ -1,7 +1,7 @@
 """CPU oracle: NumPy FP64 restatement of GO-MELT's multilevel explicit thermal step.
 
 TEST INFRASTRUCTURE.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
-legs of ``bench.py`` use this module, and only as the checker / CPU baseline;
+legs of ``bench.py`` use this module, and only as the expected values / CPU baseline;
 the product (``go-melt_gb300/``) never imports it.
 
 Each function restates the reference function of the same name in

@@ -1,6 +1,6 @@
 """Smoke check used by __graft_entry__.smoke(): one small moveEverything +
 subcycleGOMELT on the GPU engine against the NumPy oracle (test
-infrastructure; the oracle is the checker here, not the thing measured)."""
+infrastructure; the oracle gives the expected values here, it is not the thing measured)."""
 
 from __future__ import annotations
 

@@ -12,7 +12,7 @@ golden vector of their own; they are compared with the oracle's restatement,
 which tests/test_oracle_golden.py pins to the reference.
 
 Tolerances: FP64 1e-10 and FP32 1e-4 relative to the largest magnitude of
-the reference vector (the benchmark spec's FP32 bar).
+the reference vector (the FP32 bar: 1e-4 relative max temperature).
 """
 
 import json

@@ -14,7 +14,7 @@ single-track workload and on the real part-scale Level-3 window.
 
 The GPU runs with the launch shapes Engine.autotune measures (as the bench
 does) and each subcycle call as one CUDA graph.  Bars: FP64 1e-10 and FP32
-1e-4 relative max temperature per level (the benchmark spec's FP32 bar); T' to
+1e-4 relative max temperature per level (the FP32 correctness bar); T' to
 the same bars relative to the peak temperature; phases and melt time exactly
 (FP64) or on all but a few threshold-straddling nodes (FP32: a node within
 rounding of T_liquidus may flip).
