@@ -64,3 +64,26 @@ def test_reference_arm_runs_on_rank_zero_only(rank):
                         "--steps", "1", "--warmup", "1"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""  # the other ranks exit 0 without work or output
+
+
+def test_reference_arm_line_on_rank_zero():
+    """Rank 0 of the reference arm prints one JSON line with the GPU arm's
+    metric, unit and config, the CPU sample described in cpu_baseline and an
+    e2e block of the line's own value with no host-device bytes."""
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [s for s in r.stdout.splitlines() if s.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 1
+    assert d["metric"] == bench.METRIC and d["config"] == bench.bench_config(1)
+    assert d["unit"] == "mm/s" and d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
